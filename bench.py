@@ -1,0 +1,395 @@
+"""Benchmark: particle-substeps/s of the MPM substep on one GB300.
+
+Workload (default): the 1M-particle three-box scene on a sparse 4^3-block grid
+over a 256^3 domain (fixed-corotated, snow and Drucker-Prager sand boxes,
+dt = 5e-5), synthetic and seeded.  A "step" is one substep over all particles.
+
+  value        particle-substeps/s with the state resident in HBM (CUDA events
+               around K substeps on the library's stream)
+  e2e          the same metric through the C ABI with host buffers: per e2e step
+               sv_create (host->device upload of the state), one frame of
+               substeps (1/24 s of simulated time), sv_download (device->host)
+  roofline     the dominant kernel's algorithmic bytes per launch / its average
+               CUDA-event duration, against the measured HBM copy bandwidth
+  cpu_baseline the CPU oracle (the reference substep restated in C++, fp32,
+               all host threads) on a bounded sample of the same scene
+
+--impl reference runs only the CPU restatement of the reference substep (the
+reference itself is Rust and cannot be built here) on the same scene.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-substeps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scene", default="three_boxes_1m")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bound on the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(scene, seconds_budget: float):
+    """Times the CPU oracle (fp32, all host threads) on the full scene for as
+    many substeps as fit the time budget (at least one)."""
+    import oracle
+
+    threads = os.cpu_count() or 1
+    o = oracle.OracleState(scene.io_state.particles, scene.consts, scene.extras, fp64=False, threads=threads)
+    n = scene.io_state.particles.n
+    done = 0
+    t0 = time.perf_counter()
+    while True:
+        o.step(1, scene.dt, scene.gravity)
+        done += 1
+        if time.perf_counter() - t0 > seconds_budget or done >= scene.substeps:
+            break
+    dt = time.perf_counter() - t0
+    o.close()
+    return {
+        "value": n * done / dt,
+        "unit": METRIC,
+        "cores": threads,
+        "kind": "port",
+        "sample": f"{done} substeps of the full {n}-particle scene (first substeps from the initial state), "
+                  f"{dt:.1f} s, fp32 C++ restatement of the reference CPU substep",
+    }
+
+
+def algorithmic_bytes(kernel: str, live: int, grid_nodes: int, cell_form: bool):
+    """Algorithmic HBM bytes per launch (SURVEY 8d per-unit figures)."""
+    x = 12 + (12 if cell_form else 0)
+    if kernel == "p2g":
+        # read x, v, C, F, material/flags; write grid m + p per active node
+        return live * (x + 12 + 36 + 36 + 4) + grid_nodes * 16
+    if kernel == "g2p":
+        # read x, F, material/flags and grid v; write x, v, C, F
+        return live * (x + 36 + 4) + grid_nodes * 12 + live * (x + 12 + 36 + 36)
+    if kernel == "grid_update":
+        return grid_nodes * (16 + 12)
+    if kernel == "radix_sort":
+        return live * 16  # key + index written and read once
+    return None
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    from squishy_volumes_gb300 import CudaState, FrameInput, Harness, RunParameters, scenes
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    scene = scenes.SCENES[args.scene]()
+    p = scene.io_state.particles
+    n = p.n
+    gpu = CudaState.from_io_state(scene.io_state, scene.consts, scene.extras)
+    # warm-up
+    status, done = gpu.step(args.warmup, scene.dt, scene.gravity)
+    if status:
+        raise RuntimeError(f"warm-up status {status:#x}")
+    torch.cuda.synchronize()
+    stats0 = gpu.stats()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    # timed region: K substeps queued on a torch stream handed to the
+    # library, bracketed by CUDA events recorded on that same stream
+    stream = torch.cuda.Stream(device=dev)
+    gpu.set_stream(stream.cuda_stream)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        status, done = gpu.step(args.steps, scene.dt, scene.gravity)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    elapsed = ev0.elapsed_time(ev1) * 1e-3
+    stats1 = gpu.stats()
+    if status or done != args.steps:
+        raise RuntimeError(f"timed run status {status:#x}, done {done}")
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    live = stats1["live_particles"]
+    value = live * args.steps * world / elapsed
+    launches = stats1["kernel_launches"] - stats0["kernel_launches"]
+
+    # per-kernel durations: the same K substeps again with CUDA events around
+    # every kernel group on the library's stream
+    gpu.set_profiling(True)
+    gpu.step(args.steps, scene.dt, scene.gravity)
+    prof = json.loads(gpu.profile_report())
+    gpu.set_profiling(False)
+    st = gpu.stats()
+    grid_nodes = st["grid_blocks"] * 64
+    total_ms = sum(v["ms"] for v in prof.values())
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])[0]
+    hbm, peak_kind = measured_peaks()
+    cell_form = scene.extras.position_form == 1
+    alg = algorithmic_bytes(dom, live, grid_nodes, cell_form)
+    avg_ms = prof[dom]["ms"] / prof[dom]["launches"]
+    achieved = alg / (avg_ms * 1e-3) / 1e9 if alg else None
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get(args.scene, {}).get(dom)
+        except Exception:
+            traffic = None
+    roofline = {
+        "kernel": dom,
+        "bound": "hbm",
+        "achieved": round(achieved, 1) if achieved else None,
+        "peak": hbm,
+        "peak_kind": peak_kind,
+        "unit": "GB/s",
+        "frac": round(achieved / hbm, 4) if achieved else None,
+        "traffic": traffic,
+        "share": round(prof[dom]["ms"] / total_ms, 4),
+        "kernels_ms_per_substep": {k: round(v["ms"] / args.steps, 5) for k, v in prof.items()},
+    }
+    # whole-substep roofline with the SURVEY 8d per-particle-substep figure
+    rho = grid_nodes / max(live, 1)
+    bps = 212 + (24 if cell_form else 0) + 56 * rho
+    sub_achieved = bps * live * args.steps / elapsed / 1e9 * world
+    roofline["substep"] = {
+        "bytes_per_particle_substep": round(bps, 1),
+        "achieved": round(sub_achieved, 1),
+        "frac": round(sub_achieved / hbm, 4),
+    }
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        fps = scene.consts.frames_per_second
+        frame_substeps = int(math.ceil((1.0 / fps) / scene.dt))
+        frame_substeps = min(frame_substeps, scene.substeps)
+        reps = 2
+        h2d = p.nbytes()
+        d2h = 0
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            st_ = CudaState.from_io_state(scene.io_state, scene.consts, scene.extras)
+            params = RunParameters(target_time=frame_substeps * scene.dt * (1 - 1e-9), max_time_step=scene.dt)
+            io, err = st_.produce_next_state(Harness(), FrameInput(scene.consts, scene.gravity), params)
+            d2h = sum(getattr(io.particles, k).nbytes for k in
+                      ("flags", "positions", "position_gradients", "velocities", "velocity_gradients",
+                       "elastic_energies", "collider_bits", "plastic_j"))
+            st_.close()
+        t1 = time.perf_counter()
+        e2e = {
+            "value": n * frame_substeps * reps / (t1 - t0),
+            "unit": METRIC,
+            "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h),
+            "substeps_per_step": frame_substeps,
+            "step": "sv_create (upload) + one frame of substeps + sv_download",
+        }
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        gpu.close()
+        cpu = cpu_baseline(scene, args.cpu_seconds)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": METRIC,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded jittered boxes)",
+        "config": {
+            "workload": args.scene,
+            "particles": n,
+            "live_particles": live,
+            "grid_blocks": st["grid_blocks"],
+            "substep_dt": scene.dt,
+            "l2": "state larger than L2 (no flush)",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+        },
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "fp64_svd_particles": st["fp64_svd"],
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from squishy_volumes_gb300 import scenes
+
+    scene = scenes.SCENES[args.scene]()
+    n = scene.io_state.particles.n
+    import oracle
+
+    threads = os.cpu_count() or 1
+    o = oracle.OracleState(scene.io_state.particles, scene.consts, scene.extras, fp64=False, threads=threads)
+    # each step is one substep of the full scene; the step count is bounded
+    # so the run stays within a few minutes
+    warm = min(args.warmup, 2)
+    steps = max(1, min(args.steps, 5))
+    o.step(warm, scene.dt, scene.gravity)
+    t0 = time.perf_counter()
+    o.step(steps, scene.dt, scene.gravity)
+    el = time.perf_counter() - t0
+    o.close()
+    v = n * steps / el
+    line = {
+        "metric": METRIC,
+        "value": v,
+        "unit": METRIC,
+        "impl": "reference",
+        "n_gpus": world,
+        "steps": steps,
+        "warmup": warm,
+        "ms_per_step": el / steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded jittered boxes)",
+        "config": {"workload": args.scene, "particles": n, "substep_dt": scene.dt},
+        "cpu_baseline": {
+            "value": v,
+            "unit": METRIC,
+            "cores": threads,
+            "kind": "port",
+            "sample": f"{steps} substeps of the full scene after {warm} warm-up substeps; the reference is Rust "
+                      "(no cargo/rustc here), so this is its CPU substep restated in C++ (oracle/)",
+        },
+        "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,195 @@
+/*
+ * squishy_volumes_cuda.h -- C ABI of the GB300 MPM substep library
+ * (libsquishy_volumes_cuda.so).
+ *
+ * It replaces the CPU backend of Squishy Volumes behind the backend switch
+ * rust/crates/core/src/compute_thread.rs:101-117 (`enum ComputeState`):
+ *
+ *   reference call                                          | entry point here
+ *   --------------------------------------------------------+---------------------------
+ *   CpuState::from_io_state (cpu/src/cpu_state.rs:25-66)    | sv_create
+ *   CpuState::produce_next_state (cpu/src/cpu_state.rs:146-197),
+ *     its substep loop :167-194 with adaptive_time_steps off | sv_step
+ *   CpuState::to_io_state (cpu/src/cpu_state.rs:68-135)     | sv_download, sv_download_grid
+ *   drop(CpuState)                                          | sv_destroy
+ *   error Display (cpu/src/errors.rs:9-36)                  | sv_last_error_string
+ *
+ * Conventions
+ *  - Plain pointers and sizes; no callbacks.  The caller owns every host
+ *    buffer; the handle owns all device memory.
+ *  - Return value: 0 = success, negative = fatal (CUDA error, out of memory,
+ *    invalid argument); the message is in sv_last_error_string() (per thread).
+ *  - sv_step reports physics outcomes in *status_out as a bit mask that
+ *    mirrors the reference GPU status word (rust/crates/gpu/src/status.rs:27-30):
+ *    SV_STATUS_PARTICLE_INVERTED means a particle reached det F <= 0 and got
+ *    the FAILED flag; like the reference's EnergyError the state is still
+ *    valid and should be stored (compute_thread.rs:165-169).
+ *  - One handle is driven from one host thread at a time (the reference calls
+ *    its backend from its single compute thread, compute_thread.rs:78).
+ *  - Particle arrays follow rust/crates/file_frame/src/particles.rs:92-109:
+ *    positions [n][3], position_gradients [n][9] column-major (nalgebra),
+ *    velocities [n][3], velocity_gradients [n][9], flags u32 (ParticleFlags,
+ *    :21-33), and ParticleParameters (:55-90) spread into per-particle arrays.
+ */
+#ifndef SQUISHY_VOLUMES_CUDA_H
+#define SQUISHY_VOLUMES_CUDA_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ParticleFlags, rust/crates/file_frame/src/particles.rs:21-33. */
+#define SV_IS_SOLID (1u << 0)
+#define SV_IS_FLUID (1u << 1)
+#define SV_USE_VISCOSITY (1u << 2)
+#define SV_USE_SAND_ALPHA (1u << 3)
+#define SV_HAS_GOAL (1u << 4)
+#define SV_TOMBSTONED (1u << 5)
+#define SV_FAILED (1u << 6)
+
+/* Status bits of sv_step (rust/crates/gpu/src/status.rs:27-30 meaning). */
+#define SV_STATUS_CAPACITY_EXCEEDED (1u << 0) /* grid block capacity too small */
+#define SV_STATUS_PARTICLE_INVERTED (1u << 3) /* det F <= 0: FAILED set */
+#define SV_STATUS_CANCELED (1u << 8)          /* cancel flag seen between substeps */
+
+/* Material models.  SV_MODEL_REFERENCE selects what the reference does from
+ * the flags: Neo-Hookean solid (plus the sand return map with
+ * SV_USE_SAND_ALPHA) or the inviscid fluid.  The other two are additions
+ * that the reference does not have. */
+#define SV_MODEL_REFERENCE 0u
+#define SV_MODEL_FIXED_COROTATED 1u
+#define SV_MODEL_SNOW 2u
+
+typedef struct sv_consts {
+    /* InputConsts::scaled_grid_node_size / scaled_domain_{min,max}
+     * (rust/crates/file_input/src/header.rs:36-58) */
+    float grid_node_size;
+    float domain_min[3];
+    float domain_max[3];
+    /* Addition (not in the reference): a grid boundary plane on axis
+     * ground_axis at ground_height; 0 = off, 1 = sticky, 2 = slip. */
+    int32_t ground_mode;
+    int32_t ground_axis;
+    float ground_height;
+    /* Addition: 0 = fp32 positions; 1 = int32 cell index + fp32 in-cell offset. */
+    uint32_t position_form;
+    /* When the fp32 3x3 SVD is redone in fp64: 0 = never, 1 = det F < 0.05
+     * (default), 2 = det F < 0.05 or min singular-value gap < 1e-4. */
+    uint32_t svd_fp64_policy;
+    /* Grid block (4^3 nodes) capacity; 0 = size it from the domain. */
+    uint64_t block_capacity;
+    uint32_t reserved[6];
+} sv_consts;
+
+typedef struct sv_particles {
+    uint64_t n;
+    uint32_t *flags;
+    float *positions;
+    float *position_gradients;
+    float *velocities;
+    float *velocity_gradients;
+    float *elastic_energies;       /* may be NULL */
+    uint32_t *collider_bits;       /* may be NULL (all 0) */
+    /* ParticleParameters (read by sv_create only) */
+    const float *mass;
+    const float *initial_volume;
+    const float *viscosity_dynamic; /* NULL unless some particle has SV_USE_VISCOSITY */
+    const float *viscosity_bulk;
+    const float *mu;               /* solids */
+    const float *lambda;
+    const float *sand_alpha;       /* NULL unless some particle has SV_USE_SAND_ALPHA */
+    const int32_t *exponent;       /* fluids */
+    const float *bulk_modulus;
+    /* additions (NULL = all SV_MODEL_REFERENCE) */
+    const uint32_t *model;
+    const float *hardening;        /* snow xi */
+    const float *crit_compression; /* snow theta_c */
+    const float *crit_stretch;     /* snow theta_s */
+    float *plastic_j;              /* snow hardening state J_p (in and out), may be NULL */
+} sv_particles;
+
+typedef struct sv_handle sv_handle;
+
+/* CpuState::from_io_state (cpu/src/cpu_state.rs:25-66): uploads the particles
+ * and sizes the sparse grid.  Fails on invalid flags (neither or both of
+ * IS_SOLID/IS_FLUID, like core/src/initialization.rs:197-201), on a domain
+ * whose dense block index exceeds 2^26 blocks, or on a CUDA error. */
+int sv_create(const sv_consts *consts, const sv_particles *particles, sv_handle **out);
+
+/* The substep loop of CpuState::produce_next_state (cpu_state.rs:167-194)
+ * with adaptive_time_steps = false: n_substeps substeps of size dt with the
+ * given (already interpolated) gravity.  `cancel` may be NULL; when it points
+ * at a nonzero value between substeps, the call stops (Harness::check,
+ * xpu/src/harness.rs:69-75) and reports SV_STATUS_CANCELED.  The number of
+ * substeps completed is written to *substeps_done when that is not NULL. */
+int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
+            const volatile int32_t *cancel, uint32_t *status_out, uint32_t *substeps_done);
+
+/* CpuState::to_io_state (cpu_state.rs:68-135): particle state in the
+ * caller's original order.  Only the mutable arrays of `out` are written
+ * (flags, positions, position_gradients, velocities, velocity_gradients,
+ * elastic_energies, collider_bits, plastic_j); NULL arrays are skipped. */
+int sv_download(sv_handle *h, sv_particles *out);
+
+/* The grid of the most recent substep (to_io_state's store_grid part):
+ * nodes with mass > 0, sorted by node id (i, j, k).  Writes up to `capacity`
+ * entries; *count gets the total. */
+int sv_download_grid(sv_handle *h, int32_t *node_ids, float *masses, float *velocities,
+                     uint64_t capacity, uint64_t *count);
+
+void sv_destroy(sv_handle *h);
+
+/* Message of the last failure on this thread ("" if none). */
+const char *sv_last_error_string(void);
+
+/* ---- inspection entry points used by the parity tests and the benchmark ---- */
+
+/* Runs the first half of one substep (binning sort, external force, P2G,
+ * grid update) on the current state without changing particle state; the
+ * grid is then readable with sv_download_grid. */
+int sv_p2g_only(sv_handle *h, float dt, const float gravity[3]);
+
+/* Binning keys of the current particles (in device order) and the stable
+ * sort permutation of those keys.  Key contract:
+ * c = floor(x / dx - 0.5) in fp32, lc = c - origin,
+ * key = (((lc.x>>2)*nb.y + (lc.y>>2))*nb.z + (lc.z>>2)) << 6
+ *       | (lc.x&3)<<4 | (lc.y&3)<<2 | (lc.z&3), 0xFFFFFFFF when tombstoned.
+ * Also returns the original particle index of each device slot. */
+int sv_binning(sv_handle *h, uint32_t *keys, uint32_t *perm, uint32_t *original_index);
+
+/* Grid layout: node origin and block counts of the dense block index. */
+int sv_grid_layout(sv_handle *h, int32_t origin[3], int32_t nblocks[3]);
+
+/* Stable LSD radix sort of n (key, index) pairs on the device: writes the
+ * permutation that stably sorts `keys` (host buffers; allocates device
+ * memory per call). */
+int sv_sort_pairs(const uint32_t *keys, uint32_t *perm, uint64_t n);
+
+typedef struct sv_stats {
+    uint64_t particles;
+    uint64_t live_particles;
+    uint64_t particle_blocks;   /* occupied 4^3 blocks in the last substep */
+    uint64_t grid_blocks;       /* active grid blocks in the last substep */
+    uint64_t fp64_svd;          /* particles that took the fp64 SVD, summed over substeps */
+    uint64_t substeps;
+    uint64_t device_bytes;      /* device memory held by the handle */
+    uint64_t kernel_launches;   /* kernels launched by this handle so far */
+} sv_stats;
+int sv_get_stats(sv_handle *h, sv_stats *out);
+
+/* Runs the handle's work on a caller-owned CUDA stream (a cudaStream_t passed
+ * as void*; NULL returns to the handle's own stream).  The previous stream is
+ * synchronised first; the caller keeps ownership of its stream. */
+int sv_set_stream(sv_handle *h, void *stream);
+
+/* Per-kernel timing with CUDA events on the handle's stream (off by
+ * default).  sv_profile_report writes a JSON object
+ * {"kernel": {"launches": L, "ms": T}, ...} and returns its length. */
+int sv_set_profiling(sv_handle *h, int enable);
+int sv_profile_report(sv_handle *h, char *buffer, uint64_t capacity);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

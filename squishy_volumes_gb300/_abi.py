@@ -1,0 +1,151 @@
+"""ctypes view of the C ABI in include/squishy_volumes_cuda.h.
+
+The shared library is the product; this module only declares its structs and
+signatures.  Loading fails loudly when the library has not been built: there
+is no fallback implementation.
+"""
+
+from __future__ import annotations
+
+import ctypes as ct
+import os
+from pathlib import Path
+
+from . import build as _build
+
+u32p = ct.POINTER(ct.c_uint32)
+i32p = ct.POINTER(ct.c_int32)
+f32p = ct.POINTER(ct.c_float)
+
+SV_IS_SOLID = 1 << 0
+SV_IS_FLUID = 1 << 1
+SV_USE_VISCOSITY = 1 << 2
+SV_USE_SAND_ALPHA = 1 << 3
+SV_HAS_GOAL = 1 << 4
+SV_TOMBSTONED = 1 << 5
+SV_FAILED = 1 << 6
+
+SV_STATUS_CAPACITY_EXCEEDED = 1 << 0
+SV_STATUS_PARTICLE_INVERTED = 1 << 3
+SV_STATUS_CANCELED = 1 << 8
+
+SV_MODEL_REFERENCE = 0
+SV_MODEL_FIXED_COROTATED = 1
+SV_MODEL_SNOW = 2
+
+
+class SvConsts(ct.Structure):
+    _fields_ = [
+        ("grid_node_size", ct.c_float),
+        ("domain_min", ct.c_float * 3),
+        ("domain_max", ct.c_float * 3),
+        ("ground_mode", ct.c_int32),
+        ("ground_axis", ct.c_int32),
+        ("ground_height", ct.c_float),
+        ("position_form", ct.c_uint32),
+        ("svd_fp64_policy", ct.c_uint32),
+        ("block_capacity", ct.c_uint64),
+        ("reserved", ct.c_uint32 * 6),
+    ]
+
+
+class SvParticles(ct.Structure):
+    _fields_ = [
+        ("n", ct.c_uint64),
+        ("flags", u32p),
+        ("positions", f32p),
+        ("position_gradients", f32p),
+        ("velocities", f32p),
+        ("velocity_gradients", f32p),
+        ("elastic_energies", f32p),
+        ("collider_bits", u32p),
+        ("mass", f32p),
+        ("initial_volume", f32p),
+        ("viscosity_dynamic", f32p),
+        ("viscosity_bulk", f32p),
+        ("mu", f32p),
+        ("lambda_", f32p),
+        ("sand_alpha", f32p),
+        ("exponent", i32p),
+        ("bulk_modulus", f32p),
+        ("model", u32p),
+        ("hardening", f32p),
+        ("crit_compression", f32p),
+        ("crit_stretch", f32p),
+        ("plastic_j", f32p),
+    ]
+
+
+class SvStats(ct.Structure):
+    _fields_ = [
+        ("particles", ct.c_uint64),
+        ("live_particles", ct.c_uint64),
+        ("particle_blocks", ct.c_uint64),
+        ("grid_blocks", ct.c_uint64),
+        ("fp64_svd", ct.c_uint64),
+        ("substeps", ct.c_uint64),
+        ("device_bytes", ct.c_uint64),
+        ("kernel_launches", ct.c_uint64),
+    ]
+
+
+_SIGNATURES = {
+    "sv_create": (ct.c_int, [ct.POINTER(SvConsts), ct.POINTER(SvParticles), ct.POINTER(ct.c_void_p)]),
+    "sv_step": (
+        ct.c_int,
+        [ct.c_void_p, ct.c_uint32, ct.c_float, f32p, ct.POINTER(ct.c_int32), u32p, u32p],
+    ),
+    "sv_download": (ct.c_int, [ct.c_void_p, ct.POINTER(SvParticles)]),
+    "sv_download_grid": (ct.c_int, [ct.c_void_p, i32p, f32p, f32p, ct.c_uint64, ct.POINTER(ct.c_uint64)]),
+    "sv_destroy": (None, [ct.c_void_p]),
+    "sv_last_error_string": (ct.c_char_p, []),
+    "sv_p2g_only": (ct.c_int, [ct.c_void_p, ct.c_float, f32p]),
+    "sv_binning": (ct.c_int, [ct.c_void_p, u32p, u32p, u32p]),
+    "sv_grid_layout": (ct.c_int, [ct.c_void_p, i32p, i32p]),
+    "sv_sort_pairs": (ct.c_int, [u32p, u32p, ct.c_uint64]),
+    "sv_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(SvStats)]),
+    "sv_set_stream": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "sv_set_profiling": (ct.c_int, [ct.c_void_p, ct.c_int]),
+    "sv_profile_report": (ct.c_int, [ct.c_void_p, ct.c_char_p, ct.c_uint64]),
+}
+
+_lib = None
+
+
+def library_path() -> Path:
+    return Path(os.environ.get("SQUISHY_VOLUMES_CUDA_LIB", str(_build.library_path())))
+
+
+def load() -> ct.CDLL:
+    """Loads libsquishy_volumes_cuda.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not path.exists():
+            raise RuntimeError(
+                f"{path} is missing: build the CUDA library first "
+                "(python -c 'import __graft_entry__ as g; g.build()')"
+            )
+        lib = ct.CDLL(str(path))
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+class SvError(RuntimeError):
+    """A fatal error reported by the library (negative return code)."""
+
+
+def check(rc: int) -> None:
+    if rc < 0:
+        msg = load().sv_last_error_string()
+        raise SvError(msg.decode() if msg else f"error {rc}")
+
+
+def ptr(arr, typ):
+    if arr is None:
+        return ct.cast(None, typ)
+    return arr.ctypes.data_as(typ)

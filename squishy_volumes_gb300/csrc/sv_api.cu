@@ -1,0 +1,651 @@
+// sv_api.cu -- the C ABI (include/squishy_volumes_cuda.h): handle lifecycle,
+// upload/download in the reference's particle layout, and the substep loop of
+// CpuState::produce_next_state (rust/crates/cpu/src/cpu_state.rs:146-197).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "sv_internal.h"
+#include "sv_sort.cuh"
+
+using namespace sv;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(const std::string &msg) {
+    g_last_error = msg;
+    return -1;
+}
+
+#define SV_CUDA(expr)                                                                                \
+    do {                                                                                             \
+        cudaError_t e_ = (expr);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return fail(std::string("CUDA error in ") + #expr + ": " + cudaGetErrorString(e_));     \
+    } while (0)
+
+template <class T> cudaError_t dalloc(sv_handle *h, T **p, uint64_t count) {
+    size_t bytes = (size_t)count * sizeof(T);
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc((void **)p, bytes);
+    if (e == cudaSuccess) h->device_bytes += bytes;
+    return e;
+}
+
+void free_side(ParticleArrays &a) {
+    cudaFree(a.pos), cudaFree(a.cell), cudaFree(a.vel), cudaFree(a.C), cudaFree(a.F), cudaFree(a.energy),
+        cudaFree(a.orig);
+    a = ParticleArrays{};
+}
+
+void free_handle(sv_handle *h) {
+    if (!h) return;
+    for (auto &s : h->side) free_side(s);
+    cudaFree(h->materials), cudaFree(h->keys), cudaFree(h->sorted_keys), cudaFree(h->perm), cudaFree(h->sort_temp);
+    cudaFree(h->seg_start), cudaFree(h->seg_block), cudaFree(h->tile_counts), cudaFree(h->scan_temp);
+    cudaFree(h->blockmap), cudaFree(h->active_blocks), cudaFree(h->grid), cudaFree(h->counters);
+    if (h->host_counters) cudaFreeHost(h->host_counters);
+    for (auto &p : h->timer.pending) cudaEventDestroy(p.second.first), cudaEventDestroy(p.second.second);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    delete h;
+}
+
+struct MaterialKey {
+    Material m;
+    bool operator==(const MaterialKey &o) const { return std::memcmp(&m, &o.m, sizeof(Material)) == 0; }
+};
+struct MaterialHash {
+    size_t operator()(const MaterialKey &k) const {
+        const uint32_t *w = reinterpret_cast<const uint32_t *>(&k.m);
+        uint64_t h = 1469598103934665603ull;
+        for (size_t i = 0; i < sizeof(Material) / 4; ++i) h = (h ^ w[i]) * 1099511628211ull;
+        return (size_t)h;
+    }
+};
+
+int build_material(const sv_particles *p, uint64_t i, Material &m, std::string &err) {
+    std::memset(&m, 0, sizeof(m));
+    uint32_t f = p->flags[i];
+    bool solid = f & SV_IS_SOLID, fluid = f & SV_IS_FLUID;
+    if (solid == fluid) {
+        err = "particle " + std::to_string(i) + ": exactly one of IS_SOLID and IS_FLUID must be set";
+        return -1;
+    }
+    if (f & ~0x7Fu) {
+        err = "particle " + std::to_string(i) + ": unknown flag bits set";
+        return -1;
+    }
+    m.mass = p->mass[i];
+    m.initial_volume = p->initial_volume[i];
+    uint32_t model = p->model ? p->model[i] : SV_MODEL_REFERENCE;
+    if (f & SV_USE_VISCOSITY) {
+        if (!p->viscosity_dynamic || !p->viscosity_bulk) {
+            err = "USE_VISCOSITY set but viscosity arrays are NULL";
+            return -1;
+        }
+        m.use_viscosity = 1;
+        m.visc_dynamic = p->viscosity_dynamic[i];
+        m.visc_bulk = p->viscosity_bulk[i];
+    }
+    if (fluid) {
+        if (model != SV_MODEL_REFERENCE) {
+            err = "particle " + std::to_string(i) + ": fluids only have the reference model";
+            return -1;
+        }
+        m.kind = KIND_FLUID;
+        m.exponent = p->exponent ? p->exponent[i] : 0;
+        m.bulk_modulus = p->bulk_modulus ? p->bulk_modulus[i] : 0.f;
+        // util/src/elastic.rs:527-543
+        if (m.exponent <= 1) {
+            err = "particle " + std::to_string(i) + ": exponent must be greater than 1";
+            return -1;
+        }
+        if (m.bulk_modulus < 0.f) {
+            err = "particle " + std::to_string(i) + ": bulk modulus is negative";
+            return -1;
+        }
+        return 0;
+    }
+    m.mu = p->mu ? p->mu[i] : 0.f;
+    m.lambda = p->lambda ? p->lambda[i] : 0.f;
+    if (model == SV_MODEL_FIXED_COROTATED) {
+        m.kind = KIND_FIXED_COROTATED;
+    } else if (model == SV_MODEL_SNOW) {
+        m.kind = KIND_SNOW;
+        m.xi = p->hardening ? p->hardening[i] : 0.f;
+        m.theta_c = p->crit_compression ? p->crit_compression[i] : 0.f;
+        m.theta_s = p->crit_stretch ? p->crit_stretch[i] : 0.f;
+    } else if (model == SV_MODEL_REFERENCE) {
+        if (f & SV_USE_SAND_ALPHA) {
+            if (!p->sand_alpha) {
+                err = "USE_SAND_ALPHA set but sand_alpha is NULL";
+                return -1;
+            }
+            m.kind = KIND_SAND;
+            m.alpha = p->sand_alpha[i];
+        } else {
+            m.kind = KIND_NEO_HOOKEAN;
+        }
+    } else {
+        err = "particle " + std::to_string(i) + ": unknown model";
+        return -1;
+    }
+    return 0;
+}
+
+cudaError_t alloc_grid(sv_handle *h, uint64_t capacity) {
+    cudaError_t e;
+    uint32_t *active = nullptr;
+    float4 *grid = nullptr;
+    if ((e = dalloc(h, &active, capacity)) != cudaSuccess) return e;
+    if ((e = dalloc(h, &grid, capacity * 64)) != cudaSuccess) {
+        cudaFree(active);
+        return e;
+    }
+    if (h->active_blocks) {
+        // keep the previous substep's slot list so the block map can be reset
+        cudaMemcpyAsync(active, h->active_blocks, std::min(capacity, h->capacity) * 4, cudaMemcpyDeviceToDevice,
+                        h->stream);
+        cudaStreamSynchronize(h->stream);
+        cudaFree(h->active_blocks);
+        cudaFree(h->grid);
+        h->device_bytes -= h->capacity * 4 + h->capacity * 64 * sizeof(float4);
+    }
+    h->active_blocks = active;
+    h->grid = grid;
+    h->capacity = capacity;
+    return cudaSuccess;
+}
+
+int run_substep(sv_handle *h, float dt, float3 g, bool advance) {
+    if (!h->keys_valid) SV_CUDA(launch_keys(h));
+    SV_CUDA(launch_sort_and_segments(h));
+    SV_CUDA(launch_grid_activate(h));
+    SV_CUDA(launch_p2g(h, dt, g));
+    SV_CUDA(launch_grid_update(h));
+    if (advance) {
+        SV_CUDA(launch_g2p(h, dt));
+        SV_CUDA(launch_finish_substep(h));
+    }
+    return 0;
+}
+
+int read_counters(sv_handle *h) {
+    SV_CUDA(cudaMemcpyAsync(h->host_counters, h->counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    SV_CUDA(cudaStreamSynchronize(h->stream));
+    return 0;
+}
+
+}  // namespace
+
+namespace sv {
+
+void timer_begin(sv_handle *h, const char *, cudaEvent_t *start) {
+    if (!h->profiling) return;
+    cudaEventCreate(start);
+    cudaEventRecord(*start, h->stream);
+}
+
+void timer_end(sv_handle *h, const char *name, cudaEvent_t start) {
+    if (!h->profiling || !start) return;
+    cudaEvent_t stop;
+    cudaEventCreate(&stop);
+    cudaEventRecord(stop, h->stream);
+    h->timer.pending.push_back({name, {start, stop}});
+}
+
+}  // namespace sv
+
+extern "C" {
+
+const char *sv_last_error_string(void) { return g_last_error.c_str(); }
+
+int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) {
+    g_last_error.clear();
+    if (!c || !p || !out) return fail("sv_create: NULL argument");
+    *out = nullptr;
+    const uint64_t n = p->n;
+    if (n >= (1ull << 31)) return fail("sv_create: too many particles (limit 2^31 - 1)");
+    if (n > 0 && (!p->flags || !p->positions || !p->position_gradients || !p->velocities || !p->velocity_gradients ||
+                  !p->mass || !p->initial_volume))
+        return fail("sv_create: required particle array is NULL");
+    if (!(c->grid_node_size > 0.f)) return fail("sv_create: grid_node_size must be positive");
+    if (c->position_form > 1) return fail("sv_create: unknown position_form");
+    if (c->ground_mode < 0 || c->ground_mode > 2 || c->ground_axis < 0 || c->ground_axis > 2)
+        return fail("sv_create: invalid ground plane settings");
+    for (uint64_t i = 0; i < n; ++i)
+        if (p->collider_bits && p->collider_bits[i] != 0)
+            return fail("sv_create: collider bits are set but colliders are not supported by this backend");
+
+    // materials (deduplicated ParticleParameters)
+    std::vector<Material> mats;
+    std::vector<uint32_t> mat_index(n);
+    {
+        std::unordered_map<MaterialKey, uint32_t, MaterialHash> index;
+        Material prev{};
+        uint32_t prev_idx = UINT32_MAX;
+        std::string err;
+        for (uint64_t i = 0; i < n; ++i) {
+            Material m;
+            if (build_material(p, i, m, err)) return fail("sv_create: " + err);
+            if (prev_idx != UINT32_MAX && std::memcmp(&m, &prev, sizeof(m)) == 0) {
+                mat_index[i] = prev_idx;
+                continue;
+            }
+            auto it = index.find(MaterialKey{m});
+            uint32_t idx;
+            if (it == index.end()) {
+                idx = (uint32_t)mats.size();
+                if (idx >= MAX_MATERIALS) return fail("sv_create: more than 2^24 distinct particle parameter sets");
+                index.emplace(MaterialKey{m}, idx);
+                mats.push_back(m);
+            } else {
+                idx = it->second;
+            }
+            mat_index[i] = idx;
+            prev = m, prev_idx = idx;
+        }
+        if (mats.empty()) mats.push_back(Material{});
+    }
+
+    sv_handle *h = new sv_handle();
+    h->n = n;
+    for (auto &m : mats) {
+        h->any_snow |= m.kind == KIND_SNOW;
+        h->any_fcr |= m.kind == KIND_FIXED_COROTATED;
+    }
+    GridLayout &L = h->layout;
+    L.dx = c->grid_node_size;
+    L.ground_mode = c->ground_mode, L.ground_axis = c->ground_axis, L.ground_height = c->ground_height;
+    L.position_form = c->position_form;
+    L.svd_policy = c->svd_fp64_policy;
+    for (int a = 0; a < 3; ++a) {
+        L.domain_min[a] = c->domain_min[a], L.domain_max[a] = c->domain_max[a];
+        L.dmin_cells[a] = (double)c->domain_min[a] / (double)L.dx;
+        L.dmax_cells[a] = (double)c->domain_max[a] / (double)L.dx;
+    }
+    // Block index bounds: the domain plus the initial live particles (which
+    // may start outside the domain; they are culled after their first substep).
+    double lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) lo[a] = c->domain_min[a], hi[a] = c->domain_max[a];
+    for (uint64_t i = 0; i < n; ++i) {
+        if (p->flags[i] & SV_TOMBSTONED) continue;
+        for (int a = 0; a < 3; ++a) {
+            double x = p->positions[3 * i + a];
+            if (!std::isfinite(x)) {
+                free_handle(h);
+                return fail("sv_create: non-finite particle position");
+            }
+            lo[a] = std::min(lo[a], x), hi[a] = std::max(hi[a], x);
+        }
+    }
+    uint64_t total = 1;
+    for (int a = 0; a < 3; ++a) {
+        double cmin = std::floor(lo[a] / L.dx - 0.5), cmax = std::floor(hi[a] / L.dx - 0.5);
+        if (!(cmax - cmin < 4.0e8)) {
+            free_handle(h);
+            return fail("sv_create: domain too large for the dense block index");
+        }
+        L.origin[a] = (int32_t)cmin - 4;
+        L.nb[a] = (int32_t)(((int64_t)cmax - L.origin[a]) >> 2) + 3;
+        total *= (uint64_t)L.nb[a];
+        if (total > (1ull << 26)) {
+            free_handle(h);
+            return fail("sv_create: the dense block index would exceed 2^26 blocks of 4^3 nodes "
+                        "(domain / grid_node_size too large)");
+        }
+    }
+    L.total_blocks = total;
+    L.key_bits = 0;
+    while ((1ull << L.key_bits) <= total * 64) ++L.key_bits;
+
+    auto cuda_fail = [&](cudaError_t e, const char *what) {
+        free_handle(h);
+        return fail(std::string("sv_create: ") + what + ": " + cudaGetErrorString(e));
+    };
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(e, "stream");
+    h->stream = h->own_stream;
+    const bool cell = L.position_form == 1;
+    for (int s = 0; s < 2; ++s) {
+        ParticleArrays &a = h->side[s];
+        if ((e = dalloc(h, &a.pos, n)) || (cell && (e = dalloc(h, &a.cell, n))) || (e = dalloc(h, &a.vel, n)) ||
+            (e = dalloc(h, &a.C, 9 * n)) || (e = dalloc(h, &a.F, 9 * n)) || (e = dalloc(h, &a.energy, n)) ||
+            (e = dalloc(h, &a.orig, n)))
+            return cuda_fail(e, "particle buffers");
+    }
+    if ((e = dalloc(h, &h->materials, mats.size())) || (e = dalloc(h, &h->keys, n)) ||
+        (e = dalloc(h, &h->sorted_keys, n)) || (e = dalloc(h, &h->perm, n)) || (e = dalloc(h, &h->seg_start, n + 1)) ||
+        (e = dalloc(h, &h->seg_block, n)) || (e = dalloc(h, &h->counters, C_COUNT)))
+        return cuda_fail(e, "work buffers");
+    h->n_materials = (uint32_t)mats.size();
+    h->sort_temp_bytes = radix_sort_temp_bytes(n);
+    uint64_t tiles = (n + 2047) / 2048 + 1;
+    if ((e = dalloc(h, (char **)&h->sort_temp, h->sort_temp_bytes)) || (e = dalloc(h, &h->tile_counts, tiles)) ||
+        (e = dalloc(h, (char **)&h->scan_temp, scan_temp_bytes(tiles))))
+        return cuda_fail(e, "sort buffers");
+    if ((e = dalloc(h, &h->blockmap, total))) return cuda_fail(e, "block map");
+    uint64_t cap = c->block_capacity ? c->block_capacity : std::min<uint64_t>(total, std::max<uint64_t>(65536, n / 4));
+    if ((e = alloc_grid(h, cap))) return cuda_fail(e, "grid");
+    if ((e = cudaMallocHost((void **)&h->host_counters, C_COUNT * sizeof(uint32_t)))) return cuda_fail(e, "pinned");
+
+    // Upload.  Host staging in the device layout, then one copy per array.
+    {
+        std::vector<float4> pos(n), vel(n);
+        std::vector<int4> cellv(cell ? n : 0);
+        std::vector<float> C(9 * n), F(9 * n), en(n);
+        std::vector<uint32_t> orig(n);
+        for (uint64_t i = 0; i < n; ++i) {
+            uint32_t packed = (p->flags[i] & FLAG_MASK) | (mat_index[i] << MATERIAL_SHIFT);
+            float x = p->positions[3 * i], y = p->positions[3 * i + 1], z = p->positions[3 * i + 2];
+            if (!cell) {
+                pos[i] = make_float4(x, y, z, 0.f);
+            } else {
+                double q[3] = {(double)x / L.dx, (double)y / L.dx, (double)z / L.dx};
+                int ci[3];
+                float o[3];
+                for (int a = 0; a < 3; ++a) {
+                    double f = std::floor(q[a]);
+                    ci[a] = (int)f;
+                    o[a] = (float)(q[a] - f);
+                    if (o[a] >= 1.f) o[a] = 0.f, ci[a] += 1;
+                }
+                pos[i] = make_float4(o[0], o[1], o[2], 0.f);
+                cellv[i] = make_int4(ci[0], ci[1], ci[2], 0);
+            }
+            std::memcpy(&pos[i].w, &packed, 4);
+            vel[i] = make_float4(p->velocities[3 * i], p->velocities[3 * i + 1], p->velocities[3 * i + 2],
+                                 p->plastic_j ? p->plastic_j[i] : 1.f);
+            for (int k = 0; k < 9; ++k) {
+                C[(uint64_t)k * n + i] = p->velocity_gradients[9 * i + k];
+                F[(uint64_t)k * n + i] = p->position_gradients[9 * i + k];
+            }
+            en[i] = p->elastic_energies ? p->elastic_energies[i] : 0.f;
+            orig[i] = (uint32_t)i;
+        }
+        ParticleArrays &a = h->side[0];
+        if ((e = cudaMemcpy(a.pos, pos.data(), n * 16, cudaMemcpyHostToDevice)) ||
+            (cell && (e = cudaMemcpy(a.cell, cellv.data(), n * 16, cudaMemcpyHostToDevice))) ||
+            (e = cudaMemcpy(a.vel, vel.data(), n * 16, cudaMemcpyHostToDevice)) ||
+            (e = cudaMemcpy(a.C, C.data(), 9 * n * 4, cudaMemcpyHostToDevice)) ||
+            (e = cudaMemcpy(a.F, F.data(), 9 * n * 4, cudaMemcpyHostToDevice)) ||
+            (e = cudaMemcpy(a.energy, en.data(), n * 4, cudaMemcpyHostToDevice)) ||
+            (e = cudaMemcpy(a.orig, orig.data(), n * 4, cudaMemcpyHostToDevice)) ||
+            (e = cudaMemcpy(h->materials, mats.data(), mats.size() * sizeof(Material), cudaMemcpyHostToDevice)) ||
+            (e = cudaMemset(h->blockmap, 0xFF, total * 4)) || (e = cudaMemset(h->counters, 0, C_COUNT * 4)))
+            return cuda_fail(e, "upload");
+    }
+    h->collider_bits.assign(n, 0);
+    h->keys_valid = false;
+    *out = h;
+    return 0;
+}
+
+void sv_destroy(sv_handle *h) { free_handle(h); }
+
+int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3], const volatile int32_t *cancel,
+            uint32_t *status_out, uint32_t *substeps_done) {
+    g_last_error.clear();
+    if (!h) return fail("sv_step: NULL handle");
+    if (status_out) *status_out = 0;
+    if (substeps_done) *substeps_done = 0;
+    if (!(dt > 0.f)) return fail("sv_step: dt must be positive");  // cpu_state.rs:170-172 ZeroTimeStep
+    float3 g = gravity ? make_float3(gravity[0], gravity[1], gravity[2]) : make_float3(0.f, 0.f, 0.f);
+    if (read_counters(h)) return -1;
+    uint32_t base = h->host_counters[C_SUBSTEPS];
+    uint32_t fp64_before = h->host_counters[C_FP64];
+    uint32_t status = 0;
+    uint32_t done = 0;
+    const uint32_t chunk = 64;
+    while (done < n_substeps) {
+        if (cancel && *cancel) {
+            status |= SV_STATUS_CANCELED;
+            break;
+        }
+        uint32_t todo = std::min(chunk, n_substeps - done);
+        for (uint32_t s = 0; s < todo; ++s)
+            if (run_substep(h, dt, g, true)) return -1;
+        if (read_counters(h)) return -1;
+        uint32_t st = h->host_counters[C_STATUS];
+        done = h->host_counters[C_SUBSTEPS] - base;
+        if (st & ST_OUT_OF_GRID) return fail("sv_step: a live particle left the grid block index");
+        if (st & ST_CAPACITY) {
+            // Grow and redo the substeps that were skipped (gpu_state.rs:562-599
+            // redoes a frame with doubled capacity).
+            uint64_t cap = std::min<uint64_t>(h->layout.total_blocks, h->capacity * 2);
+            if (cap <= h->capacity) return fail("sv_step: grid block capacity exhausted");
+            SV_CUDA(alloc_grid(h, cap));
+            h->host_counters[C_STATUS] &= ~ST_CAPACITY;
+            SV_CUDA(cudaMemcpyAsync(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice,
+                                    h->stream));
+            SV_CUDA(cudaStreamSynchronize(h->stream));
+            continue;
+        }
+        if (st & ST_INVERTED) {
+            status |= SV_STATUS_PARTICLE_INVERTED;
+            break;
+        }
+    }
+    h->substeps_total += done;
+    h->fp64_total += (uint32_t)(h->host_counters[C_FP64] - fp64_before);
+    if (status_out) *status_out = status;
+    if (substeps_done) *substeps_done = done;
+    return 0;
+}
+
+int sv_p2g_only(sv_handle *h, float dt, const float gravity[3]) {
+    g_last_error.clear();
+    if (!h) return fail("sv_p2g_only: NULL handle");
+    float3 g = gravity ? make_float3(gravity[0], gravity[1], gravity[2]) : make_float3(0.f, 0.f, 0.f);
+    if (run_substep(h, dt, g, false)) return -1;
+    // record the slot list for the next block-map reset, without counting a substep
+    if (read_counters(h)) return -1;
+    uint32_t slots = std::min<uint64_t>(h->host_counters[C_NSLOT], h->capacity);
+    SV_CUDA(cudaMemcpyAsync(h->counters + C_NSLOT_PREV, &slots, 4, cudaMemcpyHostToDevice, h->stream));
+    SV_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->host_counters[C_STATUS] & ST_CAPACITY) return fail("sv_p2g_only: grid block capacity exceeded");
+    return 0;
+}
+
+int sv_download(sv_handle *h, sv_particles *o) {
+    g_last_error.clear();
+    if (!h || !o) return fail("sv_download: NULL argument");
+    if (o->n != h->n) return fail("sv_download: particle count mismatch");
+    const uint64_t n = h->n;
+    const ParticleArrays &a = h->side[h->cur];
+    const bool cell = h->layout.position_form == 1;
+    std::vector<float4> pos(n), vel(n);
+    std::vector<int4> cellv(cell ? n : 0);
+    std::vector<float> C(9 * n), F(9 * n), en(n);
+    std::vector<uint32_t> orig(n);
+    SV_CUDA(cudaStreamSynchronize(h->stream));
+    SV_CUDA(cudaMemcpy(pos.data(), a.pos, n * 16, cudaMemcpyDeviceToHost));
+    if (cell) SV_CUDA(cudaMemcpy(cellv.data(), a.cell, n * 16, cudaMemcpyDeviceToHost));
+    SV_CUDA(cudaMemcpy(vel.data(), a.vel, n * 16, cudaMemcpyDeviceToHost));
+    SV_CUDA(cudaMemcpy(C.data(), a.C, 9 * n * 4, cudaMemcpyDeviceToHost));
+    SV_CUDA(cudaMemcpy(F.data(), a.F, 9 * n * 4, cudaMemcpyDeviceToHost));
+    SV_CUDA(cudaMemcpy(en.data(), a.energy, n * 4, cudaMemcpyDeviceToHost));
+    SV_CUDA(cudaMemcpy(orig.data(), a.orig, n * 4, cudaMemcpyDeviceToHost));
+    const double dx = h->layout.dx;
+    for (uint64_t s = 0; s < n; ++s) {
+        const uint64_t i = orig[s];
+        if (i >= n) return fail("sv_download: corrupt original index");
+        uint32_t packed;
+        std::memcpy(&packed, &pos[s].w, 4);
+        if (o->flags) o->flags[i] = packed & FLAG_MASK;
+        if (o->positions) {
+            if (!cell) {
+                o->positions[3 * i] = pos[s].x, o->positions[3 * i + 1] = pos[s].y, o->positions[3 * i + 2] = pos[s].z;
+            } else {
+                o->positions[3 * i] = (float)(((double)cellv[s].x + pos[s].x) * dx);
+                o->positions[3 * i + 1] = (float)(((double)cellv[s].y + pos[s].y) * dx);
+                o->positions[3 * i + 2] = (float)(((double)cellv[s].z + pos[s].z) * dx);
+            }
+        }
+        if (o->velocities) o->velocities[3 * i] = vel[s].x, o->velocities[3 * i + 1] = vel[s].y, o->velocities[3 * i + 2] = vel[s].z;
+        if (o->plastic_j) o->plastic_j[i] = vel[s].w;
+        for (int k = 0; k < 9; ++k) {
+            if (o->position_gradients) o->position_gradients[9 * i + k] = F[(uint64_t)k * n + s];
+            if (o->velocity_gradients) o->velocity_gradients[9 * i + k] = C[(uint64_t)k * n + s];
+        }
+        if (o->elastic_energies) o->elastic_energies[i] = en[s];
+        if (o->collider_bits) o->collider_bits[i] = h->collider_bits[i];
+    }
+    return 0;
+}
+
+int sv_download_grid(sv_handle *h, int32_t *node_ids, float *masses, float *velocities, uint64_t capacity,
+                     uint64_t *count) {
+    g_last_error.clear();
+    if (!h) return fail("sv_download_grid: NULL handle");
+    if (read_counters(h)) return -1;
+    uint64_t slots = std::min<uint64_t>(h->host_counters[C_NSLOT_PREV], h->capacity);
+    std::vector<uint32_t> active(slots);
+    std::vector<float4> g(slots * 64);
+    if (slots) {
+        SV_CUDA(cudaMemcpy(active.data(), h->active_blocks, slots * 4, cudaMemcpyDeviceToHost));
+        SV_CUDA(cudaMemcpy(g.data(), h->grid, slots * 64 * sizeof(float4), cudaMemcpyDeviceToHost));
+    }
+    struct Node {
+        int32_t id[3];
+        float4 v;
+    };
+    std::vector<Node> nodes;
+    const GridLayout &L = h->layout;
+    for (uint64_t s = 0; s < slots; ++s) {
+        uint32_t b = active[s];
+        int bz = (int)(b % (uint32_t)L.nb[2]), r = (int)(b / (uint32_t)L.nb[2]);
+        int by = r % L.nb[1], bx = r / L.nb[1];
+        for (int l = 0; l < 64; ++l) {
+            float4 v = g[s * 64 + l];
+            if (!(v.w > 0.f)) continue;
+            Node nd;
+            nd.id[0] = L.origin[0] + 4 * bx + (l >> 4);
+            nd.id[1] = L.origin[1] + 4 * by + ((l >> 2) & 3);
+            nd.id[2] = L.origin[2] + 4 * bz + (l & 3);
+            nd.v = v;
+            nodes.push_back(nd);
+        }
+    }
+    std::sort(nodes.begin(), nodes.end(), [](const Node &x, const Node &y) {
+        if (x.id[0] != y.id[0]) return x.id[0] < y.id[0];
+        if (x.id[1] != y.id[1]) return x.id[1] < y.id[1];
+        return x.id[2] < y.id[2];
+    });
+    if (count) *count = nodes.size();
+    for (uint64_t i = 0; i < nodes.size() && i < capacity; ++i) {
+        if (node_ids) std::memcpy(&node_ids[3 * i], nodes[i].id, 12);
+        if (masses) masses[i] = nodes[i].v.w;
+        if (velocities) velocities[3 * i] = nodes[i].v.x, velocities[3 * i + 1] = nodes[i].v.y, velocities[3 * i + 2] = nodes[i].v.z;
+    }
+    return 0;
+}
+
+int sv_binning(sv_handle *h, uint32_t *keys, uint32_t *perm, uint32_t *original_index) {
+    g_last_error.clear();
+    if (!h) return fail("sv_binning: NULL handle");
+    if (!h->keys_valid) SV_CUDA(launch_keys(h));
+    SV_CUDA(launch_sort_and_segments(h));
+    SV_CUDA(cudaStreamSynchronize(h->stream));
+    const uint64_t n = h->n;
+    if (keys) SV_CUDA(cudaMemcpy(keys, h->keys, n * 4, cudaMemcpyDeviceToHost));
+    if (perm) SV_CUDA(cudaMemcpy(perm, h->perm, n * 4, cudaMemcpyDeviceToHost));
+    if (original_index) SV_CUDA(cudaMemcpy(original_index, h->side[h->cur].orig, n * 4, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int sv_grid_layout(sv_handle *h, int32_t origin[3], int32_t nblocks[3]) {
+    if (!h) return fail("sv_grid_layout: NULL handle");
+    for (int a = 0; a < 3; ++a) {
+        if (origin) origin[a] = h->layout.origin[a];
+        if (nblocks) nblocks[a] = h->layout.nb[a];
+    }
+    return 0;
+}
+
+int sv_sort_pairs(const uint32_t *keys, uint32_t *perm, uint64_t n) {
+    g_last_error.clear();
+    if (n == 0) return 0;
+    if (!keys || !perm) return fail("sv_sort_pairs: NULL argument");
+    if (n >= (1ull << 32)) return fail("sv_sort_pairs: n must be below 2^32");
+    uint32_t *dk = nullptr, *dko = nullptr, *dv = nullptr;
+    void *temp = nullptr;
+    size_t tb = radix_sort_temp_bytes(n);
+    cudaError_t e;
+    if ((e = cudaMalloc(&dk, n * 4)) || (e = cudaMalloc(&dko, n * 4)) || (e = cudaMalloc(&dv, n * 4)) ||
+        (e = cudaMalloc(&temp, tb)) || (e = cudaMemcpy(dk, keys, n * 4, cudaMemcpyHostToDevice)) ||
+        (e = radix_sort_pairs(dk, nullptr, dko, dv, n, 32, temp, 0)) ||
+        (e = cudaMemcpy(perm, dv, n * 4, cudaMemcpyDeviceToHost))) {
+        cudaFree(dk), cudaFree(dko), cudaFree(dv), cudaFree(temp);
+        return fail(std::string("sv_sort_pairs: ") + cudaGetErrorString(e));
+    }
+    cudaFree(dk), cudaFree(dko), cudaFree(dv), cudaFree(temp);
+    return 0;
+}
+
+int sv_get_stats(sv_handle *h, sv_stats *out) {
+    if (!h || !out) return fail("sv_get_stats: NULL argument");
+    if (read_counters(h)) return -1;
+    out->particles = h->n;
+    out->live_particles = h->host_counters[C_NLIVE];
+    out->particle_blocks = h->host_counters[C_NSEG];
+    out->grid_blocks = h->host_counters[C_NSLOT_PREV];
+    out->fp64_svd = h->fp64_total;
+    out->substeps = h->substeps_total;
+    out->device_bytes = h->device_bytes;
+    out->kernel_launches = h->launches;
+    return 0;
+}
+
+int sv_set_stream(sv_handle *h, void *stream) {
+    if (!h) return fail("sv_set_stream: NULL handle");
+    SV_CUDA(cudaStreamSynchronize(h->stream));
+    h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+    return 0;
+}
+
+int sv_set_profiling(sv_handle *h, int enable) {
+    if (!h) return fail("sv_set_profiling: NULL handle");
+    h->profiling = enable != 0;
+    return 0;
+}
+
+int sv_profile_report(sv_handle *h, char *buffer, uint64_t capacity) {
+    if (!h) return fail("sv_profile_report: NULL handle");
+    SV_CUDA(cudaStreamSynchronize(h->stream));
+    for (auto &p : h->timer.pending) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+        auto &t = h->timer.totals[p.first];
+        t.first += 1, t.second += ms;
+        cudaEventDestroy(p.second.first), cudaEventDestroy(p.second.second);
+    }
+    h->timer.pending.clear();
+    std::string s = "{";
+    bool first = true;
+    for (auto &kv : h->timer.totals) {
+        char buf[256];
+        snprintf(buf, sizeof buf, "%s\"%s\": {\"launches\": %llu, \"ms\": %.6f}", first ? "" : ", ", kv.first.c_str(),
+                 (unsigned long long)kv.second.first, kv.second.second);
+        s += buf;
+        first = false;
+    }
+    s += "}";
+    if (buffer && capacity) {
+        size_t m = std::min<size_t>(s.size(), capacity - 1);
+        std::memcpy(buffer, s.data(), m);
+        buffer[m] = 0;
+    }
+    h->timer.totals.clear();
+    return (int)s.size();
+}
+
+}  // extern "C"

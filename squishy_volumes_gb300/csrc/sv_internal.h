@@ -1,0 +1,139 @@
+// sv_internal.h -- device state of one handle and the launchers of the
+// substep kernels (sv_substep.cu), shared with the C ABI (sv_api.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/squishy_volumes_cuda.h"
+#include "sv_math.cuh"
+
+namespace sv {
+
+// Particle flag bits (file_frame/src/particles.rs:21-33) live in the low 8
+// bits of the packed word; the material index in the upper 24.
+constexpr uint32_t FLAG_MASK = 0xFFu;
+constexpr uint32_t MATERIAL_SHIFT = 8;
+constexpr uint32_t MAX_MATERIALS = 1u << 24;
+constexpr uint32_t SENTINEL_KEY = 0xFFFFFFFFu;
+
+// Device status word bits.  Any bit in STOP_MASK makes every later kernel of
+// the run leave the particle state untouched.
+constexpr uint32_t ST_CAPACITY = SV_STATUS_CAPACITY_EXCEEDED;
+constexpr uint32_t ST_INVERTED = SV_STATUS_PARTICLE_INVERTED;
+constexpr uint32_t ST_OUT_OF_GRID = 1u << 4;  // a live particle left the block index
+constexpr uint32_t STOP_MASK = ST_CAPACITY | ST_INVERTED | ST_OUT_OF_GRID;
+
+// Device counters (one u32/u64 array so one copy reads them all).
+enum Counter : int {
+    C_STATUS = 0,
+    C_NSEG = 1,       // particle blocks (segments) this substep
+    C_NSLOT = 2,      // grid blocks claimed this substep
+    C_NSLOT_PREV = 3, // grid blocks of the previous substep (to reset the block map)
+    C_NLIVE = 4,      // live particles (segments cover [0, n_live))
+    C_SUBSTEPS = 5,   // substeps completed
+    C_FP64 = 6,       // particles that took the fp64 SVD (low 32 bits)
+    C_STOP = 7,       // STOP_MASK bits latched for the kernels that follow
+    C_COUNT = 8,
+};
+
+// One side of the particle state (ping-pong).  Structure of arrays: pos and
+// vel as float4 so one 16-byte load brings a vector and its companion word;
+// the two 3x3 matrices as nine planar float arrays each (fully coalesced).
+struct ParticleArrays {
+    float4 *pos;     // fp32 form: x, y, z, packed flags|material
+                     // cell form: offset x, y, z in [0,1) cell units, packed
+    int4 *cell;      // cell form only: cell x, y, z, unused
+    float4 *vel;     // vx, vy, vz, plastic J (snow)
+    float *C;        // [9][n] velocity gradient, column-major element planes
+    float *F;        // [9][n] position gradient
+    float *energy;   // [n]
+    uint32_t *orig;  // [n] original particle index (the reference's sort_map)
+};
+
+struct GridLayout {
+    int32_t origin[3];  // node/cell index of local cell 0
+    int32_t nb[3];      // blocks per axis
+    uint64_t total_blocks;
+    float dx;
+    float domain_min[3], domain_max[3];
+    double dmin_cells[3], dmax_cells[3];  // domain in cell units (cell form cull)
+    int32_t ground_mode, ground_axis;
+    float ground_height;
+    uint32_t position_form;
+    uint32_t svd_policy;
+    int key_bits;
+};
+
+struct KernelTimer {
+    std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    std::map<std::string, std::pair<uint64_t, double>> totals;  // launches, ms
+};
+
+}  // namespace sv
+
+struct sv_handle {
+    sv::GridLayout layout;
+    uint64_t n = 0;
+    int cur = 0;
+    sv::ParticleArrays side[2] = {};
+    sv::Material *materials = nullptr;
+    uint32_t n_materials = 0;
+    bool any_snow = false, any_fcr = false;
+
+    uint32_t *keys = nullptr;         // [n] binning keys in device order (valid when keys_valid)
+    bool keys_valid = false;
+    uint32_t *sorted_keys = nullptr;  // [n]
+    uint32_t *perm = nullptr;         // [n] device slot of each sorted position
+    void *sort_temp = nullptr;
+    size_t sort_temp_bytes = 0;
+
+    uint32_t *seg_start = nullptr;  // [n + 1]
+    uint32_t *seg_block = nullptr;  // [n]
+    uint32_t *tile_counts = nullptr;
+    void *scan_temp = nullptr;
+
+    int32_t *blockmap = nullptr;       // [total_blocks] slot or -1
+    uint32_t *active_blocks = nullptr; // [capacity]
+    float4 *grid = nullptr;            // [capacity * 64] (px, py, pz, m) -> (vx, vy, vz, m)
+    uint64_t capacity = 0;
+
+    uint32_t *counters = nullptr;       // device [C_COUNT]
+    uint32_t *host_counters = nullptr;  // pinned mirror
+
+    cudaStream_t stream = nullptr;      // stream all work is queued on
+    cudaStream_t own_stream = nullptr;  // the handle's own stream
+    uint64_t device_bytes = 0;
+    uint64_t fp64_total = 0;
+    uint64_t substeps_total = 0;
+    uint64_t launches = 0;  // kernels launched by this handle
+
+    // host-side copies of what the substep never changes
+    std::vector<uint32_t> collider_bits;
+
+    bool profiling = false;
+    sv::KernelTimer timer;
+};
+
+namespace sv {
+
+// Launchers (sv_substep.cu).  All run on h->stream and read counts from
+// device memory, so a substep needs no host synchronisation.
+cudaError_t launch_keys(sv_handle *h);
+cudaError_t launch_sort_and_segments(sv_handle *h);
+cudaError_t launch_grid_activate(sv_handle *h);
+cudaError_t launch_p2g(sv_handle *h, float dt, float3 gravity);
+cudaError_t launch_grid_update(sv_handle *h);
+cudaError_t launch_g2p(sv_handle *h, float dt);
+cudaError_t launch_finish_substep(sv_handle *h);
+
+// Per-kernel timing hooks.
+void timer_begin(sv_handle *h, const char *name, cudaEvent_t *start);
+void timer_end(sv_handle *h, const char *name, cudaEvent_t start);
+
+int sm_count();
+
+}  // namespace sv

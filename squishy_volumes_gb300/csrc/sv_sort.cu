@@ -1,0 +1,264 @@
+// sv_sort.cu -- stable LSD radix sort and exclusive scan, written for
+// sm_103a: 8-bit digits, per-tile histograms scanned digit-major, and a
+// stable scatter whose in-tile ranks come from __match_any_sync peer groups
+// processed row by row (so equal digits keep input order).
+#include "sv_sort.cuh"
+
+namespace sv {
+
+namespace {
+
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+constexpr int SORT_WARPS = 8;
+constexpr int SORT_THREADS = SORT_WARPS * 32;
+constexpr int SORT_ITEMS = 8;
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;
+constexpr int RADIX = 256;
+
+inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan of SCAN_ITEMS consecutive values per thread.
+// Returns the block total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t (&v)[SCAN_ITEMS], uint32_t *warp_sums) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t local = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        uint32_t t = v[i];
+        v[i] = local;
+        local += t;
+    }
+    uint32_t inc = warp_inclusive_scan(local, lane);
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t s = warp_sums[lane];
+        uint32_t si = warp_inclusive_scan(s, lane);
+        warp_sums[lane] = si - s;
+        if (lane == 31) warp_sums[32] = si;
+    }
+    __syncthreads();
+    uint32_t off = warp_sums[warp] + inc - local;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) v[i] += off;
+    uint32_t total = warp_sums[32];
+    __syncthreads();
+    return total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t *in, uint64_t n, uint32_t *sums) {
+    __shared__ uint32_t red[32];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i)
+        if (base + i < n) s += in[base + i];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) red[warp] = s;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t t = red[lane];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) sums[blockIdx.x] = t;
+    }
+}
+
+// Scans one SCAN_TILE per block and adds the block's offset (offsets may be
+// null for a single block).
+__global__ void __launch_bounds__(SCAN_THREADS)
+    k_scan_tile(const uint32_t *in, uint32_t *out, uint64_t n, const uint32_t *offsets) {
+    __shared__ uint32_t warp_sums[33];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) v[i] = base + i < n ? in[base + i] : 0u;
+    block_exclusive_scan(v, warp_sums);
+    uint32_t off = offsets ? offsets[blockIdx.x] : 0u;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i)
+        if (base + i < n) out[base + i] = v[i] + off;
+}
+
+// Per-tile digit histogram, stored digit-major: hist[d * tiles + tile].
+__global__ void __launch_bounds__(SORT_THREADS)
+    k_radix_hist(const uint32_t *keys, uint64_t n, int shift, uint32_t mask, uint32_t *hist, uint32_t tiles) {
+    __shared__ uint32_t h[RADIX];
+    for (int i = threadIdx.x; i < RADIX; i += SORT_THREADS) h[i] = 0;
+    __syncthreads();
+    uint64_t base = (uint64_t)blockIdx.x * SORT_TILE;
+#pragma unroll
+    for (int j = 0; j < SORT_ITEMS; ++j) {
+        uint64_t e = base + (uint64_t)j * SORT_THREADS + threadIdx.x;
+        if (e < n) atomicAdd(&h[(keys[e] >> shift) & mask], 1u);
+    }
+    __syncthreads();
+    for (uint32_t d = threadIdx.x; d <= mask; d += SORT_THREADS) hist[(uint64_t)d * tiles + blockIdx.x] = h[d];
+}
+
+// Stable scatter (vals_in == nullptr means "value = element index").  Warp w owns elements [w*32*ITEMS, (w+1)*32*ITEMS) of the
+// tile; row j of lane l is element w*32*ITEMS + j*32 + l, so walking rows in
+// order and lanes in order visits the warp's elements in input order.
+__global__ void __launch_bounds__(SORT_THREADS)
+    k_radix_scatter(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
+                    uint64_t n, int shift, uint32_t mask, const uint32_t *scanned, uint32_t tiles) {
+    __shared__ uint32_t wcnt[SORT_WARPS][RADIX];
+    __shared__ uint32_t gbase[RADIX];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < SORT_WARPS * RADIX; i += SORT_THREADS) (&wcnt[0][0])[i] = 0;
+    for (uint32_t d = threadIdx.x; d <= mask; d += SORT_THREADS) gbase[d] = scanned[(uint64_t)d * tiles + blockIdx.x];
+    __syncthreads();
+    const uint32_t lt = (1u << lane) - 1u;
+    uint64_t base = (uint64_t)blockIdx.x * SORT_TILE + (uint64_t)warp * 32 * SORT_ITEMS + lane;
+    uint32_t key[SORT_ITEMS], val[SORT_ITEMS], rank[SORT_ITEMS];
+#pragma unroll
+    for (int j = 0; j < SORT_ITEMS; ++j) {
+        uint64_t e = base + (uint64_t)j * 32;
+        bool valid = e < n;
+        key[j] = valid ? keys_in[e] : 0u;
+        val[j] = valid ? (vals_in ? vals_in[e] : (uint32_t)e) : 0u;
+        uint32_t digit = valid ? (key[j] >> shift) & mask : 0xFFFFFFFFu;
+        uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        int leader = __ffs(peers) - 1;
+        uint32_t before = 0;
+        if (lane == leader && valid) {
+            before = wcnt[warp][digit];
+            wcnt[warp][digit] = before + __popc(peers);
+        }
+        before = __shfl_sync(0xffffffffu, before, leader);
+        rank[j] = before + __popc(peers & lt);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (uint32_t d = threadIdx.x; d <= mask; d += SORT_THREADS) {
+        uint32_t run = gbase[d];
+#pragma unroll
+        for (int w = 0; w < SORT_WARPS; ++w) {
+            uint32_t c = wcnt[w][d];
+            wcnt[w][d] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < SORT_ITEMS; ++j) {
+        uint64_t e = base + (uint64_t)j * 32;
+        if (e < n) {
+            uint32_t digit = (key[j] >> shift) & mask;
+            uint32_t dst = wcnt[warp][digit] + rank[j];
+            keys_out[dst] = key[j];
+            vals_out[dst] = val[j];
+        }
+    }
+}
+
+}  // namespace
+
+size_t scan_temp_bytes(uint64_t n) {
+    size_t total = 0;
+    while (n > (uint64_t)SCAN_TILE) {
+        n = (n + SCAN_TILE - 1) / SCAN_TILE;
+        total += align_up(n * sizeof(uint32_t));
+    }
+    return total + 256;
+}
+
+cudaError_t exclusive_scan_u32(const uint32_t *in, uint32_t *out, uint64_t n, void *temp, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    if (n <= (uint64_t)SCAN_TILE) {
+        k_scan_tile<<<1, SCAN_THREADS, 0, stream>>>(in, out, n, nullptr);
+        return cudaGetLastError();
+    }
+    uint64_t blocks = (n + SCAN_TILE - 1) / SCAN_TILE;
+    uint32_t *sums = static_cast<uint32_t *>(temp);
+    void *rest = static_cast<char *>(temp) + align_up(blocks * sizeof(uint32_t));
+    k_scan_reduce<<<(unsigned)blocks, SCAN_THREADS, 0, stream>>>(in, n, sums);
+    cudaError_t err = exclusive_scan_u32(sums, sums, blocks, rest, stream);
+    if (err != cudaSuccess) return err;
+    k_scan_tile<<<(unsigned)blocks, SCAN_THREADS, 0, stream>>>(in, out, n, sums);
+    return cudaGetLastError();
+}
+
+int scan_launches(uint64_t n) {
+    if (n == 0) return 0;
+    if (n <= (uint64_t)SCAN_TILE) return 1;
+    return 2 + scan_launches((n + SCAN_TILE - 1) / SCAN_TILE);
+}
+
+int radix_sort_launches(uint64_t n, int key_bits) {
+    if (n == 0) return 0;
+    if (key_bits <= 0) return 0;
+    if (key_bits > 32) key_bits = 32;
+    uint64_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    int total = 0;
+    for (int shift = 0; shift < key_bits; shift += 8) {
+        int bits = key_bits - shift < 8 ? key_bits - shift : 8;
+        total += 2 + scan_launches(((uint64_t)1 << bits) * tiles);
+    }
+    return total;
+}
+
+size_t radix_sort_temp_bytes(uint64_t n) {
+    uint64_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    uint64_t hist = tiles * RADIX;
+    return 2 * align_up(n * sizeof(uint32_t)) + 2 * align_up(hist * sizeof(uint32_t)) + scan_temp_bytes(hist);
+}
+
+cudaError_t radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
+                             uint32_t *vals_out, uint64_t n, int key_bits, void *temp, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    if (n >= (1ull << 32)) return cudaErrorInvalidValue;
+    if (key_bits <= 0) {
+        cudaError_t e = cudaMemcpyAsync(keys_out, keys_in, n * 4, cudaMemcpyDeviceToDevice, stream);
+        if (e != cudaSuccess) return e;
+        return cudaMemcpyAsync(vals_out, vals_in, n * 4, cudaMemcpyDeviceToDevice, stream);
+    }
+    if (key_bits > 32) key_bits = 32;
+    uint32_t tiles = (uint32_t)((n + SORT_TILE - 1) / SORT_TILE);
+    uint64_t hist_n = (uint64_t)tiles * RADIX;
+    char *t = static_cast<char *>(temp);
+    uint32_t *alt_keys = reinterpret_cast<uint32_t *>(t);
+    t += align_up(n * 4);
+    uint32_t *alt_vals = reinterpret_cast<uint32_t *>(t);
+    t += align_up(n * 4);
+    uint32_t *hist = reinterpret_cast<uint32_t *>(t);
+    t += align_up(hist_n * 4);
+    uint32_t *scanned = reinterpret_cast<uint32_t *>(t);
+    t += align_up(hist_n * 4);
+    void *scan_temp = t;
+
+    const int passes = (key_bits + 7) / 8;
+    const uint32_t *src_k = keys_in, *src_v = vals_in;
+    for (int p = 0; p < passes; ++p) {
+        int shift = p * 8;
+        int bits = key_bits - shift < 8 ? key_bits - shift : 8;
+        uint32_t mask = (1u << bits) - 1u;
+        bool to_out = ((passes - 1 - p) % 2) == 0;
+        uint32_t *dk = to_out ? keys_out : alt_keys, *dv = to_out ? vals_out : alt_vals;
+        uint64_t used = (uint64_t)(mask + 1) * tiles;
+        k_radix_hist<<<tiles, SORT_THREADS, 0, stream>>>(src_k, n, shift, mask, hist, tiles);
+        cudaError_t err = exclusive_scan_u32(hist, scanned, used, scan_temp, stream);
+        if (err != cudaSuccess) return err;
+        k_radix_scatter<<<tiles, SORT_THREADS, 0, stream>>>(src_k, src_v, dk, dv, n, shift, mask, scanned, tiles);
+        err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        src_k = dk, src_v = dv;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace sv

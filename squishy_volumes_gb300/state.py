@@ -1,0 +1,409 @@
+"""Host-side mirror of the reference's backend interface for the MPM substep.
+
+The reference drives its CPU backend (rust/crates/cpu/src/cpu_state.rs) with
+three calls, chosen behind `enum ComputeState`
+(rust/crates/core/src/compute_thread.rs:101-117):
+
+* ``CpuState::from_io_state(io_state)``            -> :meth:`CudaState.from_io_state`
+* ``CpuState::produce_next_state(harness, frame_input, CpuRunParameters)``
+                                                     -> :meth:`CudaState.produce_next_state`
+* ``CpuState::to_io_state(store_grid)``              -> :meth:`CudaState.to_io_state`
+
+The types below mirror ``IoState`` / ``Particles`` / ``GridNodes``
+(rust/crates/file_frame/src/{io_state,particles,grid_nodes}.rs),
+``InputConsts`` (rust/crates/file_input/src/header.rs:10-71) and the
+cancellation half of ``Harness`` (rust/crates/xpu/src/harness.rs:53-144).
+All compute goes through libsquishy_volumes_cuda.so; nothing here computes
+physics.
+"""
+
+from __future__ import annotations
+
+import ctypes as ct
+from dataclasses import dataclass, field, fields
+from typing import Optional
+
+import numpy as np
+
+from . import _abi
+from ._abi import SvConsts, SvParticles, SvStats, check, f32p, i32p, ptr, u32p
+
+
+# --------------------------------------------------------------------- types
+@dataclass
+class Particles:
+    """file_frame::Particles (particles.rs:92-109) plus ParticleParameters
+    (particles.rs:55-90) as per-particle arrays.  Matrices are [n, 9]
+    column-major like nalgebra's Matrix3.  ``model`` .. ``plastic_j`` are
+    additions (fixed-corotated and snow); ``model`` 0 means the reference's
+    own Neo-Hookean / sand / fluid selection by flags."""
+
+    flags: np.ndarray
+    positions: np.ndarray
+    position_gradients: np.ndarray
+    velocities: np.ndarray
+    velocity_gradients: np.ndarray
+    mass: np.ndarray
+    initial_volume: np.ndarray
+    mu: Optional[np.ndarray] = None
+    lambda_: Optional[np.ndarray] = None
+    sand_alpha: Optional[np.ndarray] = None
+    exponent: Optional[np.ndarray] = None
+    bulk_modulus: Optional[np.ndarray] = None
+    viscosity_dynamic: Optional[np.ndarray] = None
+    viscosity_bulk: Optional[np.ndarray] = None
+    elastic_energies: Optional[np.ndarray] = None
+    collider_bits: Optional[np.ndarray] = None
+    initial_positions: Optional[np.ndarray] = None
+    model: Optional[np.ndarray] = None
+    hardening: Optional[np.ndarray] = None
+    crit_compression: Optional[np.ndarray] = None
+    crit_stretch: Optional[np.ndarray] = None
+    plastic_j: Optional[np.ndarray] = None
+
+    _DTYPES = {
+        "flags": np.uint32,
+        "exponent": np.int32,
+        "collider_bits": np.uint32,
+        "model": np.uint32,
+    }
+
+    def __post_init__(self):
+        for f in fields(self):
+            v = getattr(self, f.name)
+            if v is None:
+                continue
+            dt = self._DTYPES.get(f.name, np.float32)
+            v = np.ascontiguousarray(v, dtype=dt)
+            if f.name in ("positions", "velocities", "initial_positions"):
+                v = v.reshape(-1, 3)
+            elif f.name in ("position_gradients", "velocity_gradients"):
+                v = v.reshape(-1, 9)
+            setattr(self, f.name, v)
+
+    @property
+    def n(self) -> int:
+        return int(self.flags.shape[0])
+
+    def copy(self) -> "Particles":
+        return Particles(**{f.name: (None if getattr(self, f.name) is None else getattr(self, f.name).copy())
+                            for f in fields(self)})
+
+    def subset(self, index) -> "Particles":
+        return Particles(**{f.name: (None if getattr(self, f.name) is None else getattr(self, f.name)[index].copy())
+                            for f in fields(self)})
+
+    def nbytes(self) -> int:
+        return sum(getattr(self, f.name).nbytes for f in fields(self) if getattr(self, f.name) is not None)
+
+    def to_struct(self, keep=None) -> SvParticles:
+        """SvParticles pointing into these arrays (they must stay alive)."""
+        s = SvParticles()
+        s.n = self.n
+        s.flags = ptr(self.flags, u32p)
+        s.positions = ptr(self.positions, f32p)
+        s.position_gradients = ptr(self.position_gradients, f32p)
+        s.velocities = ptr(self.velocities, f32p)
+        s.velocity_gradients = ptr(self.velocity_gradients, f32p)
+        s.elastic_energies = ptr(self.elastic_energies, f32p)
+        s.collider_bits = ptr(self.collider_bits, u32p)
+        s.mass = ptr(self.mass, f32p)
+        s.initial_volume = ptr(self.initial_volume, f32p)
+        s.viscosity_dynamic = ptr(self.viscosity_dynamic, f32p)
+        s.viscosity_bulk = ptr(self.viscosity_bulk, f32p)
+        s.mu = ptr(self.mu, f32p)
+        s.lambda_ = ptr(self.lambda_, f32p)
+        s.sand_alpha = ptr(self.sand_alpha, f32p)
+        s.exponent = ptr(self.exponent, i32p)
+        s.bulk_modulus = ptr(self.bulk_modulus, f32p)
+        s.model = ptr(self.model, u32p)
+        s.hardening = ptr(self.hardening, f32p)
+        s.crit_compression = ptr(self.crit_compression, f32p)
+        s.crit_stretch = ptr(self.crit_stretch, f32p)
+        s.plastic_j = ptr(self.plastic_j, f32p)
+        return s
+
+
+@dataclass
+class GridNodes:
+    """file_frame::GridNodes (grid_nodes.rs:10-15); nodes with mass > 0."""
+
+    node_ids: np.ndarray
+    collider_bits: np.ndarray
+    masses: np.ndarray
+    velocities: np.ndarray
+
+
+@dataclass
+class IoState:
+    """file_frame::IoState (io_state.rs:11-18)."""
+
+    time: float
+    particles: Particles
+    grid_nodes: Optional[GridNodes] = None
+
+
+@dataclass
+class InputConsts:
+    """The part of file_input::InputConsts (header.rs:10-71) the substep reads."""
+
+    grid_node_size: float
+    domain_min: tuple = (-100.0, -100.0, -100.0)
+    domain_max: tuple = (100.0, 100.0, 100.0)
+    simulation_scale: float = 1.0
+    frames_per_second: int = 24
+
+    def scaled_grid_node_size(self) -> float:
+        return self.grid_node_size / self.simulation_scale
+
+    def scaled_domain_min(self):
+        return tuple(d / self.simulation_scale for d in self.domain_min)
+
+    def scaled_domain_max(self):
+        return tuple(d / self.simulation_scale for d in self.domain_max)
+
+    def seconds_per_frame(self) -> float:
+        return 1.0 / self.frames_per_second
+
+
+@dataclass
+class Extras:
+    """Options the reference does not have: a grid boundary plane, the
+    int32-cell + fp32-offset position form, the fp64 SVD policy and the grid
+    block capacity (0 = automatic)."""
+
+    ground_mode: int = 0  # 0 off, 1 sticky, 2 slip
+    ground_axis: int = 2
+    ground_height: float = 0.0
+    position_form: int = 0
+    svd_fp64_policy: int = 1
+    block_capacity: int = 0
+
+
+@dataclass
+class FrameInput:
+    """The inputs of one frame the substep needs: the (interpolated) gravity
+    (xpu/src/frame_input.rs, interpolate_input.rs:29)."""
+
+    consts: InputConsts
+    gravity: tuple = (0.0, 0.0, -9.8)
+
+
+@dataclass
+class RunParameters:
+    """CpuRunParameters (cpu_state.rs:137-142).  Only adaptive_time_steps =
+    False is implemented by this backend."""
+
+    target_time: float
+    max_time_step: float
+    adaptive_time_steps: bool = False
+    store_grid: bool = False
+
+
+class Harness:
+    """Cooperative cancellation (xpu/src/harness.rs:65-79)."""
+
+    def __init__(self):
+        self._flag = ct.c_int32(0)
+
+    def cancel(self):
+        self._flag.value = 1
+
+    def canceled(self) -> bool:
+        return bool(self._flag.value)
+
+
+class EnergyError(RuntimeError):
+    """A particle's position gradient got det <= 0 (util EnergyError::
+    PositionGradientNonPositive); the state is still returned."""
+
+
+class Canceled(RuntimeError):
+    """The computation was canceled (cpu/src/errors.rs:11)."""
+
+
+class ZeroTimeStep(RuntimeError):
+    """The time step ended up being 0 (cpu/src/errors.rs:23)."""
+
+
+# --------------------------------------------------------------------- backend
+class CudaState:
+    """GB300 backend with the reference CPU backend's call surface."""
+
+    def __init__(self, handle: ct.c_void_p, n: int, time: float, consts: InputConsts, extras: Extras,
+                 initial_positions: Optional[np.ndarray], template: Particles):
+        self._lib = _abi.load()
+        self._h = handle
+        self.n = n
+        self.time = time
+        self.consts = consts
+        self.extras = extras
+        self._initial_positions = initial_positions
+        self._template = template
+
+    # -- from_io_state (cpu_state.rs:25-66)
+    @classmethod
+    def from_io_state(cls, io_state: IoState, consts: InputConsts, extras: Optional[Extras] = None) -> "CudaState":
+        extras = extras or Extras()
+        lib = _abi.load()
+        c = SvConsts()
+        c.grid_node_size = consts.scaled_grid_node_size()
+        for a in range(3):
+            c.domain_min[a] = consts.scaled_domain_min()[a]
+            c.domain_max[a] = consts.scaled_domain_max()[a]
+        c.ground_mode = extras.ground_mode
+        c.ground_axis = extras.ground_axis
+        c.ground_height = extras.ground_height
+        c.position_form = extras.position_form
+        c.svd_fp64_policy = extras.svd_fp64_policy
+        c.block_capacity = extras.block_capacity
+        p = io_state.particles
+        s = p.to_struct()
+        h = ct.c_void_p()
+        check(lib.sv_create(ct.byref(c), ct.byref(s), ct.byref(h)))
+        template = p.subset(slice(0, 0))
+        return cls(h, p.n, io_state.time, consts, extras, p.initial_positions, p)
+
+    def close(self):
+        if self._h:
+            self._lib.sv_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- the substep loop
+    def step(self, n_substeps: int, dt: float, gravity, harness: Optional[Harness] = None):
+        """Runs n_substeps substeps; returns (status bits, substeps done)."""
+        g = np.asarray(gravity, dtype=np.float32)
+        status = ct.c_uint32(0)
+        done = ct.c_uint32(0)
+        cancel = ct.byref(harness._flag) if harness is not None else None
+        check(self._lib.sv_step(self._h, int(n_substeps), float(dt), ptr(g, f32p), cancel, ct.byref(status),
+                                ct.byref(done)))
+        return int(status.value), int(done.value)
+
+    def produce_next_state(self, harness: Harness, frame_input: FrameInput, params: RunParameters):
+        """cpu_state.rs:146-197: advance to target_time in substeps of
+        max_time_step; returns (IoState, error-or-None) where the error is a
+        buffered EnergyError (state still valid).  Canceled / ZeroTimeStep
+        are raised, like the reference's outer Result."""
+        if params.adaptive_time_steps:
+            raise NotImplementedError("adaptive time steps are not part of this backend")
+        dt = np.float32(params.max_time_step)
+        if dt == 0:
+            raise ZeroTimeStep("The time step ended up being 0")
+        # the reference accumulates time in f64 one substep at a time
+        t = self.time
+        n = 0
+        while t < params.target_time:
+            t += float(dt)
+            n += 1
+        status, done = self.step(n, float(dt), frame_input.gravity, harness)
+        error = None
+        if status & _abi.SV_STATUS_PARTICLE_INVERTED:
+            # time is not advanced for the substep that failed (cpu_state.rs:178-183)
+            for _ in range(max(done - 1, 0)):
+                self.time += float(dt)
+            error = EnergyError("The position gradient has negative determinant")
+        else:
+            for _ in range(done):
+                self.time += float(dt)
+        if status & _abi.SV_STATUS_CANCELED:
+            raise Canceled("The computation was canceled")
+        return self.to_io_state(params.store_grid), error
+
+    # -- to_io_state (cpu_state.rs:68-135)
+    def download(self, out: Optional[Particles] = None) -> Particles:
+        t = self._template
+        n = self.n
+        if out is None:
+            out = Particles(
+                flags=np.zeros(n, np.uint32),
+                positions=np.zeros((n, 3), np.float32),
+                position_gradients=np.zeros((n, 9), np.float32),
+                velocities=np.zeros((n, 3), np.float32),
+                velocity_gradients=np.zeros((n, 9), np.float32),
+                mass=t.mass,
+                initial_volume=t.initial_volume,
+                mu=t.mu,
+                lambda_=t.lambda_,
+                sand_alpha=t.sand_alpha,
+                exponent=t.exponent,
+                bulk_modulus=t.bulk_modulus,
+                viscosity_dynamic=t.viscosity_dynamic,
+                viscosity_bulk=t.viscosity_bulk,
+                elastic_energies=np.zeros(n, np.float32),
+                collider_bits=np.zeros(n, np.uint32),
+                initial_positions=self._initial_positions,
+                model=t.model,
+                hardening=t.hardening,
+                crit_compression=t.crit_compression,
+                crit_stretch=t.crit_stretch,
+                plastic_j=np.ones(n, np.float32),
+            )
+        s = out.to_struct()
+        check(self._lib.sv_download(self._h, ct.byref(s)))
+        return out
+
+    def grid(self) -> GridNodes:
+        cnt = ct.c_uint64(0)
+        check(self._lib.sv_download_grid(self._h, None, None, None, 0, ct.byref(cnt)))
+        m = int(cnt.value)
+        ids = np.zeros((m, 3), np.int32)
+        masses = np.zeros(m, np.float32)
+        vel = np.zeros((m, 3), np.float32)
+        check(self._lib.sv_download_grid(self._h, ptr(ids, i32p), ptr(masses, f32p), ptr(vel, f32p), m,
+                                         ct.byref(cnt)))
+        return GridNodes(ids, np.zeros(m, np.uint32), masses, vel)
+
+    def to_io_state(self, store_grid: bool = False) -> IoState:
+        return IoState(self.time, self.download(), self.grid() if store_grid else None)
+
+    # -- inspection
+    def p2g_only(self, dt: float, gravity) -> GridNodes:
+        g = np.asarray(gravity, dtype=np.float32)
+        check(self._lib.sv_p2g_only(self._h, float(dt), ptr(g, f32p)))
+        return self.grid()
+
+    def binning(self):
+        n = self.n
+        keys = np.zeros(n, np.uint32)
+        perm = np.zeros(n, np.uint32)
+        orig = np.zeros(n, np.uint32)
+        check(self._lib.sv_binning(self._h, ptr(keys, u32p), ptr(perm, u32p), ptr(orig, u32p)))
+        return keys, perm, orig
+
+    def grid_layout(self):
+        o = np.zeros(3, np.int32)
+        nb = np.zeros(3, np.int32)
+        check(self._lib.sv_grid_layout(self._h, ptr(o, i32p), ptr(nb, i32p)))
+        return o, nb
+
+    def stats(self) -> dict:
+        s = SvStats()
+        check(self._lib.sv_get_stats(self._h, ct.byref(s)))
+        return {f[0]: int(getattr(s, f[0])) for f in SvStats._fields_}
+
+    def set_stream(self, stream_handle: int):
+        """Queue all work on a caller-owned cudaStream_t (0 = own stream)."""
+        check(self._lib.sv_set_stream(self._h, ct.c_void_p(stream_handle or None)))
+
+    def set_profiling(self, on: bool):
+        check(self._lib.sv_set_profiling(self._h, 1 if on else 0))
+
+    def profile_report(self) -> str:
+        buf = ct.create_string_buffer(1 << 16)
+        check(self._lib.sv_profile_report(self._h, buf, len(buf)))
+        return buf.value.decode()
+
+
+def sort_pairs(keys: np.ndarray) -> np.ndarray:
+    """Stable sorting permutation of u32 keys computed on the GPU."""
+    keys = np.ascontiguousarray(keys, dtype=np.uint32)
+    perm = np.zeros(keys.shape[0], np.uint32)
+    check(_abi.load().sv_sort_pairs(ptr(keys, u32p), ptr(perm, u32p), keys.shape[0]))
+    return perm

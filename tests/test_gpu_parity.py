@@ -1,0 +1,262 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Tolerances: integer and index work (binning keys, sort permutation, node
+sets, flags) must match bit for bit.  Floating-point results are compared by
+norm like the reference's check_iters_by_norm (rust/crates/gpu/src/
+test_util.rs:2738-2764: error <= 1e-6 + rel * |b|), with rel stated per field
+below; summation order differs between the two (float atomics on the GPU,
+node-ordered gathers on the CPU), so bit equality is not expected.
+"""
+
+import numpy as np
+import pytest
+
+from squishy_volumes_gb300 import CudaState, Extras, InputConsts, IoState, scenes, sort_pairs
+from squishy_volumes_gb300._abi import SV_FAILED, SV_IS_SOLID, SV_STATUS_PARTICLE_INVERTED, SV_TOMBSTONED, SvError
+
+pytestmark = pytest.mark.gpu
+
+# Relative tolerances (by norm) per field after a few substeps.
+TOL = {
+    "positions": 1e-6,
+    "velocities": 1e-4,
+    "velocity_gradients": 1e-3,
+    "position_gradients": 1e-5,
+    "elastic_energies": 1e-3,
+}
+
+
+def by_norm(a, b, rel, eps=1e-6):
+    a = np.asarray(a, np.float64).ravel()
+    b = np.asarray(b, np.float64).ravel()
+    err = np.linalg.norm(a - b)
+    scale = max(np.linalg.norm(a), np.linalg.norm(b))
+    return err <= eps + rel * scale, err / max(scale, 1e-30)
+
+
+def compare_states(gpu, ref, live, tol=TOL):
+    for name, rel in tol.items():
+        a = getattr(gpu, name)[live]
+        b = getattr(ref, name)[live]
+        ok, r = by_norm(a, b, rel)
+        assert ok, f"{name}: relative error {r:.3e} > {rel}"
+
+
+# ---------------------------------------------------------------- sort
+@pytest.mark.parametrize("n", [0, 1, 2, 1000, 4097, 100_000])
+def test_sort_pairs_is_stable_sort(cuda_lib, n):
+    rng = np.random.default_rng(n)
+    keys = rng.integers(0, 50, n).astype(np.uint32)  # many duplicates
+    perm = sort_pairs(keys)
+    np.testing.assert_array_equal(perm, np.argsort(keys, kind="stable").astype(np.uint32))
+
+
+def test_sort_pairs_full_32_bit_keys(cuda_lib):
+    rng = np.random.default_rng(42)
+    keys = rng.integers(0, 2**32, 300_000, dtype=np.uint64).astype(np.uint32)
+    keys[::7] = 0xFFFFFFFF
+    perm = sort_pairs(keys)
+    np.testing.assert_array_equal(perm, np.argsort(keys, kind="stable").astype(np.uint32))
+
+
+# ---------------------------------------------------------------- binning
+def test_binning_keys_and_permutation_match_cpu(cuda_lib, oracle_mod):
+    s = scenes.small_mixed()
+    gpu = CudaState.from_io_state(s.io_state, s.consts, s.extras)
+    origin, nb = gpu.grid_layout()
+    keys, perm, orig = gpu.binning()
+    p = s.io_state.particles
+    exp = oracle_mod.binning_keys(p.positions[orig], p.flags[orig], s.consts.grid_node_size, origin, nb)
+    np.testing.assert_array_equal(keys, exp)
+    np.testing.assert_array_equal(perm, oracle_mod.stable_sort_perm(exp))
+    # after substeps the keys come from the G2P epilogue of the last substep
+    gpu.step(3, s.dt, s.gravity)
+    keys, perm, orig = gpu.binning()
+    cur = gpu.download()
+    exp = oracle_mod.binning_keys(cur.positions[orig], cur.flags[orig], s.consts.grid_node_size, origin, nb)
+    np.testing.assert_array_equal(keys, exp)
+    np.testing.assert_array_equal(perm, oracle_mod.stable_sort_perm(exp))
+    # keys are the reference's lexicographic cell order refined to 4^3 blocks:
+    # after a substep the device order is sorted by the previous keys
+    assert np.all(np.diff(keys[perm].astype(np.int64)) >= 0)
+    gpu.close()
+
+
+# ---------------------------------------------------------------- P2G / grid
+@pytest.mark.parametrize("fp64", [False, True])
+def test_p2g_grid_matches_oracle(cuda_lib, oracle_mod, fp64):
+    s = scenes.small_mixed()
+    gpu = CudaState.from_io_state(s.io_state, s.consts, s.extras)
+    g = gpu.p2g_only(s.dt, s.gravity)
+    ref = oracle_mod.OracleState(s.io_state.particles, s.consts, s.extras, fp64=fp64)
+    ref.p2g_only(s.dt, s.gravity)
+    ids, m, v = ref.grid()
+    np.testing.assert_array_equal(g.node_ids, ids)
+    # grid mass: FP32 sums of <= 216 positive terms in a different order
+    np.testing.assert_allclose(g.masses, m, rtol=4e-6, atol=0)
+    ok, r = by_norm(g.velocities, v, 1e-5)
+    assert ok, r
+    gpu.close()
+
+
+def test_p2g_conserves_momentum(cuda_lib):
+    s = scenes.small_mixed()
+    gpu = CudaState.from_io_state(s.io_state, s.consts, Extras())
+    g = gpu.p2g_only(s.dt, s.gravity)
+    p = s.io_state.particles
+    grid_mom = (g.masses[:, None].astype(np.float64) * g.velocities).sum(0)
+    part_mom = (p.mass[:, None].astype(np.float64) * (p.velocities + s.dt * np.asarray(s.gravity, np.float32))).sum(0)
+    scale = (p.mass.astype(np.float64)[:, None] * np.abs(p.velocities)).sum()
+    assert np.all(np.abs(grid_mom - part_mom) <= 1e-6 * scale), (grid_mom, part_mom)
+    np.testing.assert_allclose(g.masses.sum(dtype=np.float64), p.mass.sum(dtype=np.float64), rtol=1e-6)
+    gpu.close()
+
+
+# ---------------------------------------------------------------- whole substeps
+@pytest.mark.parametrize("fp64", [False, True])
+def test_substeps_match_oracle(cuda_lib, oracle_mod, fp64):
+    s = scenes.small_mixed()
+    gpu = CudaState.from_io_state(s.io_state, s.consts, s.extras)
+    status, done = gpu.step(s.substeps, s.dt, s.gravity)
+    assert (status, done) == (0, s.substeps)
+    out = gpu.download()
+    ref = oracle_mod.OracleState(s.io_state.particles, s.consts, s.extras, fp64=fp64)
+    assert ref.step(s.substeps, s.dt, s.gravity) == 0
+    exp = ref.download()
+    np.testing.assert_array_equal(out.flags, exp.flags)
+    live = (exp.flags & SV_TOMBSTONED) == 0
+    compare_states(out, exp, live)
+    np.testing.assert_allclose(out.plastic_j, exp.plastic_j, rtol=1e-5)
+    gpu.close()
+
+
+def test_cube_64k_matches_fp64_oracle(cuda_lib, oracle_mod):
+    s = scenes.cube_64k()
+    gpu = CudaState.from_io_state(s.io_state, s.consts, s.extras)
+    n = 20
+    assert gpu.step(n, s.dt, s.gravity) == (0, n)
+    out = gpu.download()
+    ref = oracle_mod.OracleState(s.io_state.particles, s.consts, s.extras, fp64=True)
+    assert ref.step(n, s.dt, s.gravity) == 0
+    exp = ref.download()
+    np.testing.assert_array_equal(out.flags, exp.flags)
+    compare_states(out, exp, np.ones(out.n, bool))
+    gpu.close()
+
+
+def test_cell_offset_positions_match_fp32_positions(cuda_lib, oracle_mod):
+    s = scenes.small_mixed()
+    a = CudaState.from_io_state(s.io_state, s.consts, Extras(position_form=0))
+    b = CudaState.from_io_state(s.io_state, s.consts, Extras(position_form=1))
+    a.step(s.substeps, s.dt, s.gravity)
+    b.step(s.substeps, s.dt, s.gravity)
+    ra, rb = a.download(), b.download()
+    ref = oracle_mod.OracleState(s.io_state.particles, s.consts, None, fp64=True)
+    ref.step(s.substeps, s.dt, s.gravity)
+    exp = ref.download()
+    live = (exp.flags & SV_TOMBSTONED) == 0
+    compare_states(rb, exp, live)
+    # the cell form is at least as close to the fp64 oracle in position
+    ea = np.linalg.norm(ra.positions[live].astype(np.float64) - exp.positions[live])
+    eb = np.linalg.norm(rb.positions[live].astype(np.float64) - exp.positions[live])
+    assert eb <= ea * 1.5 + 1e-12
+    a.close(), b.close()
+
+
+# ---------------------------------------------------------------- edge cases
+def test_empty_scene(cuda_lib):
+    s = scenes.small_mixed()
+    p = s.io_state.particles.subset(slice(0, 0))
+    gpu = CudaState.from_io_state(IoState(0.0, p), s.consts)
+    assert gpu.step(3, s.dt, s.gravity) == (0, 3)
+    assert gpu.download().n == 0
+    gpu.close()
+
+
+def test_particles_leaving_domain_are_culled(cuda_lib, oracle_mod):
+    s = scenes.small_mixed()
+    p = s.io_state.particles.copy()
+    # shoot some particles out of the domain: strict bounds (cull_particles.rs:29-33)
+    p.velocities[:50] = np.array([0.0, 0.0, -200.0], np.float32)
+    io = IoState(0.0, p)
+    consts = InputConsts(grid_node_size=s.consts.grid_node_size, domain_min=(0.0, 0.0, 0.29),
+                         domain_max=(1.5, 1.5, 1.5))
+    gpu = CudaState.from_io_state(io, consts)
+    gpu.step(4, s.dt, s.gravity)
+    out = gpu.download()
+    ref = oracle_mod.OracleState(p, consts, None, fp64=True)
+    ref.step(4, s.dt, s.gravity)
+    exp = ref.download()
+    np.testing.assert_array_equal(out.flags, exp.flags)
+    assert (out.flags & SV_TOMBSTONED).any()
+    live = (exp.flags & SV_TOMBSTONED) == 0
+    compare_states(out, exp, live)
+    gpu.close()
+
+
+def test_tombstoned_input_is_carried(cuda_lib):
+    s = scenes.small_mixed()
+    p = s.io_state.particles.copy()
+    p.flags[::3] |= SV_TOMBSTONED
+    gpu = CudaState.from_io_state(IoState(0.0, p), s.consts)
+    gpu.step(2, s.dt, s.gravity)
+    out = gpu.download()
+    dead = (p.flags & SV_TOMBSTONED) != 0
+    np.testing.assert_array_equal(out.positions[dead], p.positions[dead])
+    np.testing.assert_array_equal(out.position_gradients[dead], p.position_gradients[dead])
+    gpu.close()
+
+
+def test_inverted_particle_sets_failed_and_stops(cuda_lib):
+    s = scenes.small_mixed()
+    p = s.io_state.particles.copy()
+    # A compressive affine velocity field v = -k (x - c) on the first
+    # (Neo-Hookean) box with k dt = 2: G2P recovers C = -k I and
+    # F += dt C F flips F, so det F < 0 after one substep.
+    box = np.arange(p.n) < p.n // 6
+    c = p.positions[box].mean(0)
+    k = 2.0 / s.dt
+    p.velocities[:] = 0
+    p.velocity_gradients[:] = 0
+    p.position_gradients[:] = np.eye(3, dtype=np.float32).reshape(9)
+    p.velocities[box] = -k * (p.positions[box] - c)
+    p.velocity_gradients[box] = (-k * np.eye(3, dtype=np.float32)).reshape(9)
+    gpu = CudaState.from_io_state(IoState(0.0, p), s.consts)
+    status, done = gpu.step(5, s.dt, (0, 0, 0))
+    assert status & SV_STATUS_PARTICLE_INVERTED
+    assert done == 1
+    out = gpu.download()
+    assert (out.flags[box] & SV_FAILED).any()
+    gpu.close()
+
+
+def test_invalid_flags_rejected(cuda_lib):
+    s = scenes.small_mixed()
+    p = s.io_state.particles.copy()
+    p.flags[3] = 0  # neither solid nor fluid (initialization.rs:197-201)
+    with pytest.raises(SvError):
+        CudaState.from_io_state(IoState(0.0, p), s.consts)
+
+
+def test_capacity_growth(cuda_lib, oracle_mod):
+    s = scenes.small_mixed()
+    small = CudaState.from_io_state(s.io_state, s.consts, Extras(block_capacity=4))
+    big = CudaState.from_io_state(s.io_state, s.consts, Extras())
+    assert small.step(3, s.dt, s.gravity) == (0, 3)
+    big.step(3, s.dt, s.gravity)
+    a, b = small.download(), big.download()
+    compare_states(a, b, np.ones(a.n, bool))
+    small.close(), big.close()
+
+
+def test_cancel_before_start(cuda_lib):
+    from squishy_volumes_gb300 import Harness
+    from squishy_volumes_gb300._abi import SV_STATUS_CANCELED
+
+    s = scenes.small_mixed()
+    gpu = CudaState.from_io_state(s.io_state, s.consts)
+    h = Harness()
+    h.cancel()
+    status, done = gpu.step(10, s.dt, s.gravity, h)
+    assert status & SV_STATUS_CANCELED and done == 0
+    gpu.close()
