@@ -45,6 +45,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scene", default="three_boxes_1m")
+    ap.add_argument("--sort-interval", type=int, default=0,
+                    help="substeps between binning sorts (0 adaptive, 1 every substep like the reference)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bound on the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -151,6 +153,10 @@ def cpu_baseline(scene, seconds_budget: float):
 def algorithmic_bytes(kernel: str, live: int, grid_nodes: int, cell_form: bool):
     """Algorithmic HBM bytes per launch (SURVEY 8d per-unit figures)."""
     x = 12 + (12 if cell_form else 0)
+    if kernel == "g2p2g":
+        # one full particle-substep: read x, v, C, F, material/flags, write
+        # x, v, C, F; grid: scatter writes m + p, gather reads v per node
+        return live * ((x + 12 + 36 + 36 + 4) + (x + 12 + 36 + 36)) + grid_nodes * (16 + 12)
     if kernel == "p2g":
         # read x, v, C, F, material/flags; write grid m + p per active node
         return live * (x + 12 + 36 + 36 + 4) + grid_nodes * 16
@@ -178,6 +184,7 @@ def run_ours(args, rank, world, local):
     scene = scenes.SCENES[args.scene]()
     p = scene.io_state.particles
     n = p.n
+    scene.extras.sort_interval = args.sort_interval
     gpu = CudaState.from_io_state(scene.io_state, scene.consts, scene.extras)
     # warm-up
     status, done = gpu.step(args.warmup, scene.dt, scene.gravity)
@@ -314,6 +321,8 @@ def run_ours(args, rank, world, local):
             "particles": n,
             "live_particles": live,
             "grid_blocks": st["grid_blocks"],
+            "binning_sort_interval": st["sort_interval"],
+            "binning_sorts_in_timed_region": int(stats1["sorts"] - stats0["sorts"]),
             "substep_dt": scene.dt,
             "l2": "state larger than L2 (no flush)",
             "parallelism": "replicas" if world > 1 else "single GPU",

@@ -79,7 +79,12 @@ typedef struct sv_consts {
     uint32_t svd_fp64_policy;
     /* Grid block (4^3 nodes) capacity; 0 = size it from the domain. */
     uint64_t block_capacity;
-    uint32_t reserved[6];
+    /* Substeps between binning sorts: 0 = adaptive (at most 8), 1 = every
+     * substep like the reference (cpu/src/phase/sort.rs, "only to optimize
+     * memory access"), k = every k substeps.  Results do not depend on it
+     * beyond fp32 summation order. */
+    uint32_t sort_interval;
+    uint32_t reserved[5];
 } sv_consts;
 
 typedef struct sv_particles {
@@ -175,6 +180,9 @@ typedef struct sv_stats {
     uint64_t substeps;
     uint64_t device_bytes;      /* device memory held by the handle */
     uint64_t kernel_launches;   /* kernels launched by this handle so far */
+    uint64_t sorts;             /* binning sorts run so far */
+    uint64_t sort_interval;     /* current substeps between binning sorts */
+    uint64_t tile_misses;       /* gathers that missed their block's shared tile (low 32 bits) */
 } sv_stats;
 int sv_get_stats(sv_handle *h, sv_stats *out);
 

@@ -45,7 +45,8 @@ class SvConsts(ct.Structure):
         ("position_form", ct.c_uint32),
         ("svd_fp64_policy", ct.c_uint32),
         ("block_capacity", ct.c_uint64),
-        ("reserved", ct.c_uint32 * 6),
+        ("sort_interval", ct.c_uint32),
+        ("reserved", ct.c_uint32 * 5),
     ]
 
 
@@ -86,6 +87,9 @@ class SvStats(ct.Structure):
         ("substeps", ct.c_uint64),
         ("device_bytes", ct.c_uint64),
         ("kernel_launches", ct.c_uint64),
+        ("sorts", ct.c_uint64),
+        ("sort_interval", ct.c_uint64),
+        ("tile_misses", ct.c_uint64),
     ]
 
 

@@ -49,7 +49,8 @@ void free_handle(sv_handle *h) {
     for (auto &s : h->side) free_side(s);
     cudaFree(h->materials), cudaFree(h->keys), cudaFree(h->sorted_keys), cudaFree(h->perm), cudaFree(h->sort_temp);
     cudaFree(h->seg_start), cudaFree(h->seg_block), cudaFree(h->tile_counts), cudaFree(h->scan_temp);
-    cudaFree(h->blockmap), cudaFree(h->active_blocks), cudaFree(h->grid), cudaFree(h->counters);
+    for (int s = 0; s < 2; ++s) cudaFree(h->blockmap[s]), cudaFree(h->active[s]), cudaFree(h->grid[s]);
+    cudaFree(h->counters);
     if (h->host_counters) cudaFreeHost(h->host_counters);
     for (auto &p : h->timer.pending) cudaEventDestroy(p.second.first), cudaEventDestroy(p.second.second);
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -140,40 +141,70 @@ int build_material(const sv_particles *p, uint64_t i, Material &m, std::string &
     return 0;
 }
 
+// (Re)allocates both grids and both slot lists with `capacity` blocks.  The
+// slot lists are copied so the block maps can still be reset from them.
 cudaError_t alloc_grid(sv_handle *h, uint64_t capacity) {
     cudaError_t e;
-    uint32_t *active = nullptr;
-    float4 *grid = nullptr;
-    if ((e = dalloc(h, &active, capacity)) != cudaSuccess) return e;
-    if ((e = dalloc(h, &grid, capacity * 64)) != cudaSuccess) {
-        cudaFree(active);
-        return e;
+    uint32_t *active[2] = {nullptr, nullptr};
+    float4 *grid[2] = {nullptr, nullptr};
+    for (int s = 0; s < 2; ++s) {
+        if ((e = dalloc(h, &active[s], capacity)) != cudaSuccess || (e = dalloc(h, &grid[s], capacity * 64)) != cudaSuccess) {
+            for (int t = 0; t < 2; ++t) cudaFree(active[t]), cudaFree(grid[t]);
+            return e;
+        }
     }
-    if (h->active_blocks) {
-        // keep the previous substep's slot list so the block map can be reset
-        cudaMemcpyAsync(active, h->active_blocks, std::min(capacity, h->capacity) * 4, cudaMemcpyDeviceToDevice,
-                        h->stream);
-        cudaStreamSynchronize(h->stream);
-        cudaFree(h->active_blocks);
-        cudaFree(h->grid);
-        h->device_bytes -= h->capacity * 4 + h->capacity * 64 * sizeof(float4);
+    cudaStreamSynchronize(h->stream);
+    for (int s = 0; s < 2; ++s) {
+        if (h->active[s]) {
+            cudaMemcpy(active[s], h->active[s], std::min(capacity, h->capacity) * 4, cudaMemcpyDeviceToDevice);
+            cudaFree(h->active[s]);
+            cudaFree(h->grid[s]);
+            h->device_bytes -= h->capacity * 4 + h->capacity * 64 * sizeof(float4);
+        }
+        h->active[s] = active[s];
+        h->grid[s] = grid[s];
     }
-    h->active_blocks = active;
-    h->grid = grid;
     h->capacity = capacity;
     return cudaSuccess;
 }
 
-int run_substep(sv_handle *h, float dt, float3 g, bool advance) {
+// Scatter of the current state into grid[gcur] after a fresh binning: the
+// start of a run, or the recovery after a particle left its claimed blocks.
+int standalone_p2g(sv_handle *h, float dt, float3 g) {
     if (!h->keys_valid) SV_CUDA(launch_keys(h));
     SV_CUDA(launch_sort_and_segments(h));
-    SV_CUDA(launch_grid_activate(h));
+    const int which = h->map_cur ^ 1;
+    SV_CUDA(launch_activate(h, which));
+    h->map_cur = h->map_next = which;
+    SV_CUDA(launch_clear(h, h->gcur, which));
     SV_CUDA(launch_p2g(h, dt, g));
-    SV_CUDA(launch_grid_update(h));
-    if (advance) {
-        SV_CUDA(launch_g2p(h, dt));
-        SV_CUDA(launch_finish_substep(h));
+    h->pending_valid = true;
+    h->pending_dt = dt;
+    h->pending_g[0] = g.x, h->pending_g[1] = g.y, h->pending_g[2] = g.z;
+    h->need_perm = true;
+    h->since_sort = 0;
+    return 0;
+}
+
+// One substep: (every sort_interval substeps) binning sort and block claims
+// for the next grid, grid update, fused gather/advance/scatter.
+int fused_substep(sv_handle *h, float dt, float3 g) {
+    if (h->since_sort >= h->sort_interval) {
+        if (!h->keys_valid) SV_CUDA(launch_keys(h));
+        SV_CUDA(launch_sort_and_segments(h));
+        const int which = h->map_cur ^ 1;
+        SV_CUDA(launch_activate(h, which));
+        h->map_next = which;
+        h->need_perm = true;
+        h->since_sort = 0;
+    } else {
+        h->map_next = h->map_cur;
     }
+    SV_CUDA(launch_grid_update(h, true));
+    const bool write_keys = h->since_sort + 1 >= h->sort_interval;
+    SV_CUDA(launch_g2p2g(h, dt, g, write_keys, h->need_perm));
+    h->need_perm = false;
+    h->since_sort += 1;
     return 0;
 }
 
@@ -257,9 +288,12 @@ int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) {
 
     sv_handle *h = new sv_handle();
     h->n = n;
-    for (auto &m : mats) {
-        h->any_snow |= m.kind == KIND_SNOW;
-        h->any_fcr |= m.kind == KIND_FIXED_COROTATED;
+    if (c->sort_interval == 0) {
+        h->adaptive_interval = true;
+        h->sort_interval = h->max_interval = 8;
+    } else {
+        h->adaptive_interval = false;
+        h->sort_interval = h->max_interval = c->sort_interval;
     }
     GridLayout &L = h->layout;
     L.dx = c->grid_node_size;
@@ -332,7 +366,8 @@ int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) {
     if ((e = dalloc(h, (char **)&h->sort_temp, h->sort_temp_bytes)) || (e = dalloc(h, &h->tile_counts, tiles)) ||
         (e = dalloc(h, (char **)&h->scan_temp, scan_temp_bytes(tiles))))
         return cuda_fail(e, "sort buffers");
-    if ((e = dalloc(h, &h->blockmap, total))) return cuda_fail(e, "block map");
+    if ((e = dalloc(h, &h->blockmap[0], total)) || (e = dalloc(h, &h->blockmap[1], total)))
+        return cuda_fail(e, "block map");
     uint64_t cap = c->block_capacity ? c->block_capacity : std::min<uint64_t>(total, std::max<uint64_t>(65536, n / 4));
     if ((e = alloc_grid(h, cap))) return cuda_fail(e, "grid");
     if ((e = cudaMallocHost((void **)&h->host_counters, C_COUNT * sizeof(uint32_t)))) return cuda_fail(e, "pinned");
@@ -380,7 +415,8 @@ int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) {
             (e = cudaMemcpy(a.energy, en.data(), n * 4, cudaMemcpyHostToDevice)) ||
             (e = cudaMemcpy(a.orig, orig.data(), n * 4, cudaMemcpyHostToDevice)) ||
             (e = cudaMemcpy(h->materials, mats.data(), mats.size() * sizeof(Material), cudaMemcpyHostToDevice)) ||
-            (e = cudaMemset(h->blockmap, 0xFF, total * 4)) || (e = cudaMemset(h->counters, 0, C_COUNT * 4)))
+            (e = cudaMemset(h->blockmap[0], 0xFF, total * 4)) || (e = cudaMemset(h->blockmap[1], 0xFF, total * 4)) ||
+            (e = cudaMemset(h->counters, 0, C_COUNT * 4)))
             return cuda_fail(e, "upload");
     }
     h->collider_bits.assign(n, 0);
@@ -400,8 +436,19 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
     if (!(dt > 0.f)) return fail("sv_step: dt must be positive");  // cpu_state.rs:170-172 ZeroTimeStep
     float3 g = gravity ? make_float3(gravity[0], gravity[1], gravity[2]) : make_float3(0.f, 0.f, 0.f);
     if (read_counters(h)) return -1;
-    uint32_t base = h->host_counters[C_SUBSTEPS];
-    uint32_t fp64_before = h->host_counters[C_FP64];
+    // A previous energy error does not carry over: the reference checks each
+    // substep afresh (cpu_state.rs:178-183).
+    if (h->host_counters[C_STATUS] & ST_INVERTED) {
+        h->host_counters[C_STATUS] &= ~ST_INVERTED;
+        SV_CUDA(cudaMemcpyAsync(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice, h->stream));
+        h->pending_valid = false;
+    }
+    const bool same_inputs = h->pending_valid && h->pending_dt == dt && h->pending_g[0] == g.x &&
+                             h->pending_g[1] == g.y && h->pending_g[2] == g.z;
+    if (!same_inputs) h->pending_valid = false;
+    const uint32_t base = h->host_counters[C_SUBSTEPS];
+    const uint32_t fp64_before = h->host_counters[C_FP64];
+    uint32_t fallback_before = h->host_counters[C_FALLBACK];
     uint32_t status = 0;
     uint32_t done = 0;
     const uint32_t chunk = 64;
@@ -410,27 +457,43 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
             status |= SV_STATUS_CANCELED;
             break;
         }
-        uint32_t todo = std::min(chunk, n_substeps - done);
+        const uint32_t todo = std::min(chunk, n_substeps - done);
+        if (!h->pending_valid && standalone_p2g(h, dt, g)) return -1;
         for (uint32_t s = 0; s < todo; ++s)
-            if (run_substep(h, dt, g, true)) return -1;
+            if (fused_substep(h, dt, g)) return -1;
         if (read_counters(h)) return -1;
-        uint32_t st = h->host_counters[C_STATUS];
+        const uint32_t st = h->host_counters[C_STATUS];
         done = h->host_counters[C_SUBSTEPS] - base;
         if (st & ST_OUT_OF_GRID) return fail("sv_step: a live particle left the grid block index");
-        if (st & ST_CAPACITY) {
-            // Grow and redo the substeps that were skipped (gpu_state.rs:562-599
-            // redoes a frame with doubled capacity).
-            uint64_t cap = std::min<uint64_t>(h->layout.total_blocks, h->capacity * 2);
-            if (cap <= h->capacity) return fail("sv_step: grid block capacity exhausted");
-            SV_CUDA(alloc_grid(h, cap));
-            h->host_counters[C_STATUS] &= ~ST_CAPACITY;
+        if (st & (ST_CAPACITY | ST_MOVED_FAR)) {
+            if (st & ST_CAPACITY) {
+                // Grow and redo what was skipped (gpu_state.rs:562-599 redoes a
+                // frame with doubled capacity).
+                const uint64_t cap = std::min<uint64_t>(h->layout.total_blocks, h->capacity * 2);
+                if (cap <= h->capacity) return fail("sv_step: grid block capacity exhausted");
+                SV_CUDA(alloc_grid(h, cap));
+            }
+            // A particle left the blocks claimed at the last binning: its
+            // scatter is incomplete, so bin again and redo the scatter.
+            if (st & ST_MOVED_FAR) h->sort_interval = std::max<uint32_t>(1, h->sort_interval / 2);
+            h->host_counters[C_STATUS] &= ~(ST_CAPACITY | ST_MOVED_FAR);
             SV_CUDA(cudaMemcpyAsync(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice,
                                     h->stream));
             SV_CUDA(cudaStreamSynchronize(h->stream));
+            h->pending_valid = false;
             continue;
         }
+        if (h->adaptive_interval && todo > 0) {
+            // Bin more often when many gathers miss their shared tile, less
+            // often when almost none do.
+            const double miss = (double)(h->host_counters[C_FALLBACK] - fallback_before) / ((double)h->n * todo + 1.0);
+            if (miss > 0.02 && h->sort_interval > 1) h->sort_interval /= 2;
+            else if (miss < 0.002 && h->sort_interval < h->max_interval) h->sort_interval *= 2;
+        }
+        fallback_before = h->host_counters[C_FALLBACK];
         if (st & ST_INVERTED) {
             status |= SV_STATUS_PARTICLE_INVERTED;
+            h->pending_valid = false;
             break;
         }
     }
@@ -445,12 +508,13 @@ int sv_p2g_only(sv_handle *h, float dt, const float gravity[3]) {
     g_last_error.clear();
     if (!h) return fail("sv_p2g_only: NULL handle");
     float3 g = gravity ? make_float3(gravity[0], gravity[1], gravity[2]) : make_float3(0.f, 0.f, 0.f);
-    if (run_substep(h, dt, g, false)) return -1;
-    // record the slot list for the next block-map reset, without counting a substep
+    if (standalone_p2g(h, dt, g)) return -1;
+    SV_CUDA(launch_grid_update(h, false));
+    h->vel_side = h->gcur;
+    h->vel_map = h->map_cur;
+    // the grid now holds velocities: the next substep scatters again
+    h->pending_valid = false;
     if (read_counters(h)) return -1;
-    uint32_t slots = std::min<uint64_t>(h->host_counters[C_NSLOT], h->capacity);
-    SV_CUDA(cudaMemcpyAsync(h->counters + C_NSLOT_PREV, &slots, 4, cudaMemcpyHostToDevice, h->stream));
-    SV_CUDA(cudaStreamSynchronize(h->stream));
     if (h->host_counters[C_STATUS] & ST_CAPACITY) return fail("sv_p2g_only: grid block capacity exceeded");
     return 0;
 }
@@ -507,12 +571,12 @@ int sv_download_grid(sv_handle *h, int32_t *node_ids, float *masses, float *velo
     g_last_error.clear();
     if (!h) return fail("sv_download_grid: NULL handle");
     if (read_counters(h)) return -1;
-    uint64_t slots = std::min<uint64_t>(h->host_counters[C_NSLOT_PREV], h->capacity);
+    uint64_t slots = h->vel_side < 0 ? 0 : std::min<uint64_t>(h->host_counters[C_NSLOT0 + h->vel_map], h->capacity);
     std::vector<uint32_t> active(slots);
     std::vector<float4> g(slots * 64);
     if (slots) {
-        SV_CUDA(cudaMemcpy(active.data(), h->active_blocks, slots * 4, cudaMemcpyDeviceToHost));
-        SV_CUDA(cudaMemcpy(g.data(), h->grid, slots * 64 * sizeof(float4), cudaMemcpyDeviceToHost));
+        SV_CUDA(cudaMemcpy(active.data(), h->active[h->vel_map], slots * 4, cudaMemcpyDeviceToHost));
+        SV_CUDA(cudaMemcpy(g.data(), h->grid[h->vel_side], slots * 64 * sizeof(float4), cudaMemcpyDeviceToHost));
     }
     struct Node {
         int32_t id[3];
@@ -554,6 +618,8 @@ int sv_binning(sv_handle *h, uint32_t *keys, uint32_t *perm, uint32_t *original_
     if (!h) return fail("sv_binning: NULL handle");
     if (!h->keys_valid) SV_CUDA(launch_keys(h));
     SV_CUDA(launch_sort_and_segments(h));
+    // the segments changed: the next substep bins and scatters afresh
+    h->pending_valid = false;
     SV_CUDA(cudaStreamSynchronize(h->stream));
     const uint64_t n = h->n;
     if (keys) SV_CUDA(cudaMemcpy(keys, h->keys, n * 4, cudaMemcpyDeviceToHost));
@@ -597,11 +663,14 @@ int sv_get_stats(sv_handle *h, sv_stats *out) {
     out->particles = h->n;
     out->live_particles = h->host_counters[C_NLIVE];
     out->particle_blocks = h->host_counters[C_NSEG];
-    out->grid_blocks = h->host_counters[C_NSLOT_PREV];
+    out->grid_blocks = h->host_counters[C_NSLOT0 + h->map_cur];
     out->fp64_svd = h->fp64_total;
     out->substeps = h->substeps_total;
     out->device_bytes = h->device_bytes;
     out->kernel_launches = h->launches;
+    out->sorts = h->sorts;
+    out->sort_interval = h->sort_interval;
+    out->tile_misses = h->host_counters[C_FALLBACK];
     return 0;
 }
 

@@ -25,19 +25,21 @@ constexpr uint32_t SENTINEL_KEY = 0xFFFFFFFFu;
 constexpr uint32_t ST_CAPACITY = SV_STATUS_CAPACITY_EXCEEDED;
 constexpr uint32_t ST_INVERTED = SV_STATUS_PARTICLE_INVERTED;
 constexpr uint32_t ST_OUT_OF_GRID = 1u << 4;  // a live particle left the block index
-constexpr uint32_t STOP_MASK = ST_CAPACITY | ST_INVERTED | ST_OUT_OF_GRID;
+constexpr uint32_t ST_MOVED_FAR = 1u << 5;    // a particle left the blocks claimed at binning
+constexpr uint32_t STOP_MASK = ST_CAPACITY | ST_INVERTED | ST_OUT_OF_GRID | ST_MOVED_FAR;
 
-// Device counters (one u32/u64 array so one copy reads them all).
+// Device counters (one array so one copy reads them all).
 enum Counter : int {
     C_STATUS = 0,
-    C_NSEG = 1,       // particle blocks (segments) this substep
-    C_NSLOT = 2,      // grid blocks claimed this substep
-    C_NSLOT_PREV = 3, // grid blocks of the previous substep (to reset the block map)
-    C_NLIVE = 4,      // live particles (segments cover [0, n_live))
-    C_SUBSTEPS = 5,   // substeps completed
-    C_FP64 = 6,       // particles that took the fp64 SVD (low 32 bits)
-    C_STOP = 7,       // STOP_MASK bits latched for the kernels that follow
-    C_COUNT = 8,
+    C_NSEG = 1,      // particle blocks (segments) of the last binning
+    C_NSLOT0 = 2,    // grid blocks claimed in block map 0
+    C_NSLOT1 = 3,    // grid blocks claimed in block map 1
+    C_NLIVE = 4,     // live particles at the last binning (segments cover [0, n_live))
+    C_SUBSTEPS = 5,  // substeps completed
+    C_FP64 = 6,      // particles that took the fp64 SVD
+    C_STOP = 7,      // STOP_MASK bits latched for the kernels that follow
+    C_FALLBACK = 8,  // gathers that missed their segment's shared tile
+    C_COUNT = 12,
 };
 
 // One side of the particle state (ping-pong).  Structure of arrays: pos and
@@ -78,11 +80,10 @@ struct KernelTimer {
 struct sv_handle {
     sv::GridLayout layout;
     uint64_t n = 0;
-    int cur = 0;
+    int cur = 0;  // particle side holding the state
     sv::ParticleArrays side[2] = {};
     sv::Material *materials = nullptr;
     uint32_t n_materials = 0;
-    bool any_snow = false, any_fcr = false;
 
     uint32_t *keys = nullptr;         // [n] binning keys in device order (valid when keys_valid)
     bool keys_valid = false;
@@ -96,10 +97,27 @@ struct sv_handle {
     uint32_t *tile_counts = nullptr;
     void *scan_temp = nullptr;
 
-    int32_t *blockmap = nullptr;       // [total_blocks] slot or -1
-    uint32_t *active_blocks = nullptr; // [capacity]
-    float4 *grid = nullptr;            // [capacity * 64] (px, py, pz, m) -> (vx, vy, vz, m)
+    // Two grids (the one gathered from and the one scattered into) and two
+    // block maps (dense block index -> slot), swapped when the binning is redone.
+    int32_t *blockmap[2] = {nullptr, nullptr};
+    uint32_t *active[2] = {nullptr, nullptr};
+    float4 *grid[2] = {nullptr, nullptr};  // [capacity * 64] (px, py, pz, m) -> (vx, vy, vz, m)
     uint64_t capacity = 0;
+    int gcur = 0;      // grid holding the pending scatter (momentum form)
+    int map_cur = 0;   // block map of grid[gcur]
+    int map_next = 0;  // block map of the grid being scattered into
+    int vel_side = -1, vel_map = 0;  // grid with the last velocities (for sv_download_grid)
+
+    // The pending grid is the scatter of the current state for the next
+    // substep, made with these dt and gravity.
+    bool pending_valid = false;
+    float pending_dt = 0.f;
+    float pending_g[3] = {0.f, 0.f, 0.f};
+    bool need_perm = true;   // state not yet in the order of the last binning
+    uint32_t since_sort = 0;
+    uint32_t sort_interval = 8;  // current interval between binning sorts
+    uint32_t max_interval = 8;
+    bool adaptive_interval = true;
 
     uint32_t *counters = nullptr;       // device [C_COUNT]
     uint32_t *host_counters = nullptr;  // pinned mirror
@@ -110,6 +128,7 @@ struct sv_handle {
     uint64_t fp64_total = 0;
     uint64_t substeps_total = 0;
     uint64_t launches = 0;  // kernels launched by this handle
+    uint64_t sorts = 0;     // binning sorts run
 
     // host-side copies of what the substep never changes
     std::vector<uint32_t> collider_bits;
@@ -124,11 +143,11 @@ namespace sv {
 // device memory, so a substep needs no host synchronisation.
 cudaError_t launch_keys(sv_handle *h);
 cudaError_t launch_sort_and_segments(sv_handle *h);
-cudaError_t launch_grid_activate(sv_handle *h);
+cudaError_t launch_activate(sv_handle *h, int which);
+cudaError_t launch_clear(sv_handle *h, int grid_side, int which);
 cudaError_t launch_p2g(sv_handle *h, float dt, float3 gravity);
-cudaError_t launch_grid_update(sv_handle *h);
-cudaError_t launch_g2p(sv_handle *h, float dt);
-cudaError_t launch_finish_substep(sv_handle *h);
+cudaError_t launch_grid_update(sv_handle *h, bool clear_next);
+cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 gravity, bool write_keys, bool use_perm);
 
 // Per-kernel timing hooks.
 void timer_begin(sv_handle *h, const char *name, cudaEvent_t *start);

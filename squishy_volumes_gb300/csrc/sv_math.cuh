@@ -148,6 +148,75 @@ __device__ __forceinline__ void svd3(const Mat3<T> &F, Mat3<T> &U, T S[3], Mat3<
     }
 }
 
+// fp32 one-sided Jacobi tuned for throughput: the column norms are updated
+// in closed form after each rotation (|a_p|^2 -= t g, |a_q|^2 += t g), the
+// rotation uses fast reciprocal / square-root intrinsics (any angle close to
+// the optimal one still reduces the off-diagonal, and c^2 + s^2 = 1 keeps V
+// orthogonal), and sweeps stop once every pair is orthogonal to 1e-6
+// relative -- below fp32 resolution of the products formed from the result.
+__device__ __forceinline__ void svd3_fast(const m3f &F, m3f &U, float S[3], m3f &V) {
+    float A[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) A[i] = F.a[i];
+    float W[9] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
+    float nrm[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) nrm[c] = A[c * 3] * A[c * 3] + A[c * 3 + 1] * A[c * 3 + 1] + A[c * 3 + 2] * A[c * 3 + 2];
+    for (int sweep = 0; sweep < 6; ++sweep) {
+        float off = 0.f;
+#pragma unroll
+        for (int pq = 0; pq < 3; ++pq) {
+            const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+            const float g = A[p * 3] * A[q * 3] + A[p * 3 + 1] * A[q * 3 + 1] + A[p * 3 + 2] * A[q * 3 + 2];
+            const float np = nrm[p], nq = nrm[q];
+            off = fmaxf(off, __fdividef(g * g, fmaxf(np * nq, 1e-30f)));
+            if (g != 0.f) {
+                const float d = nq - np, e = 2.f * g;
+                const float r2 = d * d + e * e;
+                const float r = r2 * rsqrtf(r2);
+                float t = __fdividef(e, fabsf(d) + r);
+                t = d < 0.f ? -t : t;
+                const float c = rsqrtf(1.f + t * t), s = c * t;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float ap = A[p * 3 + k], aq = A[q * 3 + k];
+                    A[p * 3 + k] = c * ap - s * aq;
+                    A[q * 3 + k] = s * ap + c * aq;
+                    const float wp = W[p * 3 + k], wq = W[q * 3 + k];
+                    W[p * 3 + k] = c * wp - s * wq;
+                    W[q * 3 + k] = s * wp + c * wq;
+                }
+                nrm[p] = np - t * g;
+                nrm[q] = nq + t * g;
+            }
+        }
+        if (off < 1e-12f) break;
+    }
+    bool good[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float n2 = A[c * 3] * A[c * 3] + A[c * 3 + 1] * A[c * 3 + 1] + A[c * 3 + 2] * A[c * 3 + 2];
+        const float inv = n2 > 1e-30f ? rsqrtf(n2) : 0.f;
+        S[c] = n2 * inv;
+        good[c] = n2 > 1e-30f;
+        U.a[c * 3] = A[c * 3] * inv, U.a[c * 3 + 1] = A[c * 3 + 1] * inv, U.a[c * 3 + 2] = A[c * 3 + 2] * inv;
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) V.a[i] = W[i];
+    if (!(good[0] && good[1] && good[2])) {
+        // Degenerate F: fall back to the general path in fp64 for U.
+        m3d Fd, Ud, Vd;
+        double Sd[3];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Fd.a[i] = (double)F.a[i];
+        svd3<double>(Fd, Ud, Sd, Vd, 12);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) U.a[i] = (float)Ud.a[i], V.a[i] = (float)Vd.a[i];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) S[i] = (float)Sd[i];
+    }
+}
+
 // ---------------------------------------------------------------- weights
 // Quadratic B-spline weights of the three nodes base, base+1, base+2 for a
 // particle at fx = x/dx - base in [0.5, 1.5) (rust/crates/cpu/src/kernels.rs:17-26

@@ -4,22 +4,29 @@
 // (cpu/src/phase/mod.rs:27-41) with adaptive time steps off:
 //   Sort -> ExternalForce -> UpdateGridNodes -> ScatterMomentum -> MeldGrid
 //   -> CollectVelocity -> AdvanceParticles -> CullParticles.
-// GB300 design:
-//   keys      binning key per particle (written by the previous substep's G2P)
-//   sort      stable radix sort of the keys -> permutation; 4^3-block segments
-//   activate  claim the grid blocks each particle block touches (dense block
-//             index -> slot), clear them
-//   p2g       one CTA per particle block: stress + APIC momentum accumulated in
-//             a shared-memory 6^3-node halo tile, flushed with float4 atomics
-//             (ScatterMomentum, scatter_momentum.rs:22-93; the external force,
-//             external_force.rs:17-50, is applied on the fly)
-//   grid      momentum -> velocity (MeldGrid, meld_grid.rs:16-69) + optional
-//             boundary plane
-//   g2p       one CTA per particle block: the 6^3 velocity tile staged in shared
-//             memory, v/C gather (collect_velocity.rs:19-75), x/F advance and
-//             plasticity (advance_particles.rs:17-93), cull
-//             (cull_particles.rs:17-41); writes the next state in sorted order
-//             and the next binning keys.
+//
+// GB300 design.  Substep t+1's scatter is fused into substep t's gather, so
+// each particle is read once and written once per substep and its 3x3 SVD is
+// computed once:
+//
+//   grid      momentum -> velocity on grid G_t (MeldGrid, meld_grid.rs:16-69,
+//             plus the optional boundary plane), and clears G_t+1
+//   g2p2g     one CTA per 4^3 particle block ("segment"): the 8^3-node velocity
+//             tile of G_t staged in shared memory; thread per particle: gather
+//             v and C (collect_velocity.rs:19-75), advance x and F, plasticity
+//             and energy (advance_particles.rs:17-93), cull
+//             (cull_particles.rs:17-41), write the new state; then the external
+//             force of substep t+1 (external_force.rs:17-50) and its stress
+//             (scatter_momentum.rs:22-93) into a per-particle scatter record.
+//             Warps then replay the records with one lane per stencil node,
+//             accumulating runs of same-cell particles in registers, into the
+//             8^3-node shared tile of G_t+1, flushed with float4 atomics.
+//   sort      every `sort_interval` substeps: binning keys, a stable radix sort
+//             (bit-exact against a CPU stable sort) and the 4^3-block
+//             segments; the grid blocks of the next substeps are claimed for
+//             the 27-block neighbourhood of every particle block.
+// Particles that drift out of their segment's tile take a global-memory path;
+// a particle that leaves the claimed blocks makes the host redo the binning.
 #include <cstdio>
 
 #include "sv_internal.h"
@@ -29,27 +36,36 @@ namespace sv {
 
 namespace {
 
-constexpr int P2G_THREADS = 256;
-constexpr int G2P_THREADS = 256;
+constexpr int PT = 128;  // threads (and particles per chunk) of the particle kernels
 constexpr int ELEM_THREADS = 256;
-constexpr int SEG_TILE = 2048;  // elements per tile of the segment builder
+constexpr int SEG_TILE = 2048;
 constexpr int SEG_ITEMS = SEG_TILE / ELEM_THREADS;
+constexpr int TN = 8;  // tile edge in nodes: block nodes 4b..4b+3 plus 1 below, 3 above
+constexpr int TILE_NODES = TN * TN * TN;
+constexpr uint32_t REC_NONE = 0xFFFFFFFFu;
+constexpr uint32_t REC_GLOBAL = 0x80000000u;
 
-// Shared halo tile of 6^3 nodes.  Strides chosen so that the 27 stencil
-// offsets of one cell land in 27 distinct banks (9i + 3j + k mod 32).
-constexpr int TS_Z = 1, TS_Y = 35, TS_X = 233;
-constexpr int TILE_PLANE = 5 * TS_X + 5 * TS_Y + 5 * TS_Z + 1;  // 1341
+// Scatter record of one particle: for stencil offset (i, j, k) the node gets
+// mass w m and momentum w (p0[i] + p1[j] + p2[k]) with w = p0[i].w p1[j].w
+// p2[k].w -- the APIC/MLS momentum m v + A (x_i - x_p) split by axis.
+struct Rec {
+    float4 p[9];
+};
+
+enum Mode { MODE_P2G = 0, MODE_G2P2G = 1 };
 
 struct StepArgs {
     ParticleArrays in, out;
     const Material *mats;
     uint32_t *counters;
-    const uint32_t *perm;
+    const uint32_t *perm;  // nullptr: identity
     const uint32_t *seg_start;
     const uint32_t *seg_block;
-    const int32_t *blockmap;
-    float4 *grid;
-    uint32_t *keys_out;
+    const int32_t *map_cur;   // block -> slot of the grid being gathered (G2P2G)
+    const int32_t *map_next;  // block -> slot of the grid being scattered into
+    const float4 *grid_cur;
+    float4 *grid_next;
+    uint32_t *keys_out;  // nullptr: keys not needed after this substep
     uint64_t n;
     GridLayout L;
     float dt;
@@ -67,27 +83,34 @@ __device__ __forceinline__ void block_coords(uint32_t b, const GridLayout &L, in
     bx = (int)(r / (uint32_t)L.nb[1]);
 }
 
-// Neighbour t in {0,1}^3 (bit 2 = x, bit 1 = y, bit 0 = z) of block b.
-__device__ __forceinline__ uint32_t neighbour_block(uint32_t b, int t, const GridLayout &L) {
-    return b + (uint32_t)(((t >> 2) & 1) * L.nb[1] * L.nb[2] + ((t >> 1) & 1) * L.nb[2] + (t & 1));
+// Neighbour t in [0, 27) of block b: offsets (t/9 - 1, (t/3)%3 - 1, t%3 - 1).
+__device__ __forceinline__ uint32_t neighbour27(uint32_t b, int t, const GridLayout &L) {
+    int dxb = t / 9 - 1, dyb = (t / 3) % 3 - 1, dzb = t % 3 - 1;
+    return (uint32_t)((int64_t)b + (int64_t)dxb * L.nb[1] * L.nb[2] + (int64_t)dyb * L.nb[2] + dzb);
 }
 
-// Binning key of a base cell given in global node coordinates.
+// Binning key of a base cell (global node coordinates); valid particles keep
+// one spare block on every side of their own for the 27-neighbourhood.
 __device__ __forceinline__ uint32_t cell_key(int cx, int cy, int cz, const GridLayout &L, bool &ok) {
     int lx = cx - L.origin[0], ly = cy - L.origin[1], lz = cz - L.origin[2];
-    ok = lx >= 0 && ly >= 0 && lz >= 0 && (lx >> 2) < L.nb[0] - 1 && (ly >> 2) < L.nb[1] - 1 &&
-         (lz >> 2) < L.nb[2] - 1;
+    ok = lx >= 4 && ly >= 4 && lz >= 4 && (lx >> 2) < L.nb[0] - 1 && (ly >> 2) < L.nb[1] - 1 && (lz >> 2) < L.nb[2] - 1;
     if (!ok) return SENTINEL_KEY;
     uint32_t block = ((uint32_t)(lx >> 2) * (uint32_t)L.nb[1] + (uint32_t)(ly >> 2)) * (uint32_t)L.nb[2] + (uint32_t)(lz >> 2);
     return block << 6 | (uint32_t)((lx & 3) << 4 | (ly & 3) << 2 | (lz & 3));
 }
 
-// Particle position in grid units: base cell (global node index of the
-// lowest stencil node, floor(x/dx - 0.5) as kernels.rs:46-49) and fx = x/dx -
-// base in [0.5, 1.5).
+// Slot of the block holding global node (x, y, z), or -1.
+__device__ __forceinline__ int32_t node_slot(const int32_t *map, int x, int y, int z, const GridLayout &L, int &local) {
+    int lx = x - L.origin[0], ly = y - L.origin[1], lz = z - L.origin[2];
+    if (lx < 0 || ly < 0 || lz < 0 || (lx >> 2) >= L.nb[0] || (ly >> 2) >= L.nb[1] || (lz >> 2) >= L.nb[2]) return -1;
+    local = (lx & 3) * 16 + (ly & 3) * 4 + (lz & 3);
+    return map[((uint32_t)(lx >> 2) * (uint32_t)L.nb[1] + (uint32_t)(ly >> 2)) * (uint32_t)L.nb[2] + (uint32_t)(lz >> 2)];
+}
+
+// Base cell (floor(x/dx - 0.5), kernels.rs:46-49) and fx = x/dx - base in
+// [0.5, 1.5) of a particle.
 template <bool CELL>
-__device__ __forceinline__ void grid_position(const ParticleArrays &a, uint32_t p, const float4 &pos, float dx,
-                                              int base[3], float fx[3]) {
+__device__ __forceinline__ void grid_position(const float4 &pos, const int4 &cell, float dx, int base[3], float fx[3]) {
     if (!CELL) {
         float q[3] = {pos.x / dx, pos.y / dx, pos.z / dx};
 #pragma unroll
@@ -97,9 +120,8 @@ __device__ __forceinline__ void grid_position(const ParticleArrays &a, uint32_t 
             fx[k] = q[k] - b;
         }
     } else {
-        int4 c = a.cell[p];
         float o[3] = {pos.x, pos.y, pos.z};
-        int ci[3] = {c.x, c.y, c.z};
+        int ci[3] = {cell.x, cell.y, cell.z};
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             bool hi = o[k] >= 0.5f;
@@ -109,8 +131,6 @@ __device__ __forceinline__ void grid_position(const ParticleArrays &a, uint32_t 
     }
 }
 
-__device__ __forceinline__ float sel3(const float v[3], int i) { return i == 0 ? v[0] : (i == 1 ? v[1] : v[2]); }
-
 __device__ __forceinline__ void load_mat9(const float *planes, uint64_t n, uint32_t p, m3f &m) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) m.a[k] = planes[(uint64_t)k * n + p];
@@ -118,6 +138,113 @@ __device__ __forceinline__ void load_mat9(const float *planes, uint64_t n, uint3
 __device__ __forceinline__ void store_mat9(float *planes, uint64_t n, uint64_t i, const m3f &m) {
 #pragma unroll
     for (int k = 0; k < 9; ++k) planes[(uint64_t)k * n + i] = m.a[k];
+}
+
+__device__ __forceinline__ void copy_particle(const ParticleArrays &in, const ParticleArrays &out, uint64_t n,
+                                              uint64_t src, uint64_t dst, bool cell) {
+    out.pos[dst] = in.pos[src];
+    if (cell) out.cell[dst] = in.cell[src];
+    out.vel[dst] = in.vel[src];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        out.C[(uint64_t)k * n + dst] = in.C[(uint64_t)k * n + src];
+        out.F[(uint64_t)k * n + dst] = in.F[(uint64_t)k * n + src];
+    }
+    out.energy[dst] = in.energy[src];
+    out.orig[dst] = in.orig[src];
+}
+
+// fp32 SVD with the fp64 redo for flagged particles.
+__device__ __forceinline__ void particle_svd(const m3f &F, m3f &U, float S[3], m3f &V, uint32_t policy,
+                                             uint32_t &fp64_count) {
+    svd3_fast(F, U, S, V);
+    bool redo = false;
+    if (policy >= 1 && det3(F) < 0.05f) redo = true;
+    if (policy >= 2) {
+        float g = fminf(fabsf(S[0] - S[1]), fminf(fabsf(S[1] - S[2]), fabsf(S[0] - S[2])));
+        if (g < 1e-4f) redo = true;
+    }
+    if (redo) {
+        m3d Fd, Ud, Vd;
+        double Sd[3];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Fd.a[k] = (double)F.a[k];
+        svd3<double>(Fd, Ud, Sd, Vd, 12);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) U.a[k] = (float)Ud.a[k], V.a[k] = (float)Vd.a[k];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) S[k] = (float)Sd[k];
+        ++fp64_count;
+    }
+}
+
+// P F^T of the particle's model (the part of scatter_momentum.rs:46-90 that
+// multiplies F^T (x_i - x_p)):
+//   Neo-Hookean (util/src/elastic.rs:299-311): mu F F^T + (lambda ln J - mu) I
+//   inviscid (elastic.rs:582-592):             K (1 - J^-gamma) J I
+//   fixed-corotated / snow (additions):        2 mu U (S^2 - S) U^T + lambda (J-1) J I
+// U and S are only read by the corotated kinds.
+__device__ __forceinline__ m3f stress_times_ft(const Material &m, const m3f &F, float J, const m3f &U,
+                                               const float S[3], float hard) {
+    m3f r;
+    float iso;
+    if (m.kind == KIND_FLUID) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) r.a[k] = 0.f;
+        iso = m.bulk_modulus * (1.f - 1.f / powi_f(J, m.exponent)) * J;
+    } else if (m.kind == KIND_FIXED_COROTATED || m.kind == KIND_SNOW) {
+        const float mu = m.mu * hard, la = m.lambda * hard;
+        float d[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) d[k] = 2.f * mu * (S[k] * S[k] - S[k]);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                r.a[j * 3 + i] = U.a[i] * d[0] * U.a[j] + U.a[3 + i] * d[1] * U.a[3 + j] + U.a[6 + i] * d[2] * U.a[6 + j];
+        iso = la * (J - 1.f) * J;
+    } else {
+        const m3f FFt = mat_mul_bt(F, F);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) r.a[k] = m.mu / 2.f * 2.f * FFt.a[k];
+        iso = m.lambda * logf(J) - m.mu;
+    }
+    r.a[0] += iso, r.a[4] += iso, r.a[8] += iso;
+    return r;
+}
+
+// Builds the scatter record of a particle at base cell/fx with velocity v
+// (external force already applied), velocity gradient C and stress P F^T.
+__device__ __forceinline__ void make_record(const Material &m, const m3f &C, const m3f &PFt, float J, const float v[3],
+                                            const float fx[3], float dx, float dt, Rec &rec) {
+    const float scaling = dt * 4.f / (dx * dx);  // scatter_momentum.rs:24-25
+    const float sv0 = scaling * m.initial_volume;
+    m3f A;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) A.a[k] = m.mass * C.a[k] - sv0 * PFt.a[k];
+    if (m.use_viscosity) {
+        // util/src/elastic.rs:659-677: 2 mu_d sym(C) + mu_b tr(C) I, times s J V0
+        const float sj = sv0 * J;
+        const float tr = C.a[0] + C.a[4] + C.a[8];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float s = m.visc_dynamic * (C.a[c * 3 + r] + C.a[r * 3 + c]) + (r == c ? m.visc_bulk * tr : 0.f);
+                A.a[c * 3 + r] -= sj * s;
+            }
+    }
+    float w[3][3];
+    bspline_weights(fx[0], w[0]);
+    bspline_weights(fx[1], w[1]);
+    bspline_weights(fx[2], w[2]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float dX = ((float)k - fx[0]) * dx, dY = ((float)k - fx[1]) * dx, dZ = ((float)k - fx[2]) * dx;
+        rec.p[k] = make_float4(m.mass * v[0] + A.a[0] * dX, m.mass * v[1] + A.a[1] * dX, m.mass * v[2] + A.a[2] * dX, w[0][k]);
+        rec.p[3 + k] = make_float4(A.a[3] * dY, A.a[4] * dY, A.a[5] * dY, w[1][k]);
+        rec.p[6 + k] = make_float4(A.a[6] * dZ, A.a[7] * dZ, A.a[8] * dZ, w[2][k]);
+    }
 }
 
 // ------------------------------------------------------------------ keys
@@ -129,7 +256,7 @@ template <bool CELL> __global__ void __launch_bounds__(ELEM_THREADS) k_keys(Step
         if (!(packed & SV_TOMBSTONED)) {
             int base[3];
             float fx[3];
-            grid_position<CELL>(A.in, (uint32_t)i, pos, A.L.dx, base, fx);
+            grid_position<CELL>(pos, CELL ? A.in.cell[i] : make_int4(0, 0, 0, 0), A.L.dx, base, fx);
             bool ok;
             key = cell_key(base[0], base[1], base[2], A.L, ok);
             if (!ok) atomicOr(&A.counters[C_STATUS], ST_OUT_OF_GRID);
@@ -171,8 +298,6 @@ __global__ void __launch_bounds__(ELEM_THREADS)
     }
 }
 
-// Writes segment starts in key order: thread t of the tile owns the
-// SEG_ITEMS consecutive elements [base + t*SEG_ITEMS, ...).
 __global__ void __launch_bounds__(ELEM_THREADS)
     k_seg_write(const uint32_t *sk, uint64_t n, const uint32_t *tile_offsets, uint32_t tiles, uint32_t *seg_start,
                 uint32_t *seg_block, uint32_t *counters) {
@@ -221,460 +346,459 @@ __global__ void __launch_bounds__(ELEM_THREADS)
     }
 }
 
-// ------------------------------------------------------------------ grid blocks
+// ------------------------------------------------------------------ block maps
 __global__ void __launch_bounds__(ELEM_THREADS)
-    k_reset_blockmap(int32_t *blockmap, const uint32_t *active, uint32_t *counters) {
-    uint32_t prev = counters[C_NSLOT_PREV];
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < prev; s += gridDim.x * blockDim.x)
-        blockmap[active[s]] = -1;
+    k_map_reset(int32_t *map, const uint32_t *active, uint32_t *counters, int which, uint64_t capacity) {
+    uint64_t cnt = counters[C_NSLOT0 + which];
+    if (cnt > capacity) cnt = capacity;
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < cnt; s += (uint64_t)gridDim.x * blockDim.x)
+        map[active[s]] = -1;
 }
 
-__global__ void k_latch(uint32_t *counters, int reset_slots) {
-    if (reset_slots) counters[C_NSLOT] = 0;
+// Latches the stop bits; optionally zeroes (reset_which) or clamps to the
+// capacity (clamp_which) a slot counter.
+__global__ void k_latch(uint32_t *counters, int reset_which, int clamp_which, uint64_t capacity) {
+    if (reset_which >= 0) counters[C_NSLOT0 + reset_which] = 0;
+    if (clamp_which >= 0 && counters[C_NSLOT0 + clamp_which] > capacity) counters[C_NSLOT0 + clamp_which] = (uint32_t)capacity;
     counters[C_STOP] = counters[C_STATUS] & STOP_MASK;
 }
 
+// Claims a slot for each block in the 27-neighbourhood of every segment.
 __global__ void __launch_bounds__(ELEM_THREADS)
-    k_activate(const uint32_t *seg_block, int32_t *blockmap, uint32_t *active, uint64_t capacity, GridLayout L,
-               uint32_t *counters) {
+    k_activate(const uint32_t *seg_block, int32_t *map, uint32_t *active, uint64_t capacity, GridLayout L,
+               uint32_t *counters, int which) {
     if (stopped(counters)) return;
     uint32_t nseg = counters[C_NSEG];
-    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (uint64_t)nseg * 8;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (uint64_t)nseg * 27;
          t += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t b = neighbour_block(seg_block[t >> 3], (int)(t & 7), L);
-        if (atomicCAS(&blockmap[b], -1, -2) == -1) {
-            uint32_t slot = atomicAdd(&counters[C_NSLOT], 1u);
+        uint32_t b = neighbour27(seg_block[t / 27], (int)(t % 27), L);
+        if (atomicCAS(&map[b], -1, -2) == -1) {
+            uint32_t slot = atomicAdd(&counters[C_NSLOT0 + which], 1u);
             if (slot < capacity) {
                 active[slot] = b;
-                blockmap[b] = (int32_t)slot;
+                map[b] = (int32_t)slot;
             } else {
-                blockmap[b] = -1;
+                map[b] = -1;
                 atomicOr(&counters[C_STATUS], ST_CAPACITY);
             }
         }
     }
 }
 
-__global__ void __launch_bounds__(ELEM_THREADS) k_clear_grid(float4 *grid, uint64_t capacity, uint32_t *counters) {
-    uint64_t slots = counters[C_NSLOT];
+__global__ void __launch_bounds__(ELEM_THREADS) k_clear_grid(float4 *grid, uint64_t capacity, uint32_t *counters, int which) {
+    uint64_t slots = counters[C_NSLOT0 + which];
     if (slots > capacity) slots = capacity;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < slots * 64; i += (uint64_t)gridDim.x * blockDim.x)
         grid[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-// ------------------------------------------------------------------ P2G
-template <bool CELL> __global__ void __launch_bounds__(P2G_THREADS) k_p2g(StepArgs A) {
-    __shared__ float tile[4][TILE_PLANE];
-    __shared__ int32_t nslot[8];
-    if (stopped(A.counters)) return;
-    const uint32_t nseg = A.counters[C_NSEG];
-    const float dx = A.L.dx;
-    const float scaling = A.dt * 4.f / (dx * dx);  // scatter_momentum.rs:24-25
-    const int lane = threadIdx.x & 31;
-    for (uint32_t seg = blockIdx.x; seg < nseg; seg += gridDim.x) {
-        const uint32_t b = A.seg_block[seg];
-        const uint32_t start = A.seg_start[seg], end = A.seg_start[seg + 1];
-        int bx, by, bz;
-        block_coords(b, A.L, bx, by, bz);
-        const int ox = A.L.origin[0] + 4 * bx, oy = A.L.origin[1] + 4 * by, oz = A.L.origin[2] + 4 * bz;
-        for (int i = threadIdx.x; i < 4 * TILE_PLANE; i += P2G_THREADS) (&tile[0][0])[i] = 0.f;
-        if (threadIdx.x < 8) nslot[threadIdx.x] = A.blockmap[neighbour_block(b, threadIdx.x, A.L)];
-        __syncthreads();
-        for (uint32_t i = start + threadIdx.x; i < end; i += P2G_THREADS) {
-            const uint32_t p = A.perm[i];
-            const float4 pos = A.in.pos[p];
-            float4 vel = A.in.vel[p];
-            const uint32_t packed = __float_as_uint(pos.w);
-            const Material mat = A.mats[packed >> MATERIAL_SHIFT];
-            int base[3];
-            float fx[3];
-            grid_position<CELL>(A.in, p, pos, dx, base, fx);
-            m3f F, C;
-            load_mat9(A.in.F, A.n, p, F);
-            load_mat9(A.in.C, A.n, p, C);
-            // external_force.rs:17-50: v += dt g (before P2G)
-            vel.x += A.dt * A.gravity.x, vel.y += A.dt * A.gravity.y, vel.z += A.dt * A.gravity.z;
-            const float J = det3(F);
-            m3f R;
-            float hard = 1.f;
-            if (mat.kind == KIND_FIXED_COROTATED || mat.kind == KIND_SNOW) {
-                m3f U, V;
-                float S[3];
-                svd3<float>(F, U, S, V, 6);
-                R = mat_mul_bt(U, V);
-                if (mat.kind == KIND_SNOW) hard = expf(mat.xi * (1.f - vel.w));
-            }
-            const m3f P = piola(mat, F, R, J, hard);
-            // A = m C - s V0 P F^T [- s J V0 sigma_visc]
-            const m3f PFt = mat_mul_bt(P, F);
-            const float sv0 = scaling * mat.initial_volume;
-            m3f Aff;
-#pragma unroll
-            for (int k = 0; k < 9; ++k) Aff.a[k] = mat.mass * C.a[k] - sv0 * PFt.a[k];
-            if (mat.use_viscosity) {
-                // util/src/elastic.rs:659-677: 2 mu_d sym(C) + mu_b tr(C) I
-                const float sj = sv0 * J;
-                const float tr = C.a[0] + C.a[4] + C.a[8];
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        float s = mat.visc_dynamic * (C.a[c * 3 + r] + C.a[r * 3 + c]) + (r == c ? mat.visc_bulk * tr : 0.f);
-                        Aff.a[c * 3 + r] -= sj * s;
-                    }
-            }
-            const float mvx = mat.mass * vel.x, mvy = mat.mass * vel.y, mvz = mat.mass * vel.z;
-            float wx[3], wy[3], wz[3], dX[3], dY[3], dZ[3];
-            bspline_weights(fx[0], wx);
-            bspline_weights(fx[1], wy);
-            bspline_weights(fx[2], wz);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                dX[k] = ((float)k - fx[0]) * dx;
-                dY[k] = ((float)k - fx[1]) * dx;
-                dZ[k] = ((float)k - fx[2]) * dx;
-            }
-            const int tb = (base[0] - ox) * TS_X + (base[1] - oy) * TS_Y + (base[2] - oz) * TS_Z;
-            // Lane-rotated stencil order: lanes of one cell hit 27 different nodes.
-            int o = lane % 27;
-#pragma unroll 3
-            for (int q = 0; q < 27; ++q) {
-                const int ii = o / 9, jj = (o / 3) % 3, kk = o % 3;
-                const float w = sel3(wx, ii) * sel3(wy, jj) * sel3(wz, kk);
-                const float ddx = sel3(dX, ii), ddy = sel3(dY, jj), ddz = sel3(dZ, kk);
-                const float px = w * (mvx + Aff.a[0] * ddx + Aff.a[3] * ddy + Aff.a[6] * ddz);
-                const float py = w * (mvy + Aff.a[1] * ddx + Aff.a[4] * ddy + Aff.a[7] * ddz);
-                const float pz = w * (mvz + Aff.a[2] * ddx + Aff.a[5] * ddy + Aff.a[8] * ddz);
-                const int t = tb + ii * TS_X + jj * TS_Y + kk * TS_Z;
-                atomicAdd(&tile[0][t], w * mat.mass);
-                atomicAdd(&tile[1][t], px);
-                atomicAdd(&tile[2][t], py);
-                atomicAdd(&tile[3][t], pz);
-                o = o == 26 ? 0 : o + 1;
-            }
-        }
-        __syncthreads();
-        for (int t = threadIdx.x; t < 216; t += P2G_THREADS) {
-            const int tx = t / 36, ty = (t / 6) % 6, tz = t % 6;
-            const int s = tx * TS_X + ty * TS_Y + tz * TS_Z;
-            const float m = tile[0][s];
-            if (m != 0.f || tile[1][s] != 0.f || tile[2][s] != 0.f || tile[3][s] != 0.f) {
-                const int nb = (tx >> 2) * 4 + (ty >> 2) * 2 + (tz >> 2);
-                const int32_t slot = nslot[nb];
-                if (slot >= 0) {
-                    float4 *g = &A.grid[(uint64_t)slot * 64 + ((tx & 3) * 16 + (ty & 3) * 4 + (tz & 3))];
-                    atomicAdd(g, make_float4(tile[1][s], tile[2][s], tile[3][s], m));
-                } else {
-                    atomicOr(&A.counters[C_STATUS], ST_CAPACITY);
+// ------------------------------------------------------------------ grid update
+// Momentum -> velocity on grid_cur (slots of map `wc`), and zeroes grid_next
+// (slots of map `wn`) for the scatter that follows.
+__global__ void __launch_bounds__(ELEM_THREADS)
+    k_grid_update(float4 *grid_cur, const uint32_t *active_cur, float4 *grid_next, uint64_t capacity, GridLayout L,
+                  uint32_t *counters, int wc, int wn) {
+    if (stopped(counters)) return;
+    uint64_t sc = counters[C_NSLOT0 + wc], sn = grid_next ? counters[C_NSLOT0 + wn] : 0;
+    if (sc > capacity) sc = capacity;
+    if (sn > capacity) sn = capacity;
+    const uint64_t total = (sc > sn ? sc : sn) * 64;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i < sc * 64) {
+            float4 g = grid_cur[i];
+            // meld_grid.rs:61-66: v = p / m, or 0 when m <= 0
+            float m = g.w;
+            float vx = 0.f, vy = 0.f, vz = 0.f;
+            if (m > 0.f) vx = g.x / m, vy = g.y / m, vz = g.z / m;
+            if (L.ground_mode != 0) {
+                // Addition (not in the reference): boundary plane at node height.
+                int bx, by, bz;
+                block_coords(active_cur[i >> 6], L, bx, by, bz);
+                int l = (int)(i & 63);
+                int node[3] = {L.origin[0] + 4 * bx + (l >> 4), L.origin[1] + 4 * by + ((l >> 2) & 3),
+                               L.origin[2] + 4 * bz + (l & 3)};
+                if ((float)node[L.ground_axis] * L.dx <= L.ground_height) {
+                    if (L.ground_mode == 1) vx = vy = vz = 0.f;
+                    else if (L.ground_axis == 0) vx = fmaxf(vx, 0.f);
+                    else if (L.ground_axis == 1) vy = fmaxf(vy, 0.f);
+                    else vz = fmaxf(vz, 0.f);
                 }
             }
+            grid_cur[i] = make_float4(vx, vy, vz, m);
         }
-        __syncthreads();
+        if (i < sn * 64) grid_next[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
 }
 
-// ------------------------------------------------------------------ grid update
-__global__ void __launch_bounds__(ELEM_THREADS)
-    k_grid_update(float4 *grid, const uint32_t *active, uint64_t capacity, GridLayout L, uint32_t *counters) {
-    if (stopped(counters)) return;
-    uint64_t slots = counters[C_NSLOT];
-    if (slots > capacity) slots = capacity;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < slots * 64; i += (uint64_t)gridDim.x * blockDim.x) {
-        float4 g = grid[i];
-        // meld_grid.rs:61-66: v = p / m, or 0 when m <= 0
-        float m = g.w;
-        float vx = 0.f, vy = 0.f, vz = 0.f;
-        if (m > 0.f) vx = g.x / m, vy = g.y / m, vz = g.z / m;
-        if (L.ground_mode != 0) {
-            // Addition (not in the reference): boundary plane at node height.
-            int bx, by, bz;
-            block_coords(active[i >> 6], L, bx, by, bz);
-            int l = (int)(i & 63);
-            int node[3] = {L.origin[0] + 4 * bx + (l >> 4), L.origin[1] + 4 * by + ((l >> 2) & 3), L.origin[2] + 4 * bz + (l & 3)};
-            if ((float)node[L.ground_axis] * L.dx <= L.ground_height) {
-                float *vc[3] = {&vx, &vy, &vz};
-                if (L.ground_mode == 1) vx = vy = vz = 0.f;
-                else if (*vc[L.ground_axis] < 0.f) *vc[L.ground_axis] = 0.f;
+// ------------------------------------------------------------------ particle kernel
+struct Shared {
+    float4 gv[TILE_NODES];      // velocity tile of grid_cur (G2P2G)
+    float pt[4][TILE_NODES];    // mass, px, py, pz tile of grid_next
+    Rec rec[PT];
+    uint32_t cell[PT];          // REC_NONE, tile cell index, or REC_GLOBAL
+    float mass[PT];
+    int4 gbase[PT];             // global base cell of REC_GLOBAL records
+    int32_t slot_cur[27];
+    int32_t slot_next[27];
+};
+
+// Tile node (tx, ty, tz) in [0, 8)^3 of block (bx, by, bz): global node
+// 4b - 1 + t, in neighbour block (t + 3) / 4 - 1 along each axis.
+__device__ __forceinline__ int tile_neighbour(int tx, int ty, int tz) {
+    return ((tx + 3) / 4) * 9 + ((ty + 3) / 4) * 3 + (tz + 3) / 4;
+}
+__device__ __forceinline__ int tile_local(int tx, int ty, int tz) {
+    return ((tx + 3) & 3) * 16 + ((ty + 3) & 3) * 4 + ((tz + 3) & 3);
+}
+
+// Replays the chunk's scatter records: warp w owns records [32w, 32w + 32);
+// lane l < 27 is stencil offset (l/9, (l/3)%3, l%3).  Consecutive records
+// with the same base cell accumulate in registers before one shared atomic
+// per lane and component.
+__device__ __forceinline__ void scatter_records(Shared &sh, int count, const StepArgs &A) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int li = lane / 9, lj = (lane / 3) % 3, lk = lane % 3;
+    const bool active = lane < 27;
+    float am = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
+    uint32_t cur = REC_NONE;
+    const int r0 = warp * 32, r1 = min(r0 + 32, count);
+    for (int r = r0; r < r1; ++r) {
+        const uint32_t c = sh.cell[r];
+        if (c == REC_NONE) continue;
+        if (c != cur) {
+            if (cur != REC_NONE && active) {
+                const int t = (int)cur + li * 64 + lj * 8 + lk;
+                atomicAdd(&sh.pt[0][t], am);
+                atomicAdd(&sh.pt[1][t], ax);
+                atomicAdd(&sh.pt[2][t], ay);
+                atomicAdd(&sh.pt[3][t], az);
+            }
+            am = ax = ay = az = 0.f;
+            cur = c;
+        }
+        if (active) {
+            const float4 p0 = sh.rec[r].p[li], p1 = sh.rec[r].p[3 + lj], p2 = sh.rec[r].p[6 + lk];
+            const float w = p0.w * p1.w * p2.w;
+            const float m = sh.mass[r];
+            if (c == REC_GLOBAL) {
+                // outside the tile: straight to global memory
+                const int4 gb = sh.gbase[r];
+                int local;
+                const int32_t slot = node_slot(A.map_next, gb.x + li, gb.y + lj, gb.z + lk, A.L, local);
+                if (slot >= 0)
+                    atomicAdd(&A.grid_next[(uint64_t)slot * 64 + local],
+                              make_float4(w * (p0.x + p1.x + p2.x), w * (p0.y + p1.y + p2.y), w * (p0.z + p1.z + p2.z), w * m));
+                else
+                    atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR);
+            } else {
+                am += w * m;
+                ax += w * (p0.x + p1.x + p2.x);
+                ay += w * (p0.y + p1.y + p2.y);
+                az += w * (p0.z + p1.z + p2.z);
             }
         }
-        grid[i] = make_float4(vx, vy, vz, m);
+        if (c == REC_GLOBAL) cur = REC_NONE;
+    }
+    if (cur != REC_NONE && cur != REC_GLOBAL && active) {
+        const int t = (int)cur + li * 64 + lj * 8 + lk;
+        atomicAdd(&sh.pt[0][t], am);
+        atomicAdd(&sh.pt[1][t], ax);
+        atomicAdd(&sh.pt[2][t], ay);
+        atomicAdd(&sh.pt[3][t], az);
     }
 }
 
-// ------------------------------------------------------------------ G2P
-__device__ __forceinline__ void copy_particle(const ParticleArrays &in, const ParticleArrays &out, uint64_t n,
-                                              uint64_t src, uint64_t dst, bool cell) {
-    out.pos[dst] = in.pos[src];
-    if (cell) out.cell[dst] = in.cell[src];
-    out.vel[dst] = in.vel[src];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        out.C[(uint64_t)k * n + dst] = in.C[(uint64_t)k * n + src];
-        out.F[(uint64_t)k * n + dst] = in.F[(uint64_t)k * n + src];
-    }
-    out.energy[dst] = in.energy[src];
-    out.orig[dst] = in.orig[src];
+// Record slot for a particle scattering from base cell `base` into the tile
+// whose node 0 is global node `org`.
+__device__ __forceinline__ uint32_t tile_cell(const int base[3], const int org[3], int4 &gb) {
+    const int tx = base[0] - org[0], ty = base[1] - org[1], tz = base[2] - org[2];
+    if (tx >= 0 && ty >= 0 && tz >= 0 && tx <= TN - 3 && ty <= TN - 3 && tz <= TN - 3) return (uint32_t)(tx * 64 + ty * 8 + tz);
+    gb = make_int4(base[0], base[1], base[2], 0);
+    return REC_GLOBAL;
 }
 
-template <bool CELL> __global__ void __launch_bounds__(G2P_THREADS) k_g2p(StepArgs A) {
-    __shared__ float4 gv[216];
-    __shared__ int32_t nslot[8];
+template <bool CELL, int MODE> __global__ void __launch_bounds__(PT) k_particles(StepArgs A) {
+    __shared__ Shared sh;
     if (stopped(A.counters)) {
-        // Keep the state as it is (identity copy) so the buffer swap is a no-op.
-        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x)
-            copy_particle(A.in, A.out, A.n, i, i, CELL);
+        if (MODE == MODE_G2P2G) {
+            // Keep the state as it is (identity copy) so the buffer swap is a no-op.
+            for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x)
+                copy_particle(A.in, A.out, A.n, i, i, CELL);
+        }
         return;
     }
     const uint32_t nseg = A.counters[C_NSEG];
     const uint32_t nlive = A.counters[C_NLIVE];
-    // Tombstoned particles (sorted last) are carried over unchanged.
-    for (uint64_t i = nlive + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x) {
-        copy_particle(A.in, A.out, A.n, A.perm[i], i, CELL);
-        A.keys_out[i] = SENTINEL_KEY;
-    }
     const float dx = A.L.dx;
-    uint32_t fp64_count = 0;
+    if (MODE == MODE_G2P2G) {
+        // particles that were tombstoned at binning time are carried over
+        for (uint64_t i = nlive + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x) {
+            copy_particle(A.in, A.out, A.n, A.perm ? A.perm[i] : i, i, CELL);
+            if (A.keys_out) A.keys_out[i] = SENTINEL_KEY;
+        }
+    }
+    uint32_t fp64_count = 0, fallback = 0;
     for (uint32_t seg = blockIdx.x; seg < nseg; seg += gridDim.x) {
         const uint32_t b = A.seg_block[seg];
         const uint32_t start = A.seg_start[seg], end = A.seg_start[seg + 1];
         int bx, by, bz;
         block_coords(b, A.L, bx, by, bz);
-        const int ox = A.L.origin[0] + 4 * bx, oy = A.L.origin[1] + 4 * by, oz = A.L.origin[2] + 4 * bz;
-        if (threadIdx.x < 8) nslot[threadIdx.x] = A.blockmap[neighbour_block(b, threadIdx.x, A.L)];
-        __syncthreads();
-        for (int t = threadIdx.x; t < 216; t += G2P_THREADS) {
-            const int tx = t / 36, ty = (t / 6) % 6, tz = t % 6;
-            const int32_t slot = nslot[(tx >> 2) * 4 + (ty >> 2) * 2 + (tz >> 2)];
-            gv[t] = slot >= 0 ? A.grid[(uint64_t)slot * 64 + ((tx & 3) * 16 + (ty & 3) * 4 + (tz & 3))]
-                              : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int org[3] = {A.L.origin[0] + 4 * bx - 1, A.L.origin[1] + 4 * by - 1, A.L.origin[2] + 4 * bz - 1};
+        if (threadIdx.x < 27) {
+            const uint32_t nbk = neighbour27(b, threadIdx.x, A.L);
+            sh.slot_next[threadIdx.x] = A.map_next[nbk];
+            if (MODE == MODE_G2P2G) sh.slot_cur[threadIdx.x] = A.map_cur[nbk];
         }
+        for (int t = threadIdx.x; t < 4 * TILE_NODES; t += PT) (&sh.pt[0][0])[t] = 0.f;
         __syncthreads();
-        for (uint32_t i = start + threadIdx.x; i < end; i += G2P_THREADS) {
-            const uint32_t p = A.perm[i];
-            float4 pos = A.in.pos[p];
-            uint32_t packed = __float_as_uint(pos.w);
-            const Material mat = A.mats[packed >> MATERIAL_SHIFT];
-            int base[3];
-            float fx[3];
-            grid_position<CELL>(A.in, p, pos, dx, base, fx);
-            float wx[3], wy[3], wz[3];
-            bspline_weights(fx[0], wx);
-            bspline_weights(fx[1], wy);
-            bspline_weights(fx[2], wz);
-            const int t0 = (base[0] - ox) * 36 + (base[1] - oy) * 6 + (base[2] - oz);
-            // collect_velocity.rs:50-72
-            float v[3] = {0.f, 0.f, 0.f};
-            m3f C;
-#pragma unroll
-            for (int k = 0; k < 9; ++k) C.a[k] = 0.f;
-#pragma unroll
-            for (int ii = 0; ii < 3; ++ii) {
-                const float ddx = ((float)ii - fx[0]) * dx;
-#pragma unroll
-                for (int jj = 0; jj < 3; ++jj) {
-                    const float ddy = ((float)jj - fx[1]) * dx;
-                    const float wxy = wx[ii] * wy[jj];
-#pragma unroll
-                    for (int kk = 0; kk < 3; ++kk) {
-                        const float ddz = ((float)kk - fx[2]) * dx;
-                        const float w = wxy * wz[kk];
-                        const float4 g = gv[t0 + ii * 36 + jj * 6 + kk];
-                        const float gx = g.x * w, gy = g.y * w, gz = g.z * w;
-                        v[0] += gx, v[1] += gy, v[2] += gz;
-                        C.a[0] += gx * ddx, C.a[1] += gy * ddx, C.a[2] += gz * ddx;
-                        C.a[3] += gx * ddy, C.a[4] += gy * ddy, C.a[5] += gz * ddy;
-                        C.a[6] += gx * ddz, C.a[7] += gy * ddz, C.a[8] += gz * ddz;
+        if (MODE == MODE_G2P2G) {
+            for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
+                const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
+                const int32_t slot = sh.slot_cur[tile_neighbour(tx, ty, tz)];
+                sh.gv[t] = slot >= 0 ? A.grid_cur[(uint64_t)slot * 64 + tile_local(tx, ty, tz)] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            __syncthreads();
+        }
+        for (uint32_t c0 = start; c0 < end; c0 += PT) {
+            const uint32_t i = c0 + threadIdx.x;
+            const int count = (int)min((uint32_t)PT, end - c0);
+            uint32_t rcell = REC_NONE;
+            if (i < end) {
+                const uint32_t p = A.perm ? A.perm[i] : i;
+                float4 pos = A.in.pos[p];
+                uint32_t packed = __float_as_uint(pos.w);
+                int4 cell = CELL ? A.in.cell[p] : make_int4(0, 0, 0, 0);
+                if (packed & SV_TOMBSTONED) {
+                    if (MODE == MODE_G2P2G) {
+                        copy_particle(A.in, A.out, A.n, p, i, CELL);
+                        if (A.keys_out) A.keys_out[i] = SENTINEL_KEY;
                     }
-                }
-            }
-            const float cscale = 4.f / dx / dx;
+                } else {
+                    const Material mat = A.mats[packed >> MATERIAL_SHIFT];
+                    const uint32_t kind = mat.kind;
+                    m3f F, C;
+                    float v[3];
+                    float plastic_j;
+                    load_mat9(A.in.F, A.n, p, F);
+                    if (MODE == MODE_P2G) {
+                        load_mat9(A.in.C, A.n, p, C);
+                        const float4 vel = A.in.vel[p];
+                        v[0] = vel.x, v[1] = vel.y, v[2] = vel.z;
+                        plastic_j = vel.w;
+                    } else {
+                        plastic_j = kind == KIND_SNOW ? A.in.vel[p].w : 1.f;
+                        // ---- G2P (collect_velocity.rs:40-72)
+                        int base[3];
+                        float fx[3];
+                        grid_position<CELL>(pos, cell, dx, base, fx);
+                        float w[3][3];
+                        bspline_weights(fx[0], w[0]);
+                        bspline_weights(fx[1], w[1]);
+                        bspline_weights(fx[2], w[2]);
+                        const int tx = base[0] - org[0], ty = base[1] - org[1], tz = base[2] - org[2];
+                        const bool in_tile = tx >= 0 && ty >= 0 && tz >= 0 && tx <= TN - 3 && ty <= TN - 3 && tz <= TN - 3;
+                        v[0] = v[1] = v[2] = 0.f;
 #pragma unroll
-            for (int k = 0; k < 9; ++k) C.a[k] *= cscale;
-            // advance_particles.rs:39-41: x += v dt, F += C F dt
-            m3f F;
-            load_mat9(A.in.F, A.n, p, F);
-            {
-                m3f CF = mat_mul(C, F);
+                        for (int k = 0; k < 9; ++k) C.a[k] = 0.f;
+                        if (!in_tile) ++fallback;
 #pragma unroll
-                for (int k = 0; k < 9; ++k) F.a[k] += CF.a[k] * A.dt;
-            }
-            int4 cell = make_int4(0, 0, 0, 0);
-            if (!CELL) {
-                pos.x += v[0] * A.dt, pos.y += v[1] * A.dt, pos.z += v[2] * A.dt;
-            } else {
-                cell = A.in.cell[p];
-                float o[3] = {pos.x + v[0] * A.dt / dx, pos.y + v[1] * A.dt / dx, pos.z + v[2] * A.dt / dx};
-                int ci[3] = {cell.x, cell.y, cell.z};
+                        for (int ii = 0; ii < 3; ++ii) {
+                            const float ddx = ((float)ii - fx[0]) * dx;
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    float fl = floorf(o[k]);
-                    ci[k] += (int)fl;
-                    o[k] -= fl;
-                    if (o[k] >= 1.f) o[k] = 0.f, ci[k] += 1;  // rounding guard
-                }
-                pos.x = o[0], pos.y = o[1], pos.z = o[2];
-                cell = make_int4(ci[0], ci[1], ci[2], 0);
-            }
-            // plasticity (advance_particles.rs:42-86) and energy
-            float plastic_j = 1.f;
-            if (mat.kind == KIND_SNOW) plastic_j = A.in.vel[p].w;
-            float energy = 0.f;
-            const uint32_t kind = mat.kind;
-            if (kind != KIND_NEO_HOOKEAN) {
-                m3f U, V;
-                float S[3];
-                svd3<float>(F, U, S, V, 6);
-                float det = det3(F);
-                bool redo = false;
-                if (A.L.svd_policy >= 1 && det < 0.05f) redo = true;
-                if (A.L.svd_policy >= 2) {
-                    float g = fminf(fabsf(S[0] - S[1]), fminf(fabsf(S[1] - S[2]), fabsf(S[0] - S[2])));
-                    if (g < 1e-4f) redo = true;
-                }
-                if (redo) {
-                    m3d Fd, Ud, Vd;
-                    double Sd[3];
+                            for (int jj = 0; jj < 3; ++jj) {
+                                const float ddy = ((float)jj - fx[1]) * dx;
+                                const float wxy = w[0][ii] * w[1][jj];
 #pragma unroll
-                    for (int k = 0; k < 9; ++k) Fd.a[k] = (double)F.a[k];
-                    svd3<double>(Fd, Ud, Sd, Vd, 12);
-#pragma unroll
-                    for (int k = 0; k < 9; ++k) U.a[k] = (float)Ud.a[k], V.a[k] = (float)Vd.a[k];
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) S[k] = (float)Sd[k];
-                    ++fp64_count;
-                }
-                if (kind == KIND_SAND) {
-                    // advance_particles.rs:48-71 (Drucker-Prager in Hencky strain)
-                    if (mat.mu > 0.f) {
-                        float e[3] = {logf(S[0]), logf(S[1]), logf(S[2])};
-                        float e_tr = e[0] + e[1] + e[2];
-                        float eh[3] = {e[0] - e_tr / 3.f, e[1] - e_tr / 3.f, e[2] - e_tr / 3.f};
-                        float ehn = sqrtf(eh[0] * eh[0] + eh[1] * eh[1] + eh[2] * eh[2]);
-                        if (e_tr < 0.f && ehn > 0.f) {
-                            float dg = ehn + (3.f * mat.lambda + 2.f * mat.mu) / 2.f / mat.mu * e_tr * mat.alpha;
-                            if (dg > 0.f) {
-                                float s[3];
-#pragma unroll
-                                for (int k = 0; k < 3; ++k) s[k] = expf(e[k] - dg / ehn * eh[k]);
-                                F = recompose(U, s, V);
+                                for (int kk = 0; kk < 3; ++kk) {
+                                    const float ddz = ((float)kk - fx[2]) * dx;
+                                    const float wt = wxy * w[2][kk];
+                                    float4 g;
+                                    if (in_tile) {
+                                        g = sh.gv[(tx + ii) * 64 + (ty + jj) * 8 + (tz + kk)];
+                                    } else {
+                                        int local;
+                                        const int32_t slot = node_slot(A.map_cur, base[0] + ii, base[1] + jj, base[2] + kk, A.L, local);
+                                        g = slot >= 0 ? A.grid_cur[(uint64_t)slot * 64 + local] : make_float4(0.f, 0.f, 0.f, 0.f);
+                                    }
+                                    const float gx = g.x * wt, gy = g.y * wt, gz = g.z * wt;
+                                    v[0] += gx, v[1] += gy, v[2] += gz;
+                                    C.a[0] += gx * ddx, C.a[1] += gy * ddx, C.a[2] += gz * ddx;
+                                    C.a[3] += gx * ddy, C.a[4] += gy * ddy, C.a[5] += gz * ddy;
+                                    C.a[6] += gx * ddz, C.a[7] += gy * ddz, C.a[8] += gz * ddz;
+                                }
                             }
+                        }
+                        const float cscale = 4.f / dx / dx;
+#pragma unroll
+                        for (int k = 0; k < 9; ++k) C.a[k] *= cscale;
+                        // ---- advance (advance_particles.rs:39-41): x += v dt, F += C F dt
+                        {
+                            const m3f CF = mat_mul(C, F);
+#pragma unroll
+                            for (int k = 0; k < 9; ++k) F.a[k] += CF.a[k] * A.dt;
+                        }
+                        if (!CELL) {
+                            pos.x += v[0] * A.dt, pos.y += v[1] * A.dt, pos.z += v[2] * A.dt;
                         } else {
-                            F = mat_mul_bt(U, V);
+                            float o[3] = {pos.x + v[0] * A.dt / dx, pos.y + v[1] * A.dt / dx, pos.z + v[2] * A.dt / dx};
+                            int ci[3] = {cell.x, cell.y, cell.z};
+#pragma unroll
+                            for (int k = 0; k < 3; ++k) {
+                                const float fl = floorf(o[k]);
+                                ci[k] += (int)fl;
+                                o[k] -= fl;
+                                if (o[k] >= 1.f) o[k] = 0.f, ci[k] += 1;
+                            }
+                            pos.x = o[0], pos.y = o[1], pos.z = o[2];
+                            cell = make_int4(ci[0], ci[1], ci[2], 0);
                         }
                     }
-                } else if (kind == KIND_FLUID) {
-                    // advance_particles.rs:77-85
-                    float g = powf(S[0] * S[1] * S[2], 1.f / 3.f);
-                    float s[3] = {g, g, g};
-                    F = recompose(U, s, V);
-                } else if (kind == KIND_SNOW) {
-                    float s[3];
+                    // ---- SVD, plasticity (advance_particles.rs:42-86), energy
+                    m3f U, V;
+                    float S[3] = {1.f, 1.f, 1.f};
+                    const bool need_svd = MODE == MODE_G2P2G ? kind != KIND_NEO_HOOKEAN
+                                                              : (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW);
+                    if (need_svd) particle_svd(F, U, S, V, A.L.svd_policy, fp64_count);
+                    float energy = 0.f;
+                    if (MODE == MODE_G2P2G) {
+                        if (kind == KIND_SAND) {
+                            // Drucker-Prager return map in Hencky strain (advance_particles.rs:48-71)
+                            if (mat.mu > 0.f) {
+                                const float e[3] = {logf(S[0]), logf(S[1]), logf(S[2])};
+                                const float e_tr = e[0] + e[1] + e[2];
+                                const float eh[3] = {e[0] - e_tr / 3.f, e[1] - e_tr / 3.f, e[2] - e_tr / 3.f};
+                                const float ehn = sqrtf(eh[0] * eh[0] + eh[1] * eh[1] + eh[2] * eh[2]);
+                                if (e_tr < 0.f && ehn > 0.f) {
+                                    const float dg = ehn + (3.f * mat.lambda + 2.f * mat.mu) / 2.f / mat.mu * e_tr * mat.alpha;
+                                    if (dg > 0.f) {
 #pragma unroll
-                    for (int k = 0; k < 3; ++k) s[k] = fminf(fmaxf(S[k], 1.f - mat.theta_c), 1.f + mat.theta_s);
-                    plastic_j = plastic_j * (S[0] * S[1] * S[2]) / (s[0] * s[1] * s[2]);
-                    F = recompose(U, s, V);
-                }
-                if (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW) {
-                    // psi = mu |F - R|^2 + lambda/2 (J - 1)^2 with hardening for snow
-                    const float h = kind == KIND_SNOW ? expf(mat.xi * (1.f - plastic_j)) : 1.f;
-                    const m3f Rm = mat_mul_bt(U, V);
-                    float d2 = 0.f;
+                                        for (int k = 0; k < 3; ++k) S[k] = expf(e[k] - dg / ehn * eh[k]);
+                                        F = recompose(U, S, V);
+                                    }
+                                } else {
+                                    S[0] = S[1] = S[2] = 1.f;
+                                    F = mat_mul_bt(U, V);
+                                }
+                            }
+                        } else if (kind == KIND_FLUID) {
+                            // advance_particles.rs:77-85: singular values -> geometric mean
+                            const float g = powf(S[0] * S[1] * S[2], 1.f / 3.f);
+                            S[0] = S[1] = S[2] = g;
+                            F = recompose(U, S, V);
+                        } else if (kind == KIND_SNOW) {
+                            // addition: Stomakhin et al. 2013 clamp + hardening state
+                            float s[3];
 #pragma unroll
-                    for (int k = 0; k < 9; ++k) d2 += (F.a[k] - Rm.a[k]) * (F.a[k] - Rm.a[k]);
-                    const float Jn = det3(F);
-                    energy = mat.mu * h * d2 + mat.lambda * h / 2.f * (Jn - 1.f) * (Jn - 1.f);
+                            for (int k = 0; k < 3; ++k) s[k] = fminf(fmaxf(S[k], 1.f - mat.theta_c), 1.f + mat.theta_s);
+                            plastic_j = plastic_j * (S[0] * S[1] * S[2]) / (s[0] * s[1] * s[2]);
+#pragma unroll
+                            for (int k = 0; k < 3; ++k) S[k] = s[k];
+                            F = recompose(U, S, V);
+                        }
+                    }
+                    const float J = det3(F);
+                    const float hard = kind == KIND_SNOW ? expf(mat.xi * (1.f - plastic_j)) : 1.f;
+                    bool alive = true;
+                    if (MODE == MODE_G2P2G) {
+                        if (kind == KIND_FLUID) {
+                            // util/src/elastic.rs:546-553
+                            const float K = mat.bulk_modulus, gm = (float)mat.exponent;
+                            const float at_rest = K * (1.f - 1.f / (1.f - gm));
+                            energy = K * (J - powi_f(J, 1 - mat.exponent) / (1.f - gm)) - at_rest;
+                        } else if (!(J > 0.f)) {
+                            // try_elastic_energy_neo_hookean: J <= 0 -> FAILED (advance_particles.rs:73-74)
+                            packed |= SV_FAILED;
+                            atomicOr(&A.counters[C_STATUS], ST_INVERTED);
+                        } else if (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW) {
+                            // mu |F - R|^2 + lambda/2 (J - 1)^2 = mu sum (s - 1)^2 + ...
+                            const float d2 = (S[0] - 1.f) * (S[0] - 1.f) + (S[1] - 1.f) * (S[1] - 1.f) + (S[2] - 1.f) * (S[2] - 1.f);
+                            energy = mat.mu * hard * d2 + mat.lambda * hard / 2.f * (J - 1.f) * (J - 1.f);
+                        } else {
+                            // util/src/elastic.rs:233-241
+                            float I2 = 0.f;
+#pragma unroll
+                            for (int k = 0; k < 9; ++k) I2 += F.a[k] * F.a[k];
+                            const float lj = logf(J);
+                            energy = mat.mu / 2.f * (I2 - 3.f) - mat.mu * lj + mat.lambda / 2.f * lj * lj;
+                        }
+                        // cull (cull_particles.rs:17-41): strict domain bounds
+                        bool inside;
+                        if (!CELL) {
+                            inside = pos.x > A.L.domain_min[0] && pos.x < A.L.domain_max[0] && pos.y > A.L.domain_min[1] &&
+                                     pos.y < A.L.domain_max[1] && pos.z > A.L.domain_min[2] && pos.z < A.L.domain_max[2];
+                        } else {
+                            const double q[3] = {(double)cell.x + pos.x, (double)cell.y + pos.y, (double)cell.z + pos.z};
+                            inside = q[0] > A.L.dmin_cells[0] && q[0] < A.L.dmax_cells[0] && q[1] > A.L.dmin_cells[1] &&
+                                     q[1] < A.L.dmax_cells[1] && q[2] > A.L.dmin_cells[2] && q[2] < A.L.dmax_cells[2];
+                        }
+                        if (!inside) packed |= SV_TOMBSTONED;
+                        alive = !(packed & (SV_TOMBSTONED | SV_FAILED));
+                        // write the advanced state in sorted order
+                        pos.w = __uint_as_float(packed);
+                        A.out.pos[i] = pos;
+                        if (CELL) A.out.cell[i] = cell;
+                        A.out.vel[i] = make_float4(v[0], v[1], v[2], plastic_j);
+                        store_mat9(A.out.C, A.n, i, C);
+                        store_mat9(A.out.F, A.n, i, F);
+                        A.out.energy[i] = energy;
+                        A.out.orig[i] = A.in.orig[p];
+                    }
+                    int nbase[3];
+                    float nfx[3];
+                    grid_position<CELL>(pos, cell, dx, nbase, nfx);
+                    if (MODE == MODE_G2P2G && A.keys_out) {
+                        uint32_t key = SENTINEL_KEY;
+                        if (!(packed & SV_TOMBSTONED)) {
+                            bool ok;
+                            key = cell_key(nbase[0], nbase[1], nbase[2], A.L, ok);
+                            if (!ok) atomicOr(&A.counters[C_STATUS], ST_OUT_OF_GRID);
+                        }
+                        A.keys_out[i] = key;
+                    }
+                    if (alive) {
+                        // ---- scatter record of the next substep: external force
+                        // (external_force.rs:17-50) then the momentum of
+                        // scatter_momentum.rs:38-90
+                        v[0] += A.dt * A.gravity.x, v[1] += A.dt * A.gravity.y, v[2] += A.dt * A.gravity.z;
+                        const m3f PFt = stress_times_ft(mat, F, J, U, S, hard);
+                        make_record(mat, C, PFt, J, v, nfx, dx, A.dt, sh.rec[threadIdx.x]);
+                        sh.mass[threadIdx.x] = mat.mass;
+                        int4 gb;
+                        rcell = tile_cell(nbase, org, gb);
+                        if (rcell == REC_GLOBAL) sh.gbase[threadIdx.x] = gb;
+                    }
                 }
             }
-            const float Jn = det3(F);
-            if (kind == KIND_FLUID) {
-                // util/src/elastic.rs:546-553 inviscid energy
-                float K = mat.bulk_modulus, gm = (float)mat.exponent;
-                float at_rest = K * (1.f - 1.f / (1.f - gm));
-                energy = K * (Jn - powi_f(Jn, 1 - mat.exponent) / (1.f - gm)) - at_rest;
-            } else {
-                if (!(Jn > 0.f)) {
-                    // try_elastic_energy_neo_hookean: J <= 0 -> FAILED (advance_particles.rs:73-74)
-                    packed |= SV_FAILED;
-                    atomicOr(&A.counters[C_STATUS], ST_INVERTED);
-                } else if (kind == KIND_NEO_HOOKEAN || kind == KIND_SAND) {
-                    // util/src/elastic.rs:233-241
-                    float I2 = 0.f;
-#pragma unroll
-                    for (int k = 0; k < 9; ++k) I2 += F.a[k] * F.a[k];
-                    float lj = logf(Jn);
-                    energy = mat.mu / 2.f * (I2 - 3.f) - mat.mu * lj + mat.lambda / 2.f * lj * lj;
-                }
+            sh.cell[threadIdx.x] = rcell;
+            __syncthreads();
+            scatter_records(sh, count, A);
+            __syncthreads();
+        }
+        // flush the tile of grid_next
+        for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
+            const float m = sh.pt[0][t], px = sh.pt[1][t], py = sh.pt[2][t], pz = sh.pt[3][t];
+            if (m != 0.f || px != 0.f || py != 0.f || pz != 0.f) {
+                const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
+                const int32_t slot = sh.slot_next[tile_neighbour(tx, ty, tz)];
+                if (slot >= 0) atomicAdd(&A.grid_next[(uint64_t)slot * 64 + tile_local(tx, ty, tz)], make_float4(px, py, pz, m));
+                else atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR);
             }
-            // cull_particles.rs:17-41: strict domain bounds
-            bool inside;
-            if (!CELL) {
-                inside = pos.x > A.L.domain_min[0] && pos.x < A.L.domain_max[0] && pos.y > A.L.domain_min[1] &&
-                         pos.y < A.L.domain_max[1] && pos.z > A.L.domain_min[2] && pos.z < A.L.domain_max[2];
-            } else {
-                double q[3] = {(double)cell.x + pos.x, (double)cell.y + pos.y, (double)cell.z + pos.z};
-                inside = true;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) inside = inside && q[k] > A.L.dmin_cells[k] && q[k] < A.L.dmax_cells[k];
-            }
-            if (!inside) packed |= SV_TOMBSTONED;
-            uint32_t key = SENTINEL_KEY;
-            if (!(packed & SV_TOMBSTONED)) {
-                int nbase[3];
-                float nfx[3];
-                if (!CELL) {
-                    float4 np = pos;
-                    grid_position<false>(A.in, p, np, dx, nbase, nfx);
-                } else {
-                    float o[3] = {pos.x, pos.y, pos.z};
-                    int ci[3] = {cell.x, cell.y, cell.z};
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) nbase[k] = ci[k] - (o[k] >= 0.5f ? 0 : 1);
-                }
-                bool ok;
-                key = cell_key(nbase[0], nbase[1], nbase[2], A.L, ok);
-                if (!ok) atomicOr(&A.counters[C_STATUS], ST_OUT_OF_GRID);
-            }
-            pos.w = __uint_as_float(packed);
-            A.out.pos[i] = pos;
-            if (CELL) A.out.cell[i] = cell;
-            A.out.vel[i] = make_float4(v[0], v[1], v[2], plastic_j);
-            store_mat9(A.out.C, A.n, i, C);
-            store_mat9(A.out.F, A.n, i, F);
-            A.out.energy[i] = energy;
-            A.out.orig[i] = A.in.orig[p];
-            A.keys_out[i] = key;
         }
         __syncthreads();
     }
-    // count fp64 SVDs (one atomic per warp)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) fp64_count += __shfl_xor_sync(0xffffffffu, fp64_count, o);
-    if ((threadIdx.x & 31) == 0 && fp64_count) atomicAdd(&A.counters[C_FP64], fp64_count);
+    for (int o = 16; o > 0; o >>= 1) {
+        fp64_count += __shfl_xor_sync(0xffffffffu, fp64_count, o);
+        fallback += __shfl_xor_sync(0xffffffffu, fallback, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (fp64_count) atomicAdd(&A.counters[C_FP64], fp64_count);
+        if (fallback) atomicAdd(&A.counters[C_FALLBACK], fallback);
+    }
 }
 
-__global__ void k_finish(uint32_t *counters, uint64_t capacity) {
-    uint32_t slots = counters[C_NSLOT];
-    counters[C_NSLOT_PREV] = slots < capacity ? slots : (uint32_t)capacity;
+__global__ void k_finish(uint32_t *counters) {
     if (!counters[C_STOP]) counters[C_SUBSTEPS] += 1;
-}
-
-StepArgs make_args(sv_handle *h, float dt, float3 g) {
-    StepArgs A;
-    A.in = h->side[h->cur];
-    A.out = h->side[h->cur ^ 1];
-    A.mats = h->materials;
-    A.counters = h->counters;
-    A.perm = h->perm;
-    A.seg_start = h->seg_start;
-    A.seg_block = h->seg_block;
-    A.blockmap = h->blockmap;
-    A.grid = h->grid;
-    A.keys_out = h->keys;
-    A.n = h->n;
-    A.L = h->layout;
-    A.dt = dt;
-    A.gravity = g;
-    return A;
 }
 
 unsigned elem_blocks(uint64_t work) {
@@ -691,6 +815,29 @@ struct Scoped {
     Scoped(sv_handle *h_, const char *n) : h(h_), name(n) { timer_begin(h, name, &start); }
     ~Scoped() { timer_end(h, name, start); }
 };
+
+StepArgs make_args(sv_handle *h, float dt, float3 g) {
+    StepArgs A;
+    A.in = h->side[h->cur];
+    A.out = h->side[h->cur ^ 1];
+    A.mats = h->materials;
+    A.counters = h->counters;
+    A.perm = h->perm;
+    A.seg_start = h->seg_start;
+    A.seg_block = h->seg_block;
+    A.map_cur = h->blockmap[h->map_cur];
+    A.map_next = h->blockmap[h->map_next];
+    A.grid_cur = h->grid[h->gcur];
+    A.grid_next = h->grid[h->gcur ^ 1];
+    A.keys_out = h->keys;
+    A.n = h->n;
+    A.L = h->layout;
+    A.dt = dt;
+    A.gravity = g;
+    return A;
+}
+
+unsigned particle_blocks() { return (unsigned)sm_count() * 8; }
 
 }  // namespace
 
@@ -728,6 +875,7 @@ cudaError_t launch_sort_and_segments(sv_handle *h) {
                                h->stream);
         if (err != cudaSuccess) return err;
         h->launches += radix_sort_launches(h->n, h->layout.key_bits);
+        h->sorts += 1;
     }
     Scoped s(h, "segments");
     uint32_t tiles = (uint32_t)((h->n + SEG_TILE - 1) / SEG_TILE);
@@ -740,51 +888,62 @@ cudaError_t launch_sort_and_segments(sv_handle *h) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_grid_activate(sv_handle *h) {
+cudaError_t launch_activate(sv_handle *h, int which) {
     Scoped s(h, "activate");
-    k_reset_blockmap<<<elem_blocks(h->capacity), ELEM_THREADS, 0, h->stream>>>(h->blockmap, h->active_blocks, h->counters);
-    k_latch<<<1, 1, 0, h->stream>>>(h->counters, 1);
-    k_activate<<<elem_blocks(8 * h->n / 64 + 64), ELEM_THREADS, 0, h->stream>>>(
-        h->seg_block, h->blockmap, h->active_blocks, h->capacity, h->layout, h->counters);
-    k_clear_grid<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(h->grid, h->capacity, h->counters);
-    k_latch<<<1, 1, 0, h->stream>>>(h->counters, 0);
-    h->launches += 5;
+    k_map_reset<<<elem_blocks(h->capacity), ELEM_THREADS, 0, h->stream>>>(h->blockmap[which], h->active[which], h->counters,
+                                                                            which, h->capacity);
+    k_latch<<<1, 1, 0, h->stream>>>(h->counters, which, -1, h->capacity);
+    k_activate<<<elem_blocks(27 * h->n / 64 + 64), ELEM_THREADS, 0, h->stream>>>(
+        h->seg_block, h->blockmap[which], h->active[which], h->capacity, h->layout, h->counters, which);
+    k_latch<<<1, 1, 0, h->stream>>>(h->counters, -1, which, h->capacity);
+    h->launches += 4;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_clear(sv_handle *h, int grid_side, int which) {
+    Scoped s(h, "clear");
+    k_clear_grid<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(h->grid[grid_side], h->capacity, h->counters, which);
+    h->launches += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_p2g(sv_handle *h, float dt, float3 g) {
     StepArgs A = make_args(h, dt, g);
+    A.map_next = h->blockmap[h->map_cur];
+    A.grid_next = h->grid[h->gcur];
+    A.keys_out = nullptr;
     Scoped s(h, "p2g");
-    unsigned blocks = (unsigned)sm_count() * 6;
-    if (h->layout.position_form) k_p2g<true><<<blocks, P2G_THREADS, 0, h->stream>>>(A);
-    else k_p2g<false><<<blocks, P2G_THREADS, 0, h->stream>>>(A);
+    if (h->layout.position_form) k_particles<true, MODE_P2G><<<particle_blocks(), PT, 0, h->stream>>>(A);
+    else k_particles<false, MODE_P2G><<<particle_blocks(), PT, 0, h->stream>>>(A);
     h->launches += 1;
     return cudaGetLastError();
 }
 
-cudaError_t launch_grid_update(sv_handle *h) {
+cudaError_t launch_grid_update(sv_handle *h, bool clear_next) {
     Scoped s(h, "grid_update");
-    k_grid_update<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(h->grid, h->active_blocks, h->capacity,
-                                                                                 h->layout, h->counters);
-    k_latch<<<1, 1, 0, h->stream>>>(h->counters, 0);
+    k_grid_update<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(
+        h->grid[h->gcur], h->active[h->map_cur], clear_next ? h->grid[h->gcur ^ 1] : nullptr, h->capacity, h->layout,
+        h->counters, h->map_cur, h->map_next);
+    k_latch<<<1, 1, 0, h->stream>>>(h->counters, -1, -1, h->capacity);
     h->launches += 2;
     return cudaGetLastError();
 }
 
-cudaError_t launch_g2p(sv_handle *h, float dt) {
-    StepArgs A = make_args(h, dt, make_float3(0, 0, 0));
-    Scoped s(h, "g2p");
-    unsigned blocks = (unsigned)sm_count() * 6;
-    if (h->layout.position_form) k_g2p<true><<<blocks, G2P_THREADS, 0, h->stream>>>(A);
-    else k_g2p<false><<<blocks, G2P_THREADS, 0, h->stream>>>(A);
-    h->launches += 1;
-    return cudaGetLastError();
-}
-
-cudaError_t launch_finish_substep(sv_handle *h) {
-    k_finish<<<1, 1, 0, h->stream>>>(h->counters, h->capacity);
+cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 g, bool write_keys, bool use_perm) {
+    StepArgs A = make_args(h, dt, g);
+    if (!write_keys) A.keys_out = nullptr;
+    if (!use_perm) A.perm = nullptr;
+    Scoped s(h, "g2p2g");
+    if (h->layout.position_form) k_particles<true, MODE_G2P2G><<<particle_blocks(), PT, 0, h->stream>>>(A);
+    else k_particles<false, MODE_G2P2G><<<particle_blocks(), PT, 0, h->stream>>>(A);
+    k_finish<<<1, 1, 0, h->stream>>>(h->counters);
+    h->launches += 2;
+    h->vel_side = h->gcur;
+    h->vel_map = h->map_cur;
     h->cur ^= 1;
-    h->launches += 1;
+    h->gcur ^= 1;
+    h->map_cur = h->map_next;
+    h->keys_valid = write_keys;
     return cudaGetLastError();
 }
 

@@ -178,6 +178,7 @@ class Extras:
     position_form: int = 0
     svd_fp64_policy: int = 1
     block_capacity: int = 0
+    sort_interval: int = 0  # 0 adaptive, 1 every substep, k every k substeps
 
 
 @dataclass
@@ -257,6 +258,7 @@ class CudaState:
         c.position_form = extras.position_form
         c.svd_fp64_policy = extras.svd_fp64_policy
         c.block_capacity = extras.block_capacity
+        c.sort_interval = extras.sort_interval
         p = io_state.particles
         s = p.to_struct()
         h = ct.c_void_p()

@@ -34,10 +34,29 @@ def by_norm(a, b, rel, eps=1e-6):
     return err <= eps + rel * scale, err / max(scale, 1e-30)
 
 
-def compare_states(gpu, ref, live, tol=TOL):
+def compare_states(gpu, ref, live, tol=TOL, dx=None):
     for name, rel in tol.items():
         a = getattr(gpu, name)[live]
         b = getattr(ref, name)[live]
+        if name == "velocity_gradients" and dx is not None:
+            # C ~ |v| / dx is its natural scale: in a rigid motion C vanishes
+            # analytically and both sides hold only rounding noise.
+            a64, b64 = a.astype(np.float64), b.astype(np.float64)
+            scale = max(np.linalg.norm(b64), np.linalg.norm(ref.velocities[live].astype(np.float64)) / dx)
+            r = np.linalg.norm(a64 - b64) / max(scale, 1e-30)
+            assert r <= rel, f"{name}: error {r:.3e} of max(|C|, |v|/dx) > {rel}"
+            continue
+        if name == "elastic_energies":
+            # Near rest the energy is second order in fp32 noise of F
+            # (psi ~ modulus * eps^2): floor the scale at modulus * 1e-10 per particle.
+            a64, b64 = a.astype(np.float64), b.astype(np.float64)
+            modulus = max(float(np.max(np.abs(ref.mu[live]))) if ref.mu is not None else 0.0,
+                          float(np.max(np.abs(ref.lambda_[live]))) if ref.lambda_ is not None else 0.0,
+                          float(np.max(np.abs(ref.bulk_modulus[live]))) if ref.bulk_modulus is not None else 0.0)
+            scale = max(np.linalg.norm(b64), modulus * 1e-10 * np.sqrt(max(len(b64), 1)))
+            r = np.linalg.norm(a64 - b64) / max(scale, 1e-30)
+            assert r <= rel, f"{name}: error {r:.3e} of max(|E|, modulus 1e-10 sqrt(n)) > {rel}"
+            continue
         ok, r = by_norm(a, b, rel)
         assert ok, f"{name}: relative error {r:.3e} > {rel}"
 
@@ -92,8 +111,11 @@ def test_p2g_grid_matches_oracle(cuda_lib, oracle_mod, fp64):
     ref.p2g_only(s.dt, s.gravity)
     ids, m, v = ref.grid()
     np.testing.assert_array_equal(g.node_ids, ids)
-    # grid mass: FP32 sums of <= 216 positive terms in a different order
-    np.testing.assert_allclose(g.masses, m, rtol=4e-6, atol=0)
+    # grid mass: fp32 sums of <= 216 positive terms in another order; nodes at
+    # the stencil rim hold tiny weights whose own rounding dominates, hence the
+    # absolute floor of 1e-6 of a particle mass
+    m_p = float(s.io_state.particles.mass.max())
+    np.testing.assert_allclose(g.masses, m, rtol=4e-6, atol=1e-6 * m_p)
     ok, r = by_norm(g.velocities, v, 1e-5)
     assert ok, r
     gpu.close()
@@ -113,10 +135,10 @@ def test_p2g_conserves_momentum(cuda_lib):
 
 
 # ---------------------------------------------------------------- whole substeps
-@pytest.mark.parametrize("fp64", [False, True])
-def test_substeps_match_oracle(cuda_lib, oracle_mod, fp64):
+@pytest.mark.parametrize("fp64,sort_interval", [(False, 0), (True, 0), (True, 1), (True, 3)])
+def test_substeps_match_oracle(cuda_lib, oracle_mod, fp64, sort_interval):
     s = scenes.small_mixed()
-    gpu = CudaState.from_io_state(s.io_state, s.consts, s.extras)
+    gpu = CudaState.from_io_state(s.io_state, s.consts, Extras(sort_interval=sort_interval))
     status, done = gpu.step(s.substeps, s.dt, s.gravity)
     assert (status, done) == (0, s.substeps)
     out = gpu.download()
@@ -125,7 +147,7 @@ def test_substeps_match_oracle(cuda_lib, oracle_mod, fp64):
     exp = ref.download()
     np.testing.assert_array_equal(out.flags, exp.flags)
     live = (exp.flags & SV_TOMBSTONED) == 0
-    compare_states(out, exp, live)
+    compare_states(out, exp, live, dx=s.consts.grid_node_size)
     np.testing.assert_allclose(out.plastic_j, exp.plastic_j, rtol=1e-5)
     gpu.close()
 
@@ -140,7 +162,7 @@ def test_cube_64k_matches_fp64_oracle(cuda_lib, oracle_mod):
     assert ref.step(n, s.dt, s.gravity) == 0
     exp = ref.download()
     np.testing.assert_array_equal(out.flags, exp.flags)
-    compare_states(out, exp, np.ones(out.n, bool))
+    compare_states(out, exp, np.ones(out.n, bool), dx=s.consts.grid_node_size)
     gpu.close()
 
 
@@ -155,12 +177,52 @@ def test_cell_offset_positions_match_fp32_positions(cuda_lib, oracle_mod):
     ref.step(s.substeps, s.dt, s.gravity)
     exp = ref.download()
     live = (exp.flags & SV_TOMBSTONED) == 0
-    compare_states(rb, exp, live)
+    compare_states(rb, exp, live, dx=s.consts.grid_node_size)
     # the cell form is at least as close to the fp64 oracle in position
     ea = np.linalg.norm(ra.positions[live].astype(np.float64) - exp.positions[live])
     eb = np.linalg.norm(rb.positions[live].astype(np.float64) - exp.positions[live])
     assert eb <= ea * 1.5 + 1e-12
     a.close(), b.close()
+
+
+def test_split_calls_match_one_call(cuda_lib):
+    """The scatter left pending at the end of a call is reused by the next
+    call with the same dt and gravity, and redone when they differ."""
+    s = scenes.small_mixed()
+    one = CudaState.from_io_state(s.io_state, s.consts)
+    two = CudaState.from_io_state(s.io_state, s.consts)
+    three = CudaState.from_io_state(s.io_state, s.consts)
+    one.step(10, s.dt, s.gravity)
+    two.step(4, s.dt, s.gravity)
+    two.step(6, s.dt, s.gravity)
+    three.step(4, s.dt, (0.0, 0.0, 0.0))
+    three.step(6, s.dt, s.gravity)
+    a, b, c = one.download(), two.download(), three.download()
+    compare_states(b, a, np.ones(a.n, bool), dx=s.consts.grid_node_size)
+    # gravity differed for four substeps: velocities must differ
+    assert not np.allclose(c.velocities, a.velocities)
+    one.close(), two.close(), three.close()
+
+
+def test_fast_particles_rebin(cuda_lib, oracle_mod):
+    """Particles crossing several cells per substep leave their binning
+    tiles and blocks; the result must still match the oracle."""
+    s = scenes.small_mixed()
+    p = s.io_state.particles.copy()
+    dx = s.consts.grid_node_size
+    p.velocities[:] = np.array([1.5, -1.0, 0.7], np.float32) * (dx / s.dt)  # 1.5 cells per substep
+    p.velocity_gradients[:] = 0
+    io = IoState(0.0, p)
+    gpu = CudaState.from_io_state(io, s.consts, Extras(sort_interval=8))
+    assert gpu.step(6, s.dt, (0, 0, 0)) == (0, 6)
+    out = gpu.download()
+    ref = oracle_mod.OracleState(p, s.consts, None, fp64=True)
+    ref.step(6, s.dt, (0, 0, 0))
+    exp = ref.download()
+    np.testing.assert_array_equal(out.flags, exp.flags)
+    live = (exp.flags & SV_TOMBSTONED) == 0
+    compare_states(out, exp, live, dx=dx)
+    gpu.close()
 
 
 # ---------------------------------------------------------------- edge cases
@@ -190,7 +252,7 @@ def test_particles_leaving_domain_are_culled(cuda_lib, oracle_mod):
     np.testing.assert_array_equal(out.flags, exp.flags)
     assert (out.flags & SV_TOMBSTONED).any()
     live = (exp.flags & SV_TOMBSTONED) == 0
-    compare_states(out, exp, live)
+    compare_states(out, exp, live, dx=s.consts.grid_node_size)
     gpu.close()
 
 
@@ -245,7 +307,7 @@ def test_capacity_growth(cuda_lib, oracle_mod):
     assert small.step(3, s.dt, s.gravity) == (0, 3)
     big.step(3, s.dt, s.gravity)
     a, b = small.download(), big.download()
-    compare_states(a, b, np.ones(a.n, bool))
+    compare_states(a, b, np.ones(a.n, bool), dx=s.consts.grid_node_size)
     small.close(), big.close()
 
 
