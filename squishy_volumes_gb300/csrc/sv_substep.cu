@@ -431,12 +431,18 @@ __global__ void __launch_bounds__(ELEM_THREADS)
 }
 
 // ------------------------------------------------------------------ particle kernel
+// Scatter tile layout: node (tx, ty, tz) at tx*PX + ty*PY + tz.  With PX = 3
+// and PY = 9 (mod 32) the 27 stencil offsets 9i + 3j + k of any cell fall in
+// 27 distinct shared-memory banks, so a warp's lane-per-node atomics never
+// conflict.
+constexpr int PY = 9, PX = 99;
+constexpr int PLANE = 7 * PX + 7 * PY + 8;  // 764 floats
+
 struct Shared {
-    float4 gv[TILE_NODES];      // velocity tile of grid_cur (G2P2G)
-    float pt[4][TILE_NODES];    // mass, px, py, pz tile of grid_next
+    float4 gv[TILE_NODES];      // velocity tile of grid_cur (G2P2G), tx*64 + ty*8 + tz
+    float pt[4][PLANE];         // mass, px, py, pz tile of grid_next
     Rec rec[PT];
-    uint32_t cell[PT];          // REC_NONE, tile cell index, or REC_GLOBAL
-    float mass[PT];
+    float2 meta[PT];            // (record cell as bits: REC_NONE, tile index or REC_GLOBAL; mass)
     int4 gbase[PT];             // global base cell of REC_GLOBAL records
     int32_t slot_cur[27];
     int32_t slot_next[27];
@@ -452,69 +458,135 @@ __device__ __forceinline__ int tile_local(int tx, int ty, int tz) {
 }
 
 // Replays the chunk's scatter records: warp w owns records [32w, 32w + 32);
-// lane l < 27 is stencil offset (l/9, (l/3)%3, l%3).  Consecutive records
-// with the same base cell accumulate in registers before one shared atomic
-// per lane and component.
+// lane l < 27 is stencil offset (l/9, (l/3)%3, l%3).  Run starts and ends
+// (consecutive records with the same base cell) come from two ballots, so the
+// 32-record loop is unrolled with warp-uniform predicates only; a run is
+// summed in registers and leaves with one conflict-free shared atomic per
+// lane and component.
 __device__ __forceinline__ void scatter_records(Shared &sh, int count, const StepArgs &A) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int li = lane / 9, lj = (lane / 3) % 3, lk = lane % 3;
     const bool active = lane < 27;
-    float am = 0.f, ax = 0.f, ay = 0.f, az = 0.f;
-    uint32_t cur = REC_NONE;
-    const int r0 = warp * 32, r1 = min(r0 + 32, count);
-    for (int r = r0; r < r1; ++r) {
-        const uint32_t c = sh.cell[r];
-        if (c == REC_NONE) continue;
-        if (c != cur) {
-            if (cur != REC_NONE && active) {
-                const int t = (int)cur + li * 64 + lj * 8 + lk;
-                atomicAdd(&sh.pt[0][t], am);
-                atomicAdd(&sh.pt[1][t], ax);
-                atomicAdd(&sh.pt[2][t], ay);
-                atomicAdd(&sh.pt[3][t], az);
-            }
-            am = ax = ay = az = 0.f;
-            cur = c;
-        }
-        if (active) {
-            const float4 p0 = sh.rec[r].p[li], p1 = sh.rec[r].p[3 + lj], p2 = sh.rec[r].p[6 + lk];
+    const int off = li * PX + lj * PY + lk;
+    const int r0 = warp * 32;
+    if (r0 >= count) return;
+    const float2 me = lane < count - r0 ? sh.meta[r0 + lane] : make_float2(__uint_as_float(REC_NONE), 0.f);
+    const uint32_t key = __float_as_uint(me.x);
+    const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const uint32_t next = __shfl_down_sync(0xffffffffu, key, 1);
+    const bool valid = key != REC_NONE && key != REC_GLOBAL;
+    const uint32_t start = __ballot_sync(0xffffffffu, valid && (lane == 0 || prev != key));
+    const uint32_t end = __ballot_sync(0xffffffffu, valid && (lane == 31 || next != key));
+    const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
+    const uint32_t gmask = __ballot_sync(0xffffffffu, key == REC_GLOBAL);
+    float2 amx = make_float2(0.f, 0.f), ayz = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+        if ((vmask >> r) & 1u) {
+            const float4 p0 = sh.rec[r0 + r].p[li], p1 = sh.rec[r0 + r].p[3 + lj], p2 = sh.rec[r0 + r].p[6 + lk];
             const float w = p0.w * p1.w * p2.w;
-            const float m = sh.mass[r];
-            if (c == REC_GLOBAL) {
-                // outside the tile: straight to global memory
-                const int4 gb = sh.gbase[r];
-                int local;
-                const int32_t slot = node_slot(A.map_next, gb.x + li, gb.y + lj, gb.z + lk, A.L, local);
-                if (slot >= 0)
-                    atomicAdd(&A.grid_next[(uint64_t)slot * 64 + local],
-                              make_float4(w * (p0.x + p1.x + p2.x), w * (p0.y + p1.y + p2.y), w * (p0.z + p1.z + p2.z), w * m));
-                else
-                    atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR);
-            } else {
-                am += w * m;
-                ax += w * (p0.x + p1.x + p2.x);
-                ay += w * (p0.y + p1.y + p2.y);
-                az += w * (p0.z + p1.z + p2.z);
+            const float m = __shfl_sync(0xffffffffu, me.y, r);
+            const float2 sxy = __fadd2_rn(__fadd2_rn(make_float2(p0.x, p0.y), make_float2(p1.x, p1.y)), make_float2(p2.x, p2.y));
+            const float sz = p0.z + p1.z + p2.z;
+            if ((start >> r) & 1u) amx = make_float2(0.f, 0.f), ayz = make_float2(0.f, 0.f);
+            amx = __ffma2_rn(make_float2(w, w), make_float2(m, sxy.x), amx);
+            ayz = __ffma2_rn(make_float2(w, w), make_float2(sxy.y, sz), ayz);
+            if ((end >> r) & 1u) {
+                const int t = (int)__shfl_sync(0xffffffffu, key, r) + off;
+                if (active) {
+                    atomicAdd(&sh.pt[0][t], amx.x);
+                    atomicAdd(&sh.pt[1][t], amx.y);
+                    atomicAdd(&sh.pt[2][t], ayz.x);
+                    atomicAdd(&sh.pt[3][t], ayz.y);
+                }
             }
         }
-        if (c == REC_GLOBAL) cur = REC_NONE;
     }
-    if (cur != REC_NONE && cur != REC_GLOBAL && active) {
-        const int t = (int)cur + li * 64 + lj * 8 + lk;
-        atomicAdd(&sh.pt[0][t], am);
-        atomicAdd(&sh.pt[1][t], ax);
-        atomicAdd(&sh.pt[2][t], ay);
-        atomicAdd(&sh.pt[3][t], az);
+    // records outside the tile: straight to global memory
+    for (uint32_t g = gmask; g; g &= g - 1) {
+        const int r = __ffs(g) - 1;
+        const float4 p0 = sh.rec[r0 + r].p[li], p1 = sh.rec[r0 + r].p[3 + lj], p2 = sh.rec[r0 + r].p[6 + lk];
+        const float w = p0.w * p1.w * p2.w;
+        const float m = sh.meta[r0 + r].y;
+        const int4 gb = sh.gbase[r0 + r];
+        if (active) {
+            int local;
+            const int32_t slot = node_slot(A.map_next, gb.x + li, gb.y + lj, gb.z + lk, A.L, local);
+            if (slot >= 0)
+                atomicAdd(&A.grid_next[(uint64_t)slot * 64 + local],
+                          make_float4(w * (p0.x + p1.x + p2.x), w * (p0.y + p1.y + p2.y), w * (p0.z + p1.z + p2.z), w * m));
+            else
+                atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR);
+        }
     }
 }
 
-// Record slot for a particle scattering from base cell `base` into the tile
+// Record key for a particle scattering from base cell `base` into the tile
 // whose node 0 is global node `org`.
 __device__ __forceinline__ uint32_t tile_cell(const int base[3], const int org[3], int4 &gb) {
     const int tx = base[0] - org[0], ty = base[1] - org[1], tz = base[2] - org[2];
-    if (tx >= 0 && ty >= 0 && tz >= 0 && tx <= TN - 3 && ty <= TN - 3 && tz <= TN - 3) return (uint32_t)(tx * 64 + ty * 8 + tz);
+    if (tx >= 0 && ty >= 0 && tz >= 0 && tx <= TN - 3 && ty <= TN - 3 && tz <= TN - 3) return (uint32_t)(tx * PX + ty * PY + tz);
     gb = make_int4(base[0], base[1], base[2], 0);
     return REC_GLOBAL;
+}
+
+// G2P gather (collect_velocity.rs:40-72) of v and the unscaled C from the
+// shared velocity tile, factorised over the separable weights:
+// a_ij = sum_k wz_k g_ijk, b_ij = sum_k wz_k dZ_k g_ijk, then over j and i.
+__device__ __forceinline__ void gather_tile(const float4 *gv, int t0, const float w[3][3], const float d[3][3],
+                                            float v[3], m3f &C) {
+    float3 c[3], dd[3], e[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        c[i] = dd[i] = e[i] = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float3 a = make_float3(0.f, 0.f, 0.f), b = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float4 g = gv[t0 + i * 64 + j * 8 + k];
+                const float wz = w[2][k], wzd = w[2][k] * d[2][k];
+                a.x += wz * g.x, a.y += wz * g.y, a.z += wz * g.z;
+                b.x += wzd * g.x, b.y += wzd * g.y, b.z += wzd * g.z;
+            }
+            const float wy = w[1][j], wyd = w[1][j] * d[1][j];
+            c[i].x += wy * a.x, c[i].y += wy * a.y, c[i].z += wy * a.z;
+            dd[i].x += wyd * a.x, dd[i].y += wyd * a.y, dd[i].z += wyd * a.z;
+            e[i].x += wy * b.x, e[i].y += wy * b.y, e[i].z += wy * b.z;
+        }
+    }
+    v[0] = v[1] = v[2] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) C.a[k] = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float wx = w[0][i], wxd = w[0][i] * d[0][i];
+        v[0] += wx * c[i].x, v[1] += wx * c[i].y, v[2] += wx * c[i].z;
+        C.a[0] += wxd * c[i].x, C.a[1] += wxd * c[i].y, C.a[2] += wxd * c[i].z;
+        C.a[3] += wx * dd[i].x, C.a[4] += wx * dd[i].y, C.a[5] += wx * dd[i].z;
+        C.a[6] += wx * e[i].x, C.a[7] += wx * e[i].y, C.a[8] += wx * e[i].z;
+    }
+}
+
+// The same gather from global memory for particles outside their tile.
+__device__ __forceinline__ void gather_global(const StepArgs &A, const int base[3], const float w[3][3],
+                                              const float d[3][3], float v[3], m3f &C) {
+    v[0] = v[1] = v[2] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) C.a[k] = 0.f;
+    for (int ii = 0; ii < 3; ++ii)
+        for (int jj = 0; jj < 3; ++jj)
+            for (int kk = 0; kk < 3; ++kk) {
+                const float wt = w[0][ii] * w[1][jj] * w[2][kk];
+                int local;
+                const int32_t slot = node_slot(A.map_cur, base[0] + ii, base[1] + jj, base[2] + kk, A.L, local);
+                const float4 g = slot >= 0 ? A.grid_cur[(uint64_t)slot * 64 + local] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float gx = g.x * wt, gy = g.y * wt, gz = g.z * wt;
+                v[0] += gx, v[1] += gy, v[2] += gz;
+                C.a[0] += gx * d[0][ii], C.a[1] += gy * d[0][ii], C.a[2] += gz * d[0][ii];
+                C.a[3] += gx * d[1][jj], C.a[4] += gy * d[1][jj], C.a[5] += gz * d[1][jj];
+                C.a[6] += gx * d[2][kk], C.a[7] += gy * d[2][kk], C.a[8] += gz * d[2][kk];
+            }
 }
 
 template <bool CELL, int MODE> __global__ void __launch_bounds__(PT) k_particles(StepArgs A) {
@@ -549,7 +621,7 @@ template <bool CELL, int MODE> __global__ void __launch_bounds__(PT) k_particles
             sh.slot_next[threadIdx.x] = A.map_next[nbk];
             if (MODE == MODE_G2P2G) sh.slot_cur[threadIdx.x] = A.map_cur[nbk];
         }
-        for (int t = threadIdx.x; t < 4 * TILE_NODES; t += PT) (&sh.pt[0][0])[t] = 0.f;
+        for (int t = threadIdx.x; t < 4 * PLANE; t += PT) (&sh.pt[0][0])[t] = 0.f;
         __syncthreads();
         if (MODE == MODE_G2P2G) {
             for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
@@ -563,6 +635,7 @@ template <bool CELL, int MODE> __global__ void __launch_bounds__(PT) k_particles
             const uint32_t i = c0 + threadIdx.x;
             const int count = (int)min((uint32_t)PT, end - c0);
             uint32_t rcell = REC_NONE;
+            float rmass = 0.f;
             if (i < end) {
                 const uint32_t p = A.perm ? A.perm[i] : i;
                 float4 pos = A.in.pos[p];
@@ -595,38 +668,18 @@ template <bool CELL, int MODE> __global__ void __launch_bounds__(PT) k_particles
                         bspline_weights(fx[0], w[0]);
                         bspline_weights(fx[1], w[1]);
                         bspline_weights(fx[2], w[2]);
+                        float d[3][3];
+#pragma unroll
+                        for (int a = 0; a < 3; ++a)
+#pragma unroll
+                            for (int k = 0; k < 3; ++k) d[a][k] = ((float)k - fx[a]) * dx;
                         const int tx = base[0] - org[0], ty = base[1] - org[1], tz = base[2] - org[2];
                         const bool in_tile = tx >= 0 && ty >= 0 && tz >= 0 && tx <= TN - 3 && ty <= TN - 3 && tz <= TN - 3;
-                        v[0] = v[1] = v[2] = 0.f;
-#pragma unroll
-                        for (int k = 0; k < 9; ++k) C.a[k] = 0.f;
-                        if (!in_tile) ++fallback;
-#pragma unroll
-                        for (int ii = 0; ii < 3; ++ii) {
-                            const float ddx = ((float)ii - fx[0]) * dx;
-#pragma unroll
-                            for (int jj = 0; jj < 3; ++jj) {
-                                const float ddy = ((float)jj - fx[1]) * dx;
-                                const float wxy = w[0][ii] * w[1][jj];
-#pragma unroll
-                                for (int kk = 0; kk < 3; ++kk) {
-                                    const float ddz = ((float)kk - fx[2]) * dx;
-                                    const float wt = wxy * w[2][kk];
-                                    float4 g;
-                                    if (in_tile) {
-                                        g = sh.gv[(tx + ii) * 64 + (ty + jj) * 8 + (tz + kk)];
-                                    } else {
-                                        int local;
-                                        const int32_t slot = node_slot(A.map_cur, base[0] + ii, base[1] + jj, base[2] + kk, A.L, local);
-                                        g = slot >= 0 ? A.grid_cur[(uint64_t)slot * 64 + local] : make_float4(0.f, 0.f, 0.f, 0.f);
-                                    }
-                                    const float gx = g.x * wt, gy = g.y * wt, gz = g.z * wt;
-                                    v[0] += gx, v[1] += gy, v[2] += gz;
-                                    C.a[0] += gx * ddx, C.a[1] += gy * ddx, C.a[2] += gz * ddx;
-                                    C.a[3] += gx * ddy, C.a[4] += gy * ddy, C.a[5] += gz * ddy;
-                                    C.a[6] += gx * ddz, C.a[7] += gy * ddz, C.a[8] += gz * ddz;
-                                }
-                            }
+                        if (in_tile) {
+                            gather_tile(sh.gv, tx * 64 + ty * 8 + tz, w, d, v, C);
+                        } else {
+                            ++fallback;
+                            gather_global(A, base, w, d, v, C);
                         }
                         const float cscale = 4.f / dx / dx;
 #pragma unroll
@@ -762,23 +815,24 @@ template <bool CELL, int MODE> __global__ void __launch_bounds__(PT) k_particles
                         v[0] += A.dt * A.gravity.x, v[1] += A.dt * A.gravity.y, v[2] += A.dt * A.gravity.z;
                         const m3f PFt = stress_times_ft(mat, F, J, U, S, hard);
                         make_record(mat, C, PFt, J, v, nfx, dx, A.dt, sh.rec[threadIdx.x]);
-                        sh.mass[threadIdx.x] = mat.mass;
+                        rmass = mat.mass;
                         int4 gb;
                         rcell = tile_cell(nbase, org, gb);
                         if (rcell == REC_GLOBAL) sh.gbase[threadIdx.x] = gb;
                     }
                 }
             }
-            sh.cell[threadIdx.x] = rcell;
+            sh.meta[threadIdx.x] = make_float2(__uint_as_float(rcell), rmass);
             __syncthreads();
             scatter_records(sh, count, A);
             __syncthreads();
         }
         // flush the tile of grid_next
         for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
-            const float m = sh.pt[0][t], px = sh.pt[1][t], py = sh.pt[2][t], pz = sh.pt[3][t];
+            const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
+            const int s = tx * PX + ty * PY + tz;
+            const float m = sh.pt[0][s], px = sh.pt[1][s], py = sh.pt[2][s], pz = sh.pt[3][s];
             if (m != 0.f || px != 0.f || py != 0.f || pz != 0.f) {
-                const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
                 const int32_t slot = sh.slot_next[tile_neighbour(tx, ty, tz)];
                 if (slot >= 0) atomicAdd(&A.grid_next[(uint64_t)slot * 64 + tile_local(tx, ty, tz)], make_float4(px, py, pz, m));
                 else atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR);
