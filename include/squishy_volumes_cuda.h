@@ -171,6 +171,31 @@ int sv_grid_layout(sv_handle *h, int32_t origin[3], int32_t nblocks[3]);
  * memory per call). */
 int sv_sort_pairs(const uint32_t *keys, uint32_t *perm, uint64_t n);
 
+/* No counterpart in the reference.  The same stable sort as sv_sort_pairs,
+ * for callers that must not allocate device memory: a plugin running inside
+ * a host application that hands out the whole device-memory budget from its
+ * own pool, or code that records its work into a CUDA graph, where a
+ * cudaMalloc would break the budget or the capture.  It allocates nothing:
+ * its scratch is one fixed array of about 13 MB compiled into the library,
+ * which every GPU that loads the library holds until the process exits.
+ *  - keys and perm are DEVICE pointers to n uint32 each, owned by the
+ *    caller; perm receives the permutation that stably sorts keys.
+ *  - n may be at most SV_NOALLOC_MAX_KEYS; larger n is rejected with an
+ *    error and nothing is launched.
+ *  - The work is queued on `stream` (a cudaStream_t passed as void*, NULL for
+ *    the default stream) and the call returns without waiting for it.
+ *  - The first call on a device looks up the scratch array's device address
+ *    (with that device current) and keeps it; make that first call before
+ *    any stream capture.
+ *  - All calls share the one scratch array, so calls that can overlap on the
+ *    GPU (other streams, other host threads) race: order them on one stream
+ *    or synchronise between them.  The scratch needs no clearing between
+ *    calls: every value in it is written before it is read.
+ *  - Returns 0, or -1 with a message copied into error[0..error_capacity). */
+#define SV_NOALLOC_MAX_KEYS (1u << 20)
+int sv_sort_pairs_noalloc(const uint32_t *keys, uint32_t *perm, uint64_t n, void *stream, char *error,
+                          uint64_t error_capacity);
+
 typedef struct sv_stats {
     uint64_t particles;
     uint64_t live_particles;

@@ -4,6 +4,9 @@
 // processed row by row (so equal digits keep input order).
 #include "sv_sort.cuh"
 
+#include <cstring>
+#include <mutex>
+
 namespace sv {
 
 namespace {
@@ -262,3 +265,85 @@ cudaError_t radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, u
 }
 
 }  // namespace sv
+
+// ---------------------------------------------------------------------------
+// Allocation-free sort (sv_sort_pairs_noalloc in the C ABI).
+//
+// Some callers cannot call cudaMalloc: a plugin inside a host application
+// that owns the whole device-memory budget through its own pool, or code
+// recording work into a CUDA graph, where an allocation would break the
+// accounting or the capture.  For them the sort's scratch (the sorted keys,
+// the ping-pong pair buffers, the digit histograms and the scan partials)
+// lives in one file-scope device array of fixed size instead, so the call
+// allocates nothing.  The array exists on every GPU that loads the library
+// for the life of the process.
+namespace sv {
+namespace {
+
+constexpr uint64_t NOALLOC_MAX_KEYS = 1ull << 20;  // SV_NOALLOC_MAX_KEYS in the C header
+
+constexpr size_t ce_align(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t ce_scan_temp(uint64_t n) {
+    return n > (uint64_t)SCAN_TILE ? ce_align(((n + SCAN_TILE - 1) / SCAN_TILE) * 4) + ce_scan_temp((n + SCAN_TILE - 1) / SCAN_TILE)
+                                   : 256;
+}
+constexpr size_t ce_sort_temp(uint64_t n) {
+    return 2 * ce_align(n * 4) + 2 * ce_align(((n + SORT_TILE - 1) / SORT_TILE) * RADIX * 4) +
+           ce_scan_temp(((n + SORT_TILE - 1) / SORT_TILE) * RADIX);
+}
+// sorted keys, then the radix sort's temporary storage
+constexpr size_t NOALLOC_KEYS_BYTES = ce_align(NOALLOC_MAX_KEYS * 4);
+constexpr size_t NOALLOC_BYTES = NOALLOC_KEYS_BYTES + ce_sort_temp(NOALLOC_MAX_KEYS);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+// Device address of g_noalloc_scratch per device, looked up once per device
+// with that device current (the host-side name is only a stand-in).
+constexpr int NOALLOC_MAX_DEVICES = 64;
+void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+std::mutex g_noalloc_mutex;
+
+}  // namespace
+
+}  // namespace sv
+
+extern "C" {
+
+int sv_sort_pairs_noalloc(const uint32_t *keys, uint32_t *perm, uint64_t n, void *stream, char *error, uint64_t error_capacity) {
+    using namespace sv;
+    auto report = [&](const char *msg) {
+        if (error && error_capacity) {
+            std::strncpy(error, msg, error_capacity - 1);
+            error[error_capacity - 1] = 0;
+        }
+        return -1;
+    };
+    if (n == 0) return 0;
+    if (n > NOALLOC_MAX_KEYS) return report("sv_sort_pairs_noalloc: n exceeds SV_NOALLOC_MAX_KEYS (1048576)");
+    if (!keys || !perm) return report("sv_sort_pairs_noalloc: NULL argument");
+    if (radix_sort_temp_bytes(n) > NOALLOC_BYTES - NOALLOC_KEYS_BYTES)
+        return report("sv_sort_pairs_noalloc: internal scratch size mismatch");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return report("sv_sort_pairs_noalloc: no usable current device");
+    void *base;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_addr[dev]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) return report(cudaGetErrorString(e));
+            g_noalloc_addr[dev] = p;
+        }
+        base = g_noalloc_addr[dev];
+    }
+    // Nothing in the scratch needs to start at zero: every histogram, scan
+    // and pair buffer is fully written before it is read.
+    uint32_t *sorted_keys = static_cast<uint32_t *>(base);
+    void *temp = static_cast<unsigned char *>(base) + NOALLOC_KEYS_BYTES;
+    cudaError_t e = radix_sort_pairs(keys, nullptr, sorted_keys, perm, n, 32, temp, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return report(cudaGetErrorString(e));
+    return 0;
+}
+
+}  // extern "C"
