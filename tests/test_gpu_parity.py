@@ -135,6 +135,39 @@ def test_p2g_conserves_momentum(cuda_lib):
 
 
 # ---------------------------------------------------------------- whole substeps
+def test_matches_committed_golden_vectors(cuda_lib):
+    """The CUDA path against tests/golden/oracle_small_mixed.npz (fp64 oracle
+    output committed with its generator, tests/golden/make_golden.py)."""
+    from pathlib import Path
+
+    from squishy_volumes_gb300 import Particles
+
+    g = np.load(Path(__file__).parent / "golden" / "oracle_small_mixed.npz")
+    names = ["flags", "positions", "position_gradients", "velocities", "velocity_gradients", "mass",
+             "initial_volume", "mu", "lambda_", "sand_alpha", "exponent", "bulk_modulus", "viscosity_dynamic",
+             "viscosity_bulk", "model", "hardening", "crit_compression", "crit_stretch", "plastic_j"]
+    p = Particles(**{k: g[f"in_{k}"] for k in names})
+    consts = InputConsts(grid_node_size=float(g["grid_node_size"]), domain_min=tuple(g["domain_min"]),
+                         domain_max=tuple(g["domain_max"]))
+    gpu = CudaState.from_io_state(IoState(0.0, p), consts)
+    assert gpu.step(int(g["substeps"]), float(g["dt"]), g["gravity"]) == (0, int(g["substeps"]))
+    out = gpu.download()
+
+    class Ref:
+        pass
+
+    ref = Ref()
+    for k in ["flags", "positions", "position_gradients", "velocities", "velocity_gradients", "elastic_energies",
+              "plastic_j"]:
+        setattr(ref, k, g[f"out_{k}"])
+    ref.mu, ref.lambda_, ref.bulk_modulus = p.mu, p.lambda_, p.bulk_modulus
+    np.testing.assert_array_equal(out.flags, ref.flags)
+    live = (ref.flags & SV_TOMBSTONED) == 0
+    compare_states(out, ref, live, dx=consts.grid_node_size)
+    gpu.close()
+
+
+
 @pytest.mark.parametrize("fp64,sort_interval", [(False, 0), (True, 0), (True, 1), (True, 3)])
 def test_substeps_match_oracle(cuda_lib, oracle_mod, fp64, sort_interval):
     s = scenes.small_mixed()
