@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bound on the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--error-substeps", type=int, default=0,
+                    help="also run this many substeps from the initial state on the GPU and on the fp64 CPU oracle "
+                         "and report the relative errors of x, v, C, F")
     return ap.parse_args()
 
 
@@ -150,8 +153,41 @@ def cpu_baseline(scene, seconds_budget: float):
     }
 
 
+def error_vs_fp64(scene, substeps: int):
+    """Relative L2 error of the GPU state against the fp64 oracle after
+    `substeps` substeps from the same initial state (live particles)."""
+    import oracle
+    from squishy_volumes_gb300 import CudaState
+
+    gpu = CudaState.from_io_state(scene.io_state, scene.consts, scene.extras)
+    gpu.step(substeps, scene.dt, scene.gravity)
+    out = gpu.download()
+    gpu.close()
+    ref = oracle.OracleState(scene.io_state.particles, scene.consts, scene.extras, fp64=True,
+                             threads=os.cpu_count() or 1)
+    ref.step(substeps, scene.dt, scene.gravity)
+    exp = ref.download()
+    ref.close()
+    live = (exp.flags & 32) == 0
+    res = {"substeps": substeps, "particles_compared": int(live.sum())}
+    vnorm = np.linalg.norm(exp.velocities[live].astype(np.float64))
+    for k in ("positions", "velocities", "velocity_gradients", "position_gradients"):
+        a = getattr(out, k)[live].astype(np.float64)
+        b = getattr(exp, k)[live].astype(np.float64)
+        d = np.abs(a - b)
+        # C vanishes in rigid motion; its natural scale is |v| / dx
+        scale = max(np.linalg.norm(b), vnorm / scene.consts.grid_node_size) if k == "velocity_gradients" \
+            else np.linalg.norm(b)
+        res[k] = {"rel_l2": float(np.linalg.norm(a - b) / max(scale, 1e-300)), "max_abs": float(d.max()) if d.size else 0.0}
+    res["flags_equal"] = bool(np.array_equal(out.flags, exp.flags))
+    return res
+
+
 def algorithmic_bytes(kernel: str, live: int, grid_nodes: int, cell_form: bool):
-    """Algorithmic HBM bytes per launch (SURVEY 8d per-unit figures)."""
+    """Algorithmic HBM bytes per launch: per particle-substep the particle
+    state is read (x 12, v 12, C 36, F 36, material/flags 4 = 100 B) and
+    written (96 B), +12 B each way in the int32-cell form; per active grid
+    node the scatter writes m + p (16 B) and the gather reads v (12 B)."""
     x = 12 + (12 if cell_form else 0)
     if kernel == "g2p2g":
         # one full particle-substep: read x, v, C, F, material/flags, write
@@ -181,11 +217,28 @@ def run_ours(args, rank, world, local):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=dev)
-    scene = scenes.SCENES[args.scene]()
+    made = scenes.SCENES[args.scene]()
+    if isinstance(made, list):
+        # batched configuration: every scene in one handle; the CPU baseline
+        # and the fp64 error report use the largest scene alone
+        from squishy_volumes_gb300.state import BatchedCudaState
+
+        batch = made
+        scene = max(batch, key=lambda s: s.io_state.particles.n)
+        n = sum(s.io_state.particles.n for s in batch)
+        scene.extras.sort_interval = args.sort_interval
+        make_gpu = lambda: BatchedCudaState.from_scenes([s.io_state for s in batch], [s.consts for s in batch],
+                                                       scene.extras)
+        h2d_particles = [s.io_state.particles for s in batch]
+    else:
+        batch = None
+        scene = made
+        n = scene.io_state.particles.n
+        scene.extras.sort_interval = args.sort_interval
+        make_gpu = lambda: CudaState.from_io_state(scene.io_state, scene.consts, scene.extras)
+        h2d_particles = [scene.io_state.particles]
     p = scene.io_state.particles
-    n = p.n
-    scene.extras.sort_interval = args.sort_interval
-    gpu = CudaState.from_io_state(scene.io_state, scene.consts, scene.extras)
+    gpu = make_gpu()
     # warm-up
     status, done = gpu.step(args.warmup, scene.dt, scene.gravity)
     if status:
@@ -261,7 +314,8 @@ def run_ours(args, rank, world, local):
         "share": round(prof[dom]["ms"] / total_ms, 4),
         "kernels_ms_per_substep": {k: round(v["ms"] / args.steps, 5) for k, v in prof.items()},
     }
-    # whole-substep roofline with the SURVEY 8d per-particle-substep figure
+    # whole-substep roofline: 212 B per particle-substep of state and binning
+    # (+24 B in the int32-cell form) plus 56 B per active grid node
     rho = grid_nodes / max(live, 1)
     bps = 212 + (24 if cell_form else 0) + 56 * rho
     sub_achieved = bps * live * args.steps / elapsed / 1e9 * world
@@ -278,11 +332,11 @@ def run_ours(args, rank, world, local):
         frame_substeps = int(math.ceil((1.0 / fps) / scene.dt))
         frame_substeps = min(frame_substeps, scene.substeps)
         reps = 2
-        h2d = p.nbytes()
+        h2d = sum(q.nbytes() for q in h2d_particles)
         d2h = 0
         t0 = time.perf_counter()
         for _ in range(reps):
-            st_ = CudaState.from_io_state(scene.io_state, scene.consts, scene.extras)
+            st_ = make_gpu()
             params = RunParameters(target_time=frame_substeps * scene.dt * (1 - 1e-9), max_time_step=scene.dt)
             io, err = st_.produce_next_state(Harness(), FrameInput(scene.consts, scene.gravity), params)
             d2h = sum(getattr(io.particles, k).nbytes for k in
@@ -298,6 +352,10 @@ def run_ours(args, rank, world, local):
             "substeps_per_step": frame_substeps,
             "step": "sv_create (upload) + one frame of substeps + sv_download",
         }
+
+    error = None
+    if args.error_substeps > 0 and rank == 0:
+        error = error_vs_fp64(scene, args.error_substeps)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -319,6 +377,7 @@ def run_ours(args, rank, world, local):
         "config": {
             "workload": args.scene,
             "particles": n,
+            "scenes": len(batch) if batch else 1,
             "live_particles": live,
             "grid_blocks": st["grid_blocks"],
             "binning_sort_interval": st["sort_interval"],
@@ -333,6 +392,7 @@ def run_ours(args, rank, world, local):
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "fp64_svd_particles": st["fp64_svd"],
+        "error_vs_fp64": error,
     }
     if rank == 0:
         print(json.dumps(line))

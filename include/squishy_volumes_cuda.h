@@ -145,6 +145,20 @@ int sv_download_grid(sv_handle *h, int32_t *node_ids, float *masses, float *velo
 
 void sv_destroy(sv_handle *h);
 
+/* Addition (not in the reference): many independent scenes advanced by the
+ * same launches.  Scene s has its own consts[s] (domain, cull bounds) and
+ * particles[s]; all scenes share grid_node_size, the ground plane (which must
+ * be on axis 2) and the SVD policy, and are stepped together by sv_step with
+ * one dt and gravity.  Scenes are placed side by side in x and y in one block
+ * index and always use the int32-cell + fp32-offset position form, so their
+ * placement is an exact whole-cell translation; sv_download and
+ * sv_download_scene return positions in each scene's own coordinates, while
+ * grid node ids from sv_download_grid are in the shared placement. */
+int sv_create_batched(const sv_consts *consts, const sv_particles *particles, uint32_t n_scenes, sv_handle **out);
+uint32_t sv_scene_count(sv_handle *h);
+/* sv_download restricted to one scene (out->n must equal that scene's count). */
+int sv_download_scene(sv_handle *h, uint32_t scene, sv_particles *out);
+
 /* Message of the last failure on this thread ("" if none). */
 const char *sv_last_error_string(void);
 

@@ -102,6 +102,10 @@ _SIGNATURES = {
     "sv_download": (ct.c_int, [ct.c_void_p, ct.POINTER(SvParticles)]),
     "sv_download_grid": (ct.c_int, [ct.c_void_p, i32p, f32p, f32p, ct.c_uint64, ct.POINTER(ct.c_uint64)]),
     "sv_destroy": (None, [ct.c_void_p]),
+    "sv_create_batched": (ct.c_int, [ct.POINTER(SvConsts), ct.POINTER(SvParticles), ct.c_uint32,
+                                     ct.POINTER(ct.c_void_p)]),
+    "sv_scene_count": (ct.c_uint32, [ct.c_void_p]),
+    "sv_download_scene": (ct.c_int, [ct.c_void_p, ct.c_uint32, ct.POINTER(SvParticles)]),
     "sv_last_error_string": (ct.c_char_p, []),
     "sv_p2g_only": (ct.c_int, [ct.c_void_p, ct.c_float, f32p]),
     "sv_binning": (ct.c_int, [ct.c_void_p, u32p, u32p, u32p]),

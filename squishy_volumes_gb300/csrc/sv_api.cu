@@ -2,6 +2,7 @@
 // upload/download in the reference's particle layout, and the substep loop of
 // CpuState::produce_next_state (rust/crates/cpu/src/cpu_state.rs:146-197).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -50,7 +51,7 @@ void free_handle(sv_handle *h) {
     cudaFree(h->materials), cudaFree(h->keys), cudaFree(h->sorted_keys), cudaFree(h->perm), cudaFree(h->sort_temp);
     cudaFree(h->seg_start), cudaFree(h->seg_block), cudaFree(h->tile_counts), cudaFree(h->scan_temp);
     for (int s = 0; s < 2; ++s) cudaFree(h->blockmap[s]), cudaFree(h->active[s]), cudaFree(h->grid[s]);
-    cudaFree(h->counters);
+    cudaFree(h->counters), cudaFree(h->scenes);
     if (h->host_counters) cudaFreeHost(h->host_counters);
     for (auto &p : h->timer.pending) cudaEventDestroy(p.second.first), cudaEventDestroy(p.second.second);
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -238,24 +239,46 @@ extern "C" {
 
 const char *sv_last_error_string(void) { return g_last_error.c_str(); }
 
-int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) {
-    g_last_error.clear();
-    if (!c || !p || !out) return fail("sv_create: NULL argument");
-    *out = nullptr;
-    const uint64_t n = p->n;
-    if (n >= (1ull << 31)) return fail("sv_create: too many particles (limit 2^31 - 1)");
-    if (n > 0 && (!p->flags || !p->positions || !p->position_gradients || !p->velocities || !p->velocity_gradients ||
-                  !p->mass || !p->initial_volume))
-        return fail("sv_create: required particle array is NULL");
-    if (!(c->grid_node_size > 0.f)) return fail("sv_create: grid_node_size must be positive");
-    if (c->position_form > 1) return fail("sv_create: unknown position_form");
-    if (c->ground_mode < 0 || c->ground_mode > 2 || c->ground_axis < 0 || c->ground_axis > 2)
-        return fail("sv_create: invalid ground plane settings");
-    for (uint64_t i = 0; i < n; ++i)
-        if (p->collider_bits && p->collider_bits[i] != 0)
-            return fail("sv_create: collider bits are set but colliders are not supported by this backend");
+namespace {
 
-    // materials (deduplicated ParticleParameters)
+// Shared by sv_create (one scene) and sv_create_batched (many).  Batched
+// scenes are laid side by side in x and y in one block index, each
+// translated by a whole number of cells (so translation is exact in the
+// int32-cell position form, which batched handles always use) and separated
+// by at least 16 cells, more than any particle can travel before its own
+// scene's domain culls it.
+int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, bool batched, sv_handle **out) {
+    g_last_error.clear();
+    if (!cs || !ps || !out || n_scenes == 0) return fail("sv_create: NULL argument");
+    *out = nullptr;
+    const sv_consts &c = cs[0];
+    uint64_t n = 0;
+    std::vector<uint64_t> first(n_scenes + 1, 0);
+    for (uint32_t s = 0; s < n_scenes; ++s) {
+        const sv_particles *p = &ps[s];
+        const sv_consts &cc = cs[s];
+        if (p->n > 0 && (!p->flags || !p->positions || !p->position_gradients || !p->velocities ||
+                         !p->velocity_gradients || !p->mass || !p->initial_volume))
+            return fail("sv_create: required particle array is NULL");
+        if (!(cc.grid_node_size > 0.f)) return fail("sv_create: grid_node_size must be positive");
+        if (cc.position_form > 1) return fail("sv_create: unknown position_form");
+        if (cc.ground_mode < 0 || cc.ground_mode > 2 || cc.ground_axis < 0 || cc.ground_axis > 2)
+            return fail("sv_create: invalid ground plane settings");
+        if (batched && (cc.grid_node_size != c.grid_node_size || cc.ground_mode != c.ground_mode ||
+                        cc.ground_axis != c.ground_axis || cc.ground_height != c.ground_height ||
+                        cc.svd_fp64_policy != c.svd_fp64_policy))
+            return fail("sv_create_batched: scenes must share grid_node_size, ground plane and SVD policy");
+        if (batched && cc.ground_mode != 0 && cc.ground_axis != 2)
+            return fail("sv_create_batched: the ground plane must be on axis 2 (scenes are laid out in x and y)");
+        for (uint64_t i = 0; i < p->n; ++i)
+            if (p->collider_bits && p->collider_bits[i] != 0)
+                return fail("sv_create: collider bits are set but colliders are not supported by this backend");
+        first[s + 1] = first[s] + p->n;
+    }
+    n = first[n_scenes];
+    if (n >= (1ull << 31)) return fail("sv_create: too many particles (limit 2^31 - 1)");
+
+    // materials (deduplicated ParticleParameters, one set per scene)
     std::vector<Material> mats;
     std::vector<uint32_t> mat_index(n);
     {
@@ -263,72 +286,113 @@ int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) {
         Material prev{};
         uint32_t prev_idx = UINT32_MAX;
         std::string err;
-        for (uint64_t i = 0; i < n; ++i) {
-            Material m;
-            if (build_material(p, i, m, err)) return fail("sv_create: " + err);
-            if (prev_idx != UINT32_MAX && std::memcmp(&m, &prev, sizeof(m)) == 0) {
-                mat_index[i] = prev_idx;
-                continue;
+        for (uint32_t s = 0; s < n_scenes; ++s) {
+            const sv_particles *p = &ps[s];
+            for (uint64_t i = 0; i < p->n; ++i) {
+                Material m;
+                if (build_material(p, i, m, err)) return fail("sv_create: " + err);
+                m.scene = s;
+                const uint64_t gi = first[s] + i;
+                if (prev_idx != UINT32_MAX && std::memcmp(&m, &prev, sizeof(m)) == 0) {
+                    mat_index[gi] = prev_idx;
+                    continue;
+                }
+                auto it = index.find(MaterialKey{m});
+                uint32_t idx;
+                if (it == index.end()) {
+                    idx = (uint32_t)mats.size();
+                    if (idx >= MAX_MATERIALS) return fail("sv_create: more than 2^24 distinct particle parameter sets");
+                    index.emplace(MaterialKey{m}, idx);
+                    mats.push_back(m);
+                } else {
+                    idx = it->second;
+                }
+                mat_index[gi] = idx;
+                prev = m, prev_idx = idx;
             }
-            auto it = index.find(MaterialKey{m});
-            uint32_t idx;
-            if (it == index.end()) {
-                idx = (uint32_t)mats.size();
-                if (idx >= MAX_MATERIALS) return fail("sv_create: more than 2^24 distinct particle parameter sets");
-                index.emplace(MaterialKey{m}, idx);
-                mats.push_back(m);
-            } else {
-                idx = it->second;
-            }
-            mat_index[i] = idx;
-            prev = m, prev_idx = idx;
         }
         if (mats.empty()) mats.push_back(Material{});
     }
 
     sv_handle *h = new sv_handle();
     h->n = n;
-    if (c->sort_interval == 0) {
+    h->batched = batched;
+    h->scene_first = first;
+    if (c.sort_interval == 0) {
         h->adaptive_interval = true;
         h->sort_interval = h->max_interval = 8;
     } else {
         h->adaptive_interval = false;
-        h->sort_interval = h->max_interval = c->sort_interval;
+        h->sort_interval = h->max_interval = c.sort_interval;
     }
     GridLayout &L = h->layout;
-    L.dx = c->grid_node_size;
-    L.ground_mode = c->ground_mode, L.ground_axis = c->ground_axis, L.ground_height = c->ground_height;
-    L.position_form = c->position_form;
-    L.svd_policy = c->svd_fp64_policy;
+    L.dx = c.grid_node_size;
+    L.ground_mode = c.ground_mode, L.ground_axis = c.ground_axis, L.ground_height = c.ground_height;
+    L.position_form = batched ? 1u : c.position_form;
+    L.svd_policy = c.svd_fp64_policy;
     for (int a = 0; a < 3; ++a) {
-        L.domain_min[a] = c->domain_min[a], L.domain_max[a] = c->domain_max[a];
-        L.dmin_cells[a] = (double)c->domain_min[a] / (double)L.dx;
-        L.dmax_cells[a] = (double)c->domain_max[a] / (double)L.dx;
+        L.domain_min[a] = c.domain_min[a], L.domain_max[a] = c.domain_max[a];
+        L.dmin_cells[a] = (double)c.domain_min[a] / (double)L.dx;
+        L.dmax_cells[a] = (double)c.domain_max[a] / (double)L.dx;
     }
-    // Block index bounds: the domain plus the initial live particles (which
+    // Per scene: cell extent of its domain and initial live particles (which
     // may start outside the domain; they are culled after their first substep).
-    double lo[3], hi[3];
-    for (int a = 0; a < 3; ++a) lo[a] = c->domain_min[a], hi[a] = c->domain_max[a];
-    for (uint64_t i = 0; i < n; ++i) {
-        if (p->flags[i] & SV_TOMBSTONED) continue;
-        for (int a = 0; a < 3; ++a) {
-            double x = p->positions[3 * i + a];
-            if (!std::isfinite(x)) {
-                free_handle(h);
-                return fail("sv_create: non-finite particle position");
+    std::vector<SceneInfo> scenes(n_scenes);
+    std::vector<std::array<int64_t, 3>> clo(n_scenes), chi(n_scenes);
+    for (uint32_t s = 0; s < n_scenes; ++s) {
+        const sv_particles *p = &ps[s];
+        double lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) lo[a] = cs[s].domain_min[a], hi[a] = cs[s].domain_max[a];
+        for (uint64_t i = 0; i < p->n; ++i) {
+            if (p->flags[i] & SV_TOMBSTONED) continue;
+            for (int a = 0; a < 3; ++a) {
+                double x = p->positions[3 * i + a];
+                if (!std::isfinite(x)) {
+                    free_handle(h);
+                    return fail("sv_create: non-finite particle position");
+                }
+                lo[a] = std::min(lo[a], x), hi[a] = std::max(hi[a], x);
             }
-            lo[a] = std::min(lo[a], x), hi[a] = std::max(hi[a], x);
+        }
+        for (int a = 0; a < 3; ++a) {
+            const double cmin = std::floor(lo[a] / L.dx - 0.5), cmax = std::floor(hi[a] / L.dx - 0.5);
+            if (!(cmax - cmin < 4.0e8) || !(std::fabs(cmin) < 1.0e9) || !(std::fabs(cmax) < 1.0e9)) {
+                free_handle(h);
+                return fail("sv_create: domain too large for the dense block index");
+            }
+            clo[s][a] = (int64_t)cmin, chi[s][a] = (int64_t)cmax;
+            scenes[s].dmin[a] = (double)cs[s].domain_min[a] / (double)L.dx;
+            scenes[s].dmax[a] = (double)cs[s].domain_max[a] / (double)L.dx;
+            scenes[s].off[a] = 0;
+        }
+    }
+    if (batched) {
+        // slots of the largest scene extent plus 16 cells, in a near-square x-y grid
+        int64_t slot[2] = {0, 0};
+        for (uint32_t s = 0; s < n_scenes; ++s)
+            for (int a = 0; a < 2; ++a) slot[a] = std::max<int64_t>(slot[a], chi[s][a] - clo[s][a] + 1 + 16);
+        for (int a = 0; a < 2; ++a) slot[a] = (slot[a] + 3) / 4 * 4;
+        const uint32_t cols = (uint32_t)std::ceil(std::sqrt((double)n_scenes));
+        for (uint32_t s = 0; s < n_scenes; ++s) {
+            const int64_t ix = s % cols, iy = s / cols;
+            scenes[s].off[0] = (int32_t)(ix * slot[0] + 8 - clo[s][0]);
+            scenes[s].off[1] = (int32_t)(iy * slot[1] + 8 - clo[s][1]);
+            scenes[s].off[2] = 0;
         }
     }
     uint64_t total = 1;
     for (int a = 0; a < 3; ++a) {
-        double cmin = std::floor(lo[a] / L.dx - 0.5), cmax = std::floor(hi[a] / L.dx - 0.5);
-        if (!(cmax - cmin < 4.0e8)) {
+        int64_t cmin = INT64_MAX, cmax = INT64_MIN;
+        for (uint32_t s = 0; s < n_scenes; ++s) {
+            cmin = std::min<int64_t>(cmin, clo[s][a] + scenes[s].off[a]);
+            cmax = std::max<int64_t>(cmax, chi[s][a] + scenes[s].off[a]);
+        }
+        if (cmax - cmin >= (int64_t)4e8 || cmin < -(int64_t)1e9 || cmax > (int64_t)1e9) {
             free_handle(h);
             return fail("sv_create: domain too large for the dense block index");
         }
-        L.origin[a] = (int32_t)cmin - 4;
-        L.nb[a] = (int32_t)(((int64_t)cmax - L.origin[a]) >> 2) + 3;
+        L.origin[a] = (int32_t)(cmin - 8);
+        L.nb[a] = (int32_t)((cmax - L.origin[a]) >> 2) + 4;
         total *= (uint64_t)L.nb[a];
         if (total > (1ull << 26)) {
             free_handle(h);
@@ -356,11 +420,14 @@ int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) {
             (e = dalloc(h, &a.orig, n)))
             return cuda_fail(e, "particle buffers");
     }
-    if ((e = dalloc(h, &h->materials, mats.size())) || (e = dalloc(h, &h->keys, n)) ||
-        (e = dalloc(h, &h->sorted_keys, n)) || (e = dalloc(h, &h->perm, n)) || (e = dalloc(h, &h->seg_start, n + 1)) ||
-        (e = dalloc(h, &h->seg_block, n)) || (e = dalloc(h, &h->counters, C_COUNT)))
+    if ((e = dalloc(h, &h->materials, mats.size())) || (e = dalloc(h, &h->scenes, n_scenes)) ||
+        (e = dalloc(h, &h->keys, n)) || (e = dalloc(h, &h->sorted_keys, n)) || (e = dalloc(h, &h->perm, n)) ||
+        (e = dalloc(h, &h->seg_start, n + 1)) || (e = dalloc(h, &h->seg_block, n)) ||
+        (e = dalloc(h, &h->counters, C_COUNT)))
         return cuda_fail(e, "work buffers");
     h->n_materials = (uint32_t)mats.size();
+    h->host_materials = mats;
+    h->host_scenes = scenes;
     h->sort_temp_bytes = radix_sort_temp_bytes(n);
     uint64_t tiles = (n + 2047) / 2048 + 1;
     if ((e = dalloc(h, (char **)&h->sort_temp, h->sort_temp_bytes)) || (e = dalloc(h, &h->tile_counts, tiles)) ||
@@ -368,7 +435,7 @@ int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) {
         return cuda_fail(e, "sort buffers");
     if ((e = dalloc(h, &h->blockmap[0], total)) || (e = dalloc(h, &h->blockmap[1], total)))
         return cuda_fail(e, "block map");
-    uint64_t cap = c->block_capacity ? c->block_capacity : std::min<uint64_t>(total, std::max<uint64_t>(65536, n / 4));
+    uint64_t cap = c.block_capacity ? c.block_capacity : std::min<uint64_t>(total, std::max<uint64_t>(65536, n / 4));
     if ((e = alloc_grid(h, cap))) return cuda_fail(e, "grid");
     if ((e = cudaMallocHost((void **)&h->host_counters, C_COUNT * sizeof(uint32_t)))) return cuda_fail(e, "pinned");
 
@@ -378,33 +445,37 @@ int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) {
         std::vector<int4> cellv(cell ? n : 0);
         std::vector<float> C(9 * n), F(9 * n), en(n);
         std::vector<uint32_t> orig(n);
-        for (uint64_t i = 0; i < n; ++i) {
-            uint32_t packed = (p->flags[i] & FLAG_MASK) | (mat_index[i] << MATERIAL_SHIFT);
-            float x = p->positions[3 * i], y = p->positions[3 * i + 1], z = p->positions[3 * i + 2];
-            if (!cell) {
-                pos[i] = make_float4(x, y, z, 0.f);
-            } else {
-                double q[3] = {(double)x / L.dx, (double)y / L.dx, (double)z / L.dx};
-                int ci[3];
-                float o[3];
-                for (int a = 0; a < 3; ++a) {
-                    double f = std::floor(q[a]);
-                    ci[a] = (int)f;
-                    o[a] = (float)(q[a] - f);
-                    if (o[a] >= 1.f) o[a] = 0.f, ci[a] += 1;
+        for (uint32_t sc = 0; sc < n_scenes; ++sc) {
+            const sv_particles *p = &ps[sc];
+            for (uint64_t li = 0; li < p->n; ++li) {
+                const uint64_t i = first[sc] + li;
+                uint32_t packed = (p->flags[li] & FLAG_MASK) | (mat_index[i] << MATERIAL_SHIFT);
+                float x = p->positions[3 * li], y = p->positions[3 * li + 1], z = p->positions[3 * li + 2];
+                if (!cell) {
+                    pos[i] = make_float4(x, y, z, 0.f);
+                } else {
+                    double q[3] = {(double)x / L.dx, (double)y / L.dx, (double)z / L.dx};
+                    int ci[3];
+                    float o[3];
+                    for (int a = 0; a < 3; ++a) {
+                        double f = std::floor(q[a]);
+                        ci[a] = (int)f + scenes[sc].off[a];
+                        o[a] = (float)(q[a] - f);
+                        if (o[a] >= 1.f) o[a] = 0.f, ci[a] += 1;
+                    }
+                    pos[i] = make_float4(o[0], o[1], o[2], 0.f);
+                    cellv[i] = make_int4(ci[0], ci[1], ci[2], 0);
                 }
-                pos[i] = make_float4(o[0], o[1], o[2], 0.f);
-                cellv[i] = make_int4(ci[0], ci[1], ci[2], 0);
+                std::memcpy(&pos[i].w, &packed, 4);
+                vel[i] = make_float4(p->velocities[3 * li], p->velocities[3 * li + 1], p->velocities[3 * li + 2],
+                                     p->plastic_j ? p->plastic_j[li] : 1.f);
+                for (int k = 0; k < 9; ++k) {
+                    C[(uint64_t)k * n + i] = p->velocity_gradients[9 * li + k];
+                    F[(uint64_t)k * n + i] = p->position_gradients[9 * li + k];
+                }
+                en[i] = p->elastic_energies ? p->elastic_energies[li] : 0.f;
+                orig[i] = (uint32_t)i;
             }
-            std::memcpy(&pos[i].w, &packed, 4);
-            vel[i] = make_float4(p->velocities[3 * i], p->velocities[3 * i + 1], p->velocities[3 * i + 2],
-                                 p->plastic_j ? p->plastic_j[i] : 1.f);
-            for (int k = 0; k < 9; ++k) {
-                C[(uint64_t)k * n + i] = p->velocity_gradients[9 * i + k];
-                F[(uint64_t)k * n + i] = p->position_gradients[9 * i + k];
-            }
-            en[i] = p->elastic_energies ? p->elastic_energies[i] : 0.f;
-            orig[i] = (uint32_t)i;
         }
         ParticleArrays &a = h->side[0];
         if ((e = cudaMemcpy(a.pos, pos.data(), n * 16, cudaMemcpyHostToDevice)) ||
@@ -415,6 +486,7 @@ int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) {
             (e = cudaMemcpy(a.energy, en.data(), n * 4, cudaMemcpyHostToDevice)) ||
             (e = cudaMemcpy(a.orig, orig.data(), n * 4, cudaMemcpyHostToDevice)) ||
             (e = cudaMemcpy(h->materials, mats.data(), mats.size() * sizeof(Material), cudaMemcpyHostToDevice)) ||
+            (e = cudaMemcpy(h->scenes, scenes.data(), n_scenes * sizeof(SceneInfo), cudaMemcpyHostToDevice)) ||
             (e = cudaMemset(h->blockmap[0], 0xFF, total * 4)) || (e = cudaMemset(h->blockmap[1], 0xFF, total * 4)) ||
             (e = cudaMemset(h->counters, 0, C_COUNT * 4)))
             return cuda_fail(e, "upload");
@@ -424,6 +496,16 @@ int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) {
     *out = h;
     return 0;
 }
+
+}  // namespace
+
+int sv_create(const sv_consts *c, const sv_particles *p, sv_handle **out) { return create_impl(c, p, 1, false, out); }
+
+int sv_create_batched(const sv_consts *consts, const sv_particles *particles, uint32_t n_scenes, sv_handle **out) {
+    return create_impl(consts, particles, n_scenes, true, out);
+}
+
+uint32_t sv_scene_count(sv_handle *h) { return h ? (uint32_t)h->host_scenes.size() : 0u; }
 
 void sv_destroy(sv_handle *h) { free_handle(h); }
 
@@ -549,9 +631,12 @@ int sv_download(sv_handle *h, sv_particles *o) {
             if (!cell) {
                 o->positions[3 * i] = pos[s].x, o->positions[3 * i + 1] = pos[s].y, o->positions[3 * i + 2] = pos[s].z;
             } else {
-                o->positions[3 * i] = (float)(((double)cellv[s].x + pos[s].x) * dx);
-                o->positions[3 * i + 1] = (float)(((double)cellv[s].y + pos[s].y) * dx);
-                o->positions[3 * i + 2] = (float)(((double)cellv[s].z + pos[s].z) * dx);
+                // back to the scene's own coordinates
+                const uint32_t mi = packed >> MATERIAL_SHIFT;
+                const SceneInfo &sc = h->host_scenes[mi < h->host_materials.size() ? h->host_materials[mi].scene : 0];
+                o->positions[3 * i] = (float)(((double)(cellv[s].x - sc.off[0]) + pos[s].x) * dx);
+                o->positions[3 * i + 1] = (float)(((double)(cellv[s].y - sc.off[1]) + pos[s].y) * dx);
+                o->positions[3 * i + 2] = (float)(((double)(cellv[s].z - sc.off[2]) + pos[s].z) * dx);
             }
         }
         if (o->velocities) o->velocities[3 * i] = vel[s].x, o->velocities[3 * i + 1] = vel[s].y, o->velocities[3 * i + 2] = vel[s].z;
@@ -563,6 +648,32 @@ int sv_download(sv_handle *h, sv_particles *o) {
         if (o->elastic_energies) o->elastic_energies[i] = en[s];
         if (o->collider_bits) o->collider_bits[i] = h->collider_bits[i];
     }
+    return 0;
+}
+
+int sv_download_scene(sv_handle *h, uint32_t scene, sv_particles *o) {
+    g_last_error.clear();
+    if (!h || !o) return fail("sv_download_scene: NULL argument");
+    if (scene >= h->host_scenes.size()) return fail("sv_download_scene: no such scene");
+    const uint64_t b = h->scene_first[scene], m = h->scene_first[scene + 1] - b;
+    if (o->n != m) return fail("sv_download_scene: particle count mismatch");
+    const uint64_t n = h->n;
+    std::vector<uint32_t> flags(n), bits(n);
+    std::vector<float> x(3 * n), F(9 * n), v(3 * n), C(9 * n), en(n), pj(n);
+    sv_particles all{};
+    all.n = n;
+    all.flags = flags.data(), all.positions = x.data(), all.position_gradients = F.data();
+    all.velocities = v.data(), all.velocity_gradients = C.data(), all.elastic_energies = en.data();
+    all.collider_bits = bits.data(), all.plastic_j = pj.data();
+    if (sv_download(h, &all) < 0) return -1;
+    if (o->flags) std::memcpy(o->flags, flags.data() + b, m * 4);
+    if (o->positions) std::memcpy(o->positions, x.data() + 3 * b, m * 12);
+    if (o->position_gradients) std::memcpy(o->position_gradients, F.data() + 9 * b, m * 36);
+    if (o->velocities) std::memcpy(o->velocities, v.data() + 3 * b, m * 12);
+    if (o->velocity_gradients) std::memcpy(o->velocity_gradients, C.data() + 9 * b, m * 36);
+    if (o->elastic_energies) std::memcpy(o->elastic_energies, en.data() + b, m * 4);
+    if (o->collider_bits) std::memcpy(o->collider_bits, bits.data() + b, m * 4);
+    if (o->plastic_j) std::memcpy(o->plastic_j, pj.data() + b, m * 4);
     return 0;
 }
 

@@ -84,6 +84,12 @@ struct sv_handle {
     sv::ParticleArrays side[2] = {};
     sv::Material *materials = nullptr;
     uint32_t n_materials = 0;
+    std::vector<sv::Material> host_materials;
+    // independent scenes sharing the handle (one unless created batched)
+    sv::SceneInfo *scenes = nullptr;
+    std::vector<sv::SceneInfo> host_scenes;
+    std::vector<uint64_t> scene_first;  // first particle of each scene (+ total at the end)
+    bool batched = false;
 
     uint32_t *keys = nullptr;         // [n] binning keys in device order (valid when keys_valid)
     bool keys_valid = false;

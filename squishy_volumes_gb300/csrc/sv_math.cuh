@@ -249,8 +249,19 @@ struct Material {
     float visc_dynamic, visc_bulk;  // USE_VISCOSITY (0, 0 otherwise)
     float xi, theta_c, theta_s;     // snow
     uint32_t use_viscosity;
-    uint32_t pad[2];
+    uint32_t scene;  // index into the handle's scene table
+    uint32_t pad;
 };
+
+// One independent scene of a handle: its particles are translated by `off`
+// whole cells in the shared block index, and culled against its own domain
+// (cell units, scene-local).
+struct SceneInfo {
+    double dmin[3], dmax[3];
+    int32_t off[3];
+    uint32_t pad;
+};
+static_assert(sizeof(SceneInfo) == 64, "SceneInfo is 64 bytes");
 static_assert(sizeof(Material) == 64, "Material is 64 bytes");
 
 __device__ __forceinline__ float powi_f(float x, int n) {

@@ -57,6 +57,7 @@ enum Mode { MODE_P2G = 0, MODE_G2P2G = 1 };
 struct StepArgs {
     ParticleArrays in, out;
     const Material *mats;
+    const SceneInfo *scenes;
     uint32_t *counters;
     const uint32_t *perm;  // nullptr: identity
     const uint32_t *seg_start;
@@ -784,9 +785,12 @@ template <bool CELL, int MODE> __global__ void __launch_bounds__(PT, 5) k_partic
                             inside = pos.x > A.L.domain_min[0] && pos.x < A.L.domain_max[0] && pos.y > A.L.domain_min[1] &&
                                      pos.y < A.L.domain_max[1] && pos.z > A.L.domain_min[2] && pos.z < A.L.domain_max[2];
                         } else {
-                            const double q[3] = {(double)cell.x + pos.x, (double)cell.y + pos.y, (double)cell.z + pos.z};
-                            inside = q[0] > A.L.dmin_cells[0] && q[0] < A.L.dmax_cells[0] && q[1] > A.L.dmin_cells[1] &&
-                                     q[1] < A.L.dmax_cells[1] && q[2] > A.L.dmin_cells[2] && q[2] < A.L.dmax_cells[2];
+                            // scene-local cell coordinates against the scene's domain
+                            const SceneInfo &sc = A.scenes[mat.scene];
+                            const double q[3] = {(double)(cell.x - sc.off[0]) + pos.x, (double)(cell.y - sc.off[1]) + pos.y,
+                                                 (double)(cell.z - sc.off[2]) + pos.z};
+                            inside = q[0] > sc.dmin[0] && q[0] < sc.dmax[0] && q[1] > sc.dmin[1] && q[1] < sc.dmax[1] &&
+                                     q[2] > sc.dmin[2] && q[2] < sc.dmax[2];
                         }
                         if (!inside) packed |= SV_TOMBSTONED;
                         alive = !(packed & (SV_TOMBSTONED | SV_FAILED));
@@ -879,6 +883,7 @@ StepArgs make_args(sv_handle *h, float dt, float3 g) {
     A.in = h->side[h->cur];
     A.out = h->side[h->cur ^ 1];
     A.mats = h->materials;
+    A.scenes = h->scenes;
     A.counters = h->counters;
     A.perm = h->perm;
     A.seg_start = h->seg_start;

@@ -213,9 +213,41 @@ def small_mixed(n_per_material: int = 300, seed: int = 5, dx: float = 0.05, defo
     return Scene("small_mixed", IoState(0.0, p), consts, Extras(), dt=1e-4, substeps=10)
 
 
+
+
+
+def batched_64(seed: int = 4, n_scenes: int = 64, median: float = 8e4, sigma: float = 1.0,
+               lo: int = 10_000, hi: int = 500_000):
+    """Batched form: independent scenes, each a seeded jittered box of one
+    material drawn from {fixed-corotated elastic, snow, sand} on its own
+    256^3 grid over the unit cube (dx = 1/256).  Particle counts are
+    lognormal, clipped to [10k, 500k]; E ~ U[5e4, 5e5], nu ~ U[0.2, 0.4],
+    friction angle ~ U[25, 40] deg; dt = 5e-5, 300 substeps, sticky ground."""
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / 256
+    counts = np.clip(np.exp(rng.normal(math.log(median), sigma, n_scenes)), lo, hi).astype(np.int64)
+    scenes_out = []
+    for s, cnt in enumerate(counts):
+        kind = ["fixed_corotated", "snow", "sand"][int(rng.integers(0, 3))]
+        E, nu = float(rng.uniform(5e4, 5e5)), float(rng.uniform(0.2, 0.4))
+        phi = float(rng.uniform(25.0, 40.0))
+        mat = Material(kind, youngs_modulus=E, poissons_ratio=nu, friction_angle_deg=phi)
+        side = max(2, int(round(cnt ** (1 / 3))))
+        dims = (side, side, max(2, int(round(cnt / side / side))))
+        lo_c = rng.integers(20, 256 - 20 - dims[0] // 2, 2)
+        pos = jittered_box(rng, (lo_c[0] * dx, lo_c[1] * dx, 30 * dx), dims, dx / 2)
+        p = build_particles([(pos, mat, rng.uniform(-0.5, 0.5, 3), dx / 2)])
+        consts = InputConsts(grid_node_size=dx, domain_min=(0.0, 0.0, 0.0), domain_max=(1.0, 1.0, 1.0))
+        extras = Extras(ground_mode=1, ground_axis=2, ground_height=8 * dx, position_form=1)
+        scenes_out.append(Scene(f"batched_{s}", IoState(0.0, p), consts, extras, dt=5e-5, substeps=300,
+                                meta={"material": kind, "E": E, "nu": nu, "friction_deg": phi}))
+    return scenes_out
+
+
 SCENES = {
     "cube_64k": cube_64k,
     "three_boxes_1m": three_boxes_1m,
     "dam_break_8m": dam_break_8m,
     "small_mixed": small_mixed,
+    "batched_64": batched_64,
 }

@@ -243,10 +243,8 @@ class CudaState:
         self._template = template
 
     # -- from_io_state (cpu_state.rs:25-66)
-    @classmethod
-    def from_io_state(cls, io_state: IoState, consts: InputConsts, extras: Optional[Extras] = None) -> "CudaState":
-        extras = extras or Extras()
-        lib = _abi.load()
+    @staticmethod
+    def _consts(consts: InputConsts, extras: Extras) -> SvConsts:
         c = SvConsts()
         c.grid_node_size = consts.scaled_grid_node_size()
         for a in range(3):
@@ -259,11 +257,17 @@ class CudaState:
         c.svd_fp64_policy = extras.svd_fp64_policy
         c.block_capacity = extras.block_capacity
         c.sort_interval = extras.sort_interval
+        return c
+
+    @classmethod
+    def from_io_state(cls, io_state: IoState, consts: InputConsts, extras: Optional[Extras] = None) -> "CudaState":
+        extras = extras or Extras()
+        lib = _abi.load()
+        c = cls._consts(consts, extras)
         p = io_state.particles
         s = p.to_struct()
         h = ct.c_void_p()
         check(lib.sv_create(ct.byref(c), ct.byref(s), ct.byref(h)))
-        template = p.subset(slice(0, 0))
         return cls(h, p.n, io_state.time, consts, extras, p.initial_positions, p)
 
     def close(self):
@@ -409,3 +413,62 @@ def sort_pairs(keys: np.ndarray) -> np.ndarray:
     perm = np.zeros(keys.shape[0], np.uint32)
     check(_abi.load().sv_sort_pairs(ptr(keys, u32p), ptr(perm, u32p), keys.shape[0]))
     return perm
+
+
+class BatchedCudaState(CudaState):
+    """Many independent scenes in one handle (sv_create_batched): one set of
+    launches advances them all.  Not in the reference, whose backend holds
+    one scene; each scene keeps its own domain and cull bounds."""
+
+    def __init__(self, handle, counts, consts_list, extras, particles_list):
+        total = sum(counts)
+        merged = _concat([p for p in particles_list])
+        super().__init__(handle, total, 0.0, consts_list[0], extras, merged.initial_positions, merged)
+        self.counts = list(counts)
+        self.first = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        self.consts_list = list(consts_list)
+        self._templates = list(particles_list)
+
+    @classmethod
+    def from_scenes(cls, io_states, consts_list, extras: Optional[Extras] = None) -> "BatchedCudaState":
+        extras = extras or Extras()
+        lib = _abi.load()
+        k = len(io_states)
+        cs = (SvConsts * k)(*[cls._consts(c, extras) for c in consts_list])
+        keep = [s.particles for s in io_states]
+        ps = (SvParticles * k)(*[p.to_struct() for p in keep])
+        h = ct.c_void_p()
+        check(lib.sv_create_batched(cs, ps, k, ct.byref(h)))
+        return cls(h, [p.n for p in keep], consts_list, extras, keep)
+
+    def scene_count(self) -> int:
+        return int(self._lib.sv_scene_count(self._h))
+
+    def download_scene(self, scene: int) -> Particles:
+        t = self._templates[scene]
+        m = t.n
+        out = Particles(
+            flags=np.zeros(m, np.uint32), positions=np.zeros((m, 3), np.float32),
+            position_gradients=np.zeros((m, 9), np.float32), velocities=np.zeros((m, 3), np.float32),
+            velocity_gradients=np.zeros((m, 9), np.float32), mass=t.mass, initial_volume=t.initial_volume,
+            mu=t.mu, lambda_=t.lambda_, sand_alpha=t.sand_alpha, exponent=t.exponent, bulk_modulus=t.bulk_modulus,
+            viscosity_dynamic=t.viscosity_dynamic, viscosity_bulk=t.viscosity_bulk,
+            elastic_energies=np.zeros(m, np.float32), collider_bits=np.zeros(m, np.uint32),
+            initial_positions=t.initial_positions, model=t.model, hardening=t.hardening,
+            crit_compression=t.crit_compression, crit_stretch=t.crit_stretch, plastic_j=np.ones(m, np.float32))
+        s = out.to_struct()
+        check(self._lib.sv_download_scene(self._h, int(scene), ct.byref(s)))
+        return out
+
+
+def _concat(parts):
+    from dataclasses import fields as _fields
+
+    out = {}
+    for f in _fields(Particles):
+        vals = [getattr(p, f.name) for p in parts]
+        if any(v is None for v in vals):
+            out[f.name] = None if all(v is None for v in vals) else None
+        else:
+            out[f.name] = np.concatenate(vals) if vals else None
+    return Particles(**out)

@@ -1,0 +1,78 @@
+"""Full-size GPU checks (the 8M-particle precision-form dam break) through
+the C ABI, by properties that do not need a CPU run of the whole scene:
+mass and momentum conservation through P2G, agreement of the int32-cell +
+fp32-offset position form with the fp32 form, and no particle lost."""
+
+import numpy as np
+import pytest
+
+from squishy_volumes_gb300 import CudaState, Extras, scenes
+from squishy_volumes_gb300._abi import SV_TOMBSTONED
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dam_break():
+    return scenes.dam_break_8m()
+
+
+def test_dam_break_8m_p2g_conserves_mass_and_momentum(cuda_lib, dam_break):
+    s = dam_break
+    p = s.io_state.particles
+    gpu = CudaState.from_io_state(s.io_state, s.consts, s.extras)
+    g = gpu.p2g_only(s.dt, s.gravity)
+    gpu.close()
+    total = p.mass.sum(dtype=np.float64)
+    np.testing.assert_allclose(g.masses.sum(dtype=np.float64), total, rtol=1e-6)
+    # at rest: the grid momentum is the gravity impulse of one substep
+    grid_mom = (g.masses[:, None].astype(np.float64) * g.velocities).sum(0)
+    exp = total * s.dt * np.asarray(s.gravity, np.float64)
+    assert np.all(np.abs(grid_mom - exp) <= 1e-5 * np.abs(exp).max() + 1e-12)
+
+
+def test_dam_break_8m_both_position_forms_run(cuda_lib, dam_break):
+    s = dam_break
+    n = 5
+    a = CudaState.from_io_state(s.io_state, s.consts, Extras(**{**s.extras.__dict__, "position_form": 1}))
+    b = CudaState.from_io_state(s.io_state, s.consts, Extras(**{**s.extras.__dict__, "position_form": 0}))
+    assert a.step(n, s.dt, s.gravity) == (0, n)
+    assert b.step(n, s.dt, s.gravity) == (0, n)
+    ra, rb = a.download(), b.download()
+    a.close(), b.close()
+    np.testing.assert_array_equal(ra.flags, rb.flags)
+    assert not (ra.flags & SV_TOMBSTONED).any()  # nothing leaves the domain in 5 substeps
+    x, y = ra.positions.astype(np.float64), rb.positions.astype(np.float64)
+    assert np.linalg.norm(x - y) <= 1e-6 * np.linalg.norm(y)
+
+
+def test_cell_form_is_closer_to_fp64_on_a_fine_grid(cuda_lib, oracle_mod):
+    """At dx = 1/512 the fp32 position ulp (6e-8 m at 0.5 m) exceeds the
+    per-substep displacement (v dt ~ 2e-8 m), so the fp32 form rounds motion
+    away; the int32-cell + fp32-offset form keeps it.  Against the fp64
+    oracle, the cell form must be the closer of the two, and its velocity
+    error no larger than that of the fp32 restatement of the reference
+    itself: the stiff fluid (K = 1e5, exponent 7) turns the ~1e-7 fp32 noise
+    of J after the volumetric reset into pressure noise, so fp32 velocities
+    of any implementation sit ~1e-2 from fp64 after a few substeps."""
+    s = scenes.dam_break_8m(fluid_dims=(40, 40, 20), box_dims=(10, 10, 10))
+    n = 5
+    ref = oracle_mod.OracleState(s.io_state.particles, s.consts, s.extras, fp64=True)
+    assert ref.step(n, s.dt, s.gravity) == 0
+    exp = ref.download()
+    ref32 = oracle_mod.OracleState(s.io_state.particles, s.consts, s.extras, fp64=False)
+    assert ref32.step(n, s.dt, s.gravity) == 0
+    o32 = ref32.download()
+    oracle32_v = np.linalg.norm(o32.velocities.astype(np.float64) - exp.velocities) / np.linalg.norm(exp.velocities)
+    errs = {}
+    for form in (0, 1):
+        g = CudaState.from_io_state(s.io_state, s.consts, Extras(**{**s.extras.__dict__, "position_form": form}))
+        assert g.step(n, s.dt, s.gravity) == (0, n)
+        out = g.download()
+        g.close()
+        np.testing.assert_array_equal(out.flags, exp.flags)
+        errs[form] = {k: np.linalg.norm(getattr(out, k).astype(np.float64) - getattr(exp, k))
+                      / np.linalg.norm(getattr(exp, k)) for k in ("positions", "velocities")}
+    assert errs[1]["velocities"] <= errs[0]["velocities"] * 1.001, errs
+    assert errs[1]["velocities"] <= 2.0 * oracle32_v + 1e-6, (errs, oracle32_v)
+    assert errs[1]["positions"] <= errs[0]["positions"] * 1.01 + 1e-12, errs
