@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--scene", default="three_boxes_1m")
     ap.add_argument("--sort-interval", type=int, default=0,
                     help="substeps between binning sorts (0 adaptive, 1 every substep like the reference)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="time binning interval x CTAs/SM candidates first and keep the fastest (sv_autotune)")
+    ap.add_argument("--no-graphs", action="store_true", help="launch every kernel directly (no CUDA graphs)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bound on the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -239,6 +242,14 @@ def run_ours(args, rank, world, local):
         h2d_particles = [scene.io_state.particles]
     p = scene.io_state.particles
     gpu = make_gpu()
+    # All work, warm-up included, is queued on a torch stream handed to the
+    # library (the CUDA graphs of the binning periods are captured on it).
+    stream = torch.cuda.Stream(device=dev)
+    gpu.set_stream(stream.cuda_stream)
+    tuned = None
+    if args.autotune:
+        tuned = gpu.autotune(scene.dt, scene.gravity, 16)
+    gpu.set_graphs(not args.no_graphs)
     # warm-up
     status, done = gpu.step(args.warmup, scene.dt, scene.gravity)
     if status:
@@ -252,10 +263,8 @@ def run_ours(args, rank, world, local):
 
             dist.barrier()
 
-    # timed region: K substeps queued on a torch stream handed to the
-    # library, bracketed by CUDA events recorded on that same stream
-    stream = torch.cuda.Stream(device=dev)
-    gpu.set_stream(stream.cuda_stream)
+    # timed region: K substeps bracketed by CUDA events recorded on the
+    # library's stream
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
@@ -382,6 +391,9 @@ def run_ours(args, rank, world, local):
             "grid_blocks": st["grid_blocks"],
             "binning_sort_interval": st["sort_interval"],
             "binning_sorts_in_timed_region": int(stats1["sorts"] - stats0["sorts"]),
+            "graph_replays_in_timed_region": int(stats1["graph_replays"] - stats0["graph_replays"]),
+            "cta_per_sm": st["cta_per_sm"],
+            "autotuned": tuned,
             "substep_dt": scene.dt,
             "l2": "state larger than L2 (no flush)",
             "parallelism": "replicas" if world > 1 else "single GPU",

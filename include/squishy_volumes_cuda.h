@@ -222,8 +222,22 @@ typedef struct sv_stats {
     uint64_t sorts;             /* binning sorts run so far */
     uint64_t sort_interval;     /* current substeps between binning sorts */
     uint64_t tile_misses;       /* gathers that missed their block's shared tile (low 32 bits) */
+    uint64_t graph_replays;     /* binning periods run as CUDA graph replays */
+    uint64_t cta_per_sm;        /* CTAs per SM of the particle kernels */
 } sv_stats;
+
+/* Whether sv_step runs whole binning periods as CUDA graphs (default on;
+ * off, and while profiling, every kernel is launched directly). */
+int sv_set_graphs(sv_handle *h, int enable);
 int sv_get_stats(sv_handle *h, sv_stats *out);
+
+/* Addition: picks the substeps between binning sorts and the CTAs per SM of
+ * the particle kernels by timing `substeps_per_trial` substeps of each
+ * candidate from a snapshot of the current state; the state is restored
+ * afterwards and the fastest configuration is kept for later sv_step calls.
+ * The chosen values are written to the out pointers when not NULL. */
+int sv_autotune(sv_handle *h, float dt, const float gravity[3], uint32_t substeps_per_trial,
+                uint32_t *sort_interval_out, uint32_t *cta_per_sm_out);
 
 /* Runs the handle's work on a caller-owned CUDA stream (a cudaStream_t passed
  * as void*; NULL returns to the handle's own stream).  The previous stream is

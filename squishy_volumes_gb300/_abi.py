@@ -90,6 +90,8 @@ class SvStats(ct.Structure):
         ("sorts", ct.c_uint64),
         ("sort_interval", ct.c_uint64),
         ("tile_misses", ct.c_uint64),
+        ("graph_replays", ct.c_uint64),
+        ("cta_per_sm", ct.c_uint64),
     ]
 
 
@@ -113,6 +115,8 @@ _SIGNATURES = {
     "sv_sort_pairs": (ct.c_int, [u32p, u32p, ct.c_uint64]),
     "sv_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(SvStats)]),
     "sv_set_stream": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "sv_set_graphs": (ct.c_int, [ct.c_void_p, ct.c_int]),
+    "sv_autotune": (ct.c_int, [ct.c_void_p, ct.c_float, f32p, ct.c_uint32, u32p, u32p]),
     "sv_set_profiling": (ct.c_int, [ct.c_void_p, ct.c_int]),
     "sv_profile_report": (ct.c_int, [ct.c_void_p, ct.c_char_p, ct.c_uint64]),
 }

@@ -55,6 +55,8 @@ void free_handle(sv_handle *h) {
     if (h->host_counters) cudaFreeHost(h->host_counters);
     for (auto &p : h->timer.pending) cudaEventDestroy(p.second.first), cudaEventDestroy(p.second.second);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    for (auto &kv : h->graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
 }
@@ -206,6 +208,74 @@ int fused_substep(sv_handle *h, float dt, float3 g) {
     SV_CUDA(launch_g2p2g(h, dt, g, write_keys, h->need_perm));
     h->need_perm = false;
     h->since_sort += 1;
+    return 0;
+}
+
+void clear_graphs(sv_handle *h) {
+    for (auto &kv : h->graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    h->graphs.clear();
+}
+
+// One binning period (the binning substep and the substeps up to the next
+// binning) as a CUDA graph: captured the first time a given launch
+// configuration occurs, replayed afterwards.  Every launch of a period reads
+// its counts from device memory, so the captured launches stay valid; only
+// the pointers and the host-side bookkeeping differ between configurations,
+// and those are in the key and the saved state.
+int run_period_graph(sv_handle *h, float dt, float3 g) {
+    sv_handle::GraphKey key{h->cur, h->gcur, h->map_cur, h->sort_interval, dt, {g.x, g.y, g.z}};
+    auto it = h->graphs.find(key);
+    if (it == h->graphs.end()) {
+        // host bookkeeping before the period, put back if the capture fails
+        const int cur0 = h->cur, gcur0 = h->gcur, map_cur0 = h->map_cur, map_next0 = h->map_next;
+        const int vel_side0 = h->vel_side, vel_map0 = h->vel_map;
+        const bool keys_valid0 = h->keys_valid, need_perm0 = h->need_perm;
+        const uint32_t since0 = h->since_sort;
+        const uint64_t l0 = h->launches, sorts0 = h->sorts;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            int rc = 0;
+            for (uint32_t s = 0; s < key.period && rc == 0; ++s) rc = fused_substep(h, dt, g);
+            e = cudaStreamEndCapture(h->stream, &graph);
+            if (rc && e == cudaSuccess) e = cudaErrorStreamCaptureInvalidated;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+        }
+        if (e != cudaSuccess) {
+            // The stream cannot be captured (e.g. the legacy default stream):
+            // run the period launch by launch from now on.
+            (void)cudaGetLastError();
+            g_last_error.clear();
+            h->cur = cur0, h->gcur = gcur0, h->map_cur = map_cur0, h->map_next = map_next0;
+            h->vel_side = vel_side0, h->vel_map = vel_map0;
+            h->keys_valid = keys_valid0, h->need_perm = need_perm0, h->since_sort = since0;
+            h->launches = l0, h->sorts = sorts0;
+            h->use_graphs = false;
+            for (uint32_t s = 0; s < key.period; ++s)
+                if (fused_substep(h, dt, g)) return -1;
+            return 0;
+        }
+        sv_handle::GraphState st;
+        st.exec = exec;
+        st.cur = h->cur, st.gcur = h->gcur, st.map_cur = h->map_cur, st.map_next = h->map_next;
+        st.vel_side = h->vel_side, st.vel_map = h->vel_map;
+        st.keys_valid = h->keys_valid, st.need_perm = h->need_perm, st.since_sort = h->since_sort;
+        st.launches = h->launches - l0;
+        it = h->graphs.emplace(key, st).first;
+        h->launches = l0;
+        h->sorts -= 1;  // counted again below, like a replay
+    }
+    const sv_handle::GraphState &st = it->second;
+    SV_CUDA(cudaGraphLaunch(st.exec, h->stream));
+    h->cur = st.cur, h->gcur = st.gcur, h->map_cur = st.map_cur, h->map_next = st.map_next;
+    h->vel_side = st.vel_side, h->vel_map = st.vel_map;
+    h->keys_valid = st.keys_valid, h->need_perm = st.need_perm, h->since_sort = st.since_sort;
+    h->launches += st.launches;
+    h->sorts += 1;
+    h->graph_launches += 1;
     return 0;
 }
 
@@ -541,8 +611,18 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
         }
         const uint32_t todo = std::min(chunk, n_substeps - done);
         if (!h->pending_valid && standalone_p2g(h, dt, g)) return -1;
-        for (uint32_t s = 0; s < todo; ++s)
-            if (fused_substep(h, dt, g)) return -1;
+        for (uint32_t s = 0; s < todo;) {
+            // whole binning periods go through CUDA graphs once the binning
+            // keys come from the previous substep (steady state)
+            if (h->use_graphs && !h->profiling && h->since_sort >= h->sort_interval && h->keys_valid &&
+                todo - s >= h->sort_interval) {
+                if (run_period_graph(h, dt, g)) return -1;
+                s += h->sort_interval;
+            } else {
+                if (fused_substep(h, dt, g)) return -1;
+                s += 1;
+            }
+        }
         if (read_counters(h)) return -1;
         const uint32_t st = h->host_counters[C_STATUS];
         done = h->host_counters[C_SUBSTEPS] - base;
@@ -554,6 +634,7 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
                 const uint64_t cap = std::min<uint64_t>(h->layout.total_blocks, h->capacity * 2);
                 if (cap <= h->capacity) return fail("sv_step: grid block capacity exhausted");
                 SV_CUDA(alloc_grid(h, cap));
+                clear_graphs(h);  // they bake the old grid pointers
             }
             // A particle left the blocks claimed at the last binning: its
             // scatter is incomplete, so bin again and redo the scatter.
@@ -782,6 +863,95 @@ int sv_get_stats(sv_handle *h, sv_stats *out) {
     out->sorts = h->sorts;
     out->sort_interval = h->sort_interval;
     out->tile_misses = h->host_counters[C_FALLBACK];
+    out->graph_replays = h->graph_launches;
+    out->cta_per_sm = h->cta_per_sm;
+    return 0;
+}
+
+int sv_autotune(sv_handle *h, float dt, const float gravity[3], uint32_t substeps_per_trial, uint32_t *sort_interval_out,
+                uint32_t *cta_per_sm_out) {
+    g_last_error.clear();
+    if (!h) return fail("sv_autotune: NULL handle");
+    if (!(dt > 0.f)) return fail("sv_autotune: dt must be positive");
+    if (substeps_per_trial == 0) substeps_per_trial = 16;
+    // snapshot of the current particle side (trials advance it)
+    ParticleArrays &a = h->side[h->cur];
+    const uint64_t n = h->n;
+    const bool cell = h->layout.position_form == 1;
+    struct Span {
+        void *dev;
+        size_t bytes;
+        void *copy;
+    };
+    std::vector<Span> spans = {{a.pos, n * 16, nullptr}, {a.vel, n * 16, nullptr}, {a.C, n * 36, nullptr},
+                               {a.F, n * 36, nullptr},   {a.energy, n * 4, nullptr}, {a.orig, n * 4, nullptr}};
+    if (cell) spans.push_back({a.cell, n * 16, nullptr});
+    auto release = [&]() {
+        for (auto &s : spans) cudaFree(s.copy);
+    };
+    SV_CUDA(cudaStreamSynchronize(h->stream));
+    for (auto &s : spans) {
+        cudaError_t e = cudaMalloc(&s.copy, s.bytes ? s.bytes : 16);
+        if (e != cudaSuccess) {
+            release();
+            return fail(std::string("sv_autotune: ") + cudaGetErrorString(e));
+        }
+        cudaMemcpy(s.copy, s.dev, s.bytes, cudaMemcpyDeviceToDevice);
+    }
+    const int cur0 = h->cur;
+    const uint64_t substeps0 = h->substeps_total, fp64_0 = h->fp64_total;
+    auto restore = [&]() {
+        cudaStreamSynchronize(h->stream);
+        h->cur = cur0;
+        ParticleArrays &b = h->side[h->cur];
+        void *dst[] = {b.pos, b.vel, b.C, b.F, b.energy, b.orig, b.cell};
+        for (size_t i = 0; i < spans.size(); ++i) cudaMemcpy(dst[i], spans[i].copy, spans[i].bytes, cudaMemcpyDeviceToDevice);
+        h->pending_valid = false;
+        h->keys_valid = false;
+        h->since_sort = 0;
+        uint32_t zero = 0;
+        cudaMemcpy(h->counters + C_STATUS, &zero, 4, cudaMemcpyHostToDevice);
+    };
+    uint32_t best_si = h->sort_interval, best_cta = h->cta_per_sm;
+    double best_ms = 1e300;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0), cudaEventCreate(&e1);
+    h->adaptive_interval = false;
+    for (uint32_t si : {1u, 2u, 4u, 8u, 16u}) {
+        for (uint32_t cta : {8u, 16u, 32u, 64u, 128u}) {
+            restore();
+            clear_graphs(h);
+            h->sort_interval = h->max_interval = si;
+            h->cta_per_sm = cta;
+            uint32_t st = 0, done = 0;
+            // warm-up covers the first scatter and one graph capture
+            if (sv_step(h, 2 * si + 2, dt, gravity, nullptr, &st, &done) < 0 || st) continue;
+            cudaEventRecord(e0, h->stream);
+            if (sv_step(h, substeps_per_trial, dt, gravity, nullptr, &st, &done) < 0 || st) continue;
+            cudaEventRecord(e1, h->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best_ms) best_ms = ms, best_si = si, best_cta = cta;
+        }
+    }
+    cudaEventDestroy(e0), cudaEventDestroy(e1);
+    restore();
+    release();
+    clear_graphs(h);
+    h->adaptive_interval = false;  // the tuned interval is kept fixed
+    h->sort_interval = h->max_interval = best_si;
+    h->cta_per_sm = best_cta;
+    h->substeps_total = substeps0, h->fp64_total = fp64_0;
+    if (sort_interval_out) *sort_interval_out = best_si;
+    if (cta_per_sm_out) *cta_per_sm_out = best_cta;
+    g_last_error.clear();
+    return 0;
+}
+
+int sv_set_graphs(sv_handle *h, int enable) {
+    if (!h) return fail("sv_set_graphs: NULL handle");
+    h->use_graphs = enable != 0;
     return 0;
 }
 
@@ -789,6 +959,7 @@ int sv_set_stream(sv_handle *h, void *stream) {
     if (!h) return fail("sv_set_stream: NULL handle");
     SV_CUDA(cudaStreamSynchronize(h->stream));
     h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+    clear_graphs(h);
     return 0;
 }
 

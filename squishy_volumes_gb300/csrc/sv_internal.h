@@ -6,6 +6,7 @@
 
 #include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/squishy_volumes_cuda.h"
@@ -141,6 +142,33 @@ struct sv_handle {
 
     bool profiling = false;
     sv::KernelTimer timer;
+
+    // CTAs per SM of the particle kernels' grid (tuned by sv_autotune).  Five
+    // are resident per SM; the rest wait in the hardware block scheduler,
+    // which balances segments of uneven size better than a fixed stride.
+    uint32_t cta_per_sm = 32;
+
+    // CUDA graphs of one binning period (a binning substep and the substeps
+    // up to the next binning), keyed by everything their launches bake in.
+    struct GraphKey {
+        int cur, gcur, map_cur;
+        uint32_t period;
+        float dt, g[3];
+        bool operator<(const GraphKey &o) const {
+            return std::tie(cur, gcur, map_cur, period, dt, g[0], g[1], g[2]) <
+                   std::tie(o.cur, o.gcur, o.map_cur, o.period, o.dt, o.g[0], o.g[1], o.g[2]);
+        }
+    };
+    struct GraphState {  // host-side state after the period
+        cudaGraphExec_t exec = nullptr;
+        int cur, gcur, map_cur, map_next, vel_side, vel_map;
+        bool keys_valid, need_perm;
+        uint32_t since_sort;
+        uint64_t launches;
+    };
+    std::map<GraphKey, GraphState> graphs;
+    bool use_graphs = true;
+    uint64_t graph_launches = 0;  // graph replays issued
 };
 
 namespace sv {

@@ -154,7 +154,13 @@ __device__ __forceinline__ void svd3(const Mat3<T> &F, Mat3<T> &U, T S[3], Mat3<
 // the optimal one still reduces the off-diagonal, and c^2 + s^2 = 1 keeps V
 // orthogonal), and sweeps stop once every pair is orthogonal to 1e-6
 // relative -- below fp32 resolution of the products formed from the result.
+// A pair already orthogonal to fp32 epsilon is left alone (the reference
+// test of one-sided Jacobi): near-identity F then gives U = V = I up to
+// rounding instead of the arbitrary 45-degree rotations of a degenerate
+// pair, whose fp32 rounding would put ~1e-7 noise into U V^T -- the fluid
+// and sand returns rebuild F from U V^T every substep.
 __device__ __forceinline__ void svd3_fast(const m3f &F, m3f &U, float S[3], m3f &V) {
+    constexpr float EPS2 = 1.4210855e-14f;  // FLT_EPSILON^2
     float A[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) A[i] = F.a[i];
@@ -170,7 +176,7 @@ __device__ __forceinline__ void svd3_fast(const m3f &F, m3f &U, float S[3], m3f 
             const float g = A[p * 3] * A[q * 3] + A[p * 3 + 1] * A[q * 3 + 1] + A[p * 3 + 2] * A[q * 3 + 2];
             const float np = nrm[p], nq = nrm[q];
             off = fmaxf(off, __fdividef(g * g, fmaxf(np * nq, 1e-30f)));
-            if (g != 0.f) {
+            if (g * g > EPS2 * np * nq) {
                 const float d = nq - np, e = 2.f * g;
                 const float r2 = d * d + e * e;
                 const float r = r2 * rsqrtf(r2);
@@ -196,8 +202,9 @@ __device__ __forceinline__ void svd3_fast(const m3f &F, m3f &U, float S[3], m3f 
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const float n2 = A[c * 3] * A[c * 3] + A[c * 3 + 1] * A[c * 3 + 1] + A[c * 3 + 2] * A[c * 3 + 2];
-        const float inv = n2 > 1e-30f ? rsqrtf(n2) : 0.f;
-        S[c] = n2 * inv;
+        // correctly rounded, so that a unit column stays exactly unit
+        S[c] = sqrtf(n2);
+        const float inv = n2 > 1e-30f ? __frcp_rn(S[c]) : 0.f;
         good[c] = n2 > 1e-30f;
         U.a[c * 3] = A[c * 3] * inv, U.a[c * 3 + 1] = A[c * 3 + 1] * inv, U.a[c * 3 + 2] = A[c * 3 + 2] * inv;
     }

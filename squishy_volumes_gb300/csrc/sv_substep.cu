@@ -900,7 +900,7 @@ StepArgs make_args(sv_handle *h, float dt, float3 g) {
     return A;
 }
 
-unsigned particle_blocks() { return (unsigned)sm_count() * 8; }
+unsigned particle_blocks(const sv_handle *h) { return (unsigned)sm_count() * (h->cta_per_sm ? h->cta_per_sm : 8); }
 
 }  // namespace
 
@@ -976,8 +976,8 @@ cudaError_t launch_p2g(sv_handle *h, float dt, float3 g) {
     A.grid_next = h->grid[h->gcur];
     A.keys_out = nullptr;
     Scoped s(h, "p2g");
-    if (h->layout.position_form) k_particles<true, MODE_P2G><<<particle_blocks(), PT, 0, h->stream>>>(A);
-    else k_particles<false, MODE_P2G><<<particle_blocks(), PT, 0, h->stream>>>(A);
+    if (h->layout.position_form) k_particles<true, MODE_P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    else k_particles<false, MODE_P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
     h->launches += 1;
     return cudaGetLastError();
 }
@@ -997,8 +997,8 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 g, bool write_keys, bool
     if (!write_keys) A.keys_out = nullptr;
     if (!use_perm) A.perm = nullptr;
     Scoped s(h, "g2p2g");
-    if (h->layout.position_form) k_particles<true, MODE_G2P2G><<<particle_blocks(), PT, 0, h->stream>>>(A);
-    else k_particles<false, MODE_G2P2G><<<particle_blocks(), PT, 0, h->stream>>>(A);
+    if (h->layout.position_form) k_particles<true, MODE_G2P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    else k_particles<false, MODE_G2P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
     k_finish<<<1, 1, 0, h->stream>>>(h->counters);
     h->launches += 2;
     h->vel_side = h->gcur;

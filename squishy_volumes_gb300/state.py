@@ -398,6 +398,18 @@ class CudaState:
         """Queue all work on a caller-owned cudaStream_t (0 = own stream)."""
         check(self._lib.sv_set_stream(self._h, ct.c_void_p(stream_handle or None)))
 
+    def set_graphs(self, on: bool):
+        check(self._lib.sv_set_graphs(self._h, 1 if on else 0))
+
+    def autotune(self, dt: float, gravity, substeps_per_trial: int = 16):
+        """Times the binning interval x CTAs-per-SM candidates on a snapshot
+        of the state (restored afterwards) and keeps the fastest."""
+        g = np.asarray(gravity, dtype=np.float32)
+        si, cta = ct.c_uint32(0), ct.c_uint32(0)
+        check(self._lib.sv_autotune(self._h, float(dt), ptr(g, f32p), int(substeps_per_trial), ct.byref(si),
+                                    ct.byref(cta)))
+        return {"sort_interval": int(si.value), "cta_per_sm": int(cta.value)}
+
     def set_profiling(self, on: bool):
         check(self._lib.sv_set_profiling(self._h, 1 if on else 0))
 

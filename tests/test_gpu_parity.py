@@ -258,6 +258,40 @@ def test_fast_particles_rebin(cuda_lib, oracle_mod):
     gpu.close()
 
 
+@pytest.mark.parametrize("form", [0, 1])
+def test_free_fall_leaves_fluid_and_sand_unstrained(cuda_lib, oracle_mod, form):
+    """Bodies at rest in free fall: the grid velocity is uniform, so C is
+    rounding noise and F must stay the identity to that noise.  The fluid
+    and sand returns rebuild F from U V^T every substep; an SVD that rotated
+    columns already orthogonal to fp32 epsilon (F = I + 1e-13) put 1e-8
+    noise into F there, which the stiff fluid turned into pressure."""
+    from squishy_volumes_gb300.scenes import Material, build_particles, jittered_box
+    from squishy_volumes_gb300 import IoState
+
+    rng = np.random.default_rng(11)
+    dx = 1.0 / 256
+    blocks = [(jittered_box(rng, (0.3, 0.3, 0.3), (24, 24, 16), dx / 2), Material("fluid", bulk_modulus=1e5), (0, 0, 0),
+               dx / 2),
+              (jittered_box(rng, (0.5, 0.3, 0.3), (16, 16, 16), dx / 2), Material("sand", youngs_modulus=1e5), (0, 0, 0),
+               dx / 2)]
+    p = build_particles(blocks)
+    consts = InputConsts(grid_node_size=dx, domain_min=(0.0, 0.0, 0.0), domain_max=(1.0, 1.0, 1.0))
+    n, dt, g = 10, 2e-5, (0.0, 0.0, -9.81)
+    gpu = CudaState.from_io_state(IoState(0.0, p), consts, Extras(position_form=form))
+    assert gpu.step(n, dt, g) == (0, n)
+    out = gpu.download()
+    gpu.close()
+    eye = np.eye(3, dtype=np.float32).reshape(9)
+    assert np.abs(out.position_gradients - eye).max() <= 1e-9
+    np.testing.assert_allclose(out.velocities[:, 2], -9.81 * n * dt, rtol=1e-5)
+    assert np.abs(out.velocities[:, :2]).max() <= 1e-9
+    ref = oracle_mod.OracleState(p, consts, None, fp64=True)
+    assert ref.step(n, dt, g) == 0
+    exp = ref.download()
+    ok, r = by_norm(out.velocities, exp.velocities, 1e-6)
+    assert ok, r
+
+
 # ---------------------------------------------------------------- edge cases
 def test_empty_scene(cuda_lib):
     s = scenes.small_mixed()

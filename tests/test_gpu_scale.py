@@ -50,11 +50,13 @@ def test_cell_form_is_closer_to_fp64_on_a_fine_grid(cuda_lib, oracle_mod):
     """At dx = 1/512 the fp32 position ulp (6e-8 m at 0.5 m) exceeds the
     per-substep displacement (v dt ~ 2e-8 m), so the fp32 form rounds motion
     away; the int32-cell + fp32-offset form keeps it.  Against the fp64
-    oracle, the cell form must be the closer of the two, and its velocity
-    error no larger than that of the fp32 restatement of the reference
-    itself: the stiff fluid (K = 1e5, exponent 7) turns the ~1e-7 fp32 noise
-    of J after the volumetric reset into pressure noise, so fp32 velocities
-    of any implementation sit ~1e-2 from fp64 after a few substeps."""
+    oracle the cell form must be the closer of the two in position, and both
+    forms' velocities must stay within twice the error of the fp32
+    restatement of the reference.  The fluid column at rest is the sharp
+    case: its volumetric return rebuilds F from U V^T every substep, and the
+    stiff fluid (K = 1e5, exponent 7) turns any rounding noise of that
+    rebuild into pressure; an SVD that rotates already-orthogonal columns
+    put the GPU 1.7e-2 away from fp64 here."""
     s = scenes.dam_break_8m(fluid_dims=(40, 40, 20), box_dims=(10, 10, 10))
     n = 5
     ref = oracle_mod.OracleState(s.io_state.particles, s.consts, s.extras, fp64=True)
@@ -73,6 +75,6 @@ def test_cell_form_is_closer_to_fp64_on_a_fine_grid(cuda_lib, oracle_mod):
         np.testing.assert_array_equal(out.flags, exp.flags)
         errs[form] = {k: np.linalg.norm(getattr(out, k).astype(np.float64) - getattr(exp, k))
                       / np.linalg.norm(getattr(exp, k)) for k in ("positions", "velocities")}
-    assert errs[1]["velocities"] <= errs[0]["velocities"] * 1.001, errs
-    assert errs[1]["velocities"] <= 2.0 * oracle32_v + 1e-6, (errs, oracle32_v)
-    assert errs[1]["positions"] <= errs[0]["positions"] * 1.01 + 1e-12, errs
+    for form in (0, 1):
+        assert errs[form]["velocities"] <= 2.0 * oracle32_v + 1e-9, (errs, oracle32_v)
+    assert errs[1]["positions"] <= errs[0]["positions"], errs
