@@ -250,6 +250,26 @@ int sv_set_stream(sv_handle *h, void *stream);
 int sv_set_profiling(sv_handle *h, int enable);
 int sv_profile_report(sv_handle *h, char *buffer, uint64_t capacity);
 
+/* ------------------------------------------------------------------ learned closure
+ * Addition (not in the reference): a small MLP that maps principal stretches
+ * and material parameters to principal Kirchhoff stress and projected
+ * stretch, evaluated on the tensor cores (bf16 operands, fp32 accumulation).
+ * Network: x (16) -> ReLU (32) -> ReLU (32) -> y (16, the first 6 used).
+ * Parameters are an fp32 vector of sv_mlp_param_count() values:
+ * W1[32][16], b1[32], W2[32][32], b2[32], W3[16][32], b3[16] (row-major,
+ * out x in).
+ *
+ * The two entry points below are stateless inspection calls on host
+ * buffers (they allocate device memory per call) used to check the kernels:
+ *   sv_mlp_forward: y[n][16] = network(x[n][16]);
+ *   sv_mlp_grad:    loss = sum_r w[r] sum_{o<6} (y[r][o] - t[r][o])^2 / n, its
+ *                   gradient with respect to the parameters into grad[], and
+ *                   y[n][16] when y is not NULL. */
+int sv_mlp_param_count(void);
+int sv_mlp_forward(const float *params, const float *x, uint64_t n, float *y);
+int sv_mlp_grad(const float *params, const float *x, const float *t, const float *w, uint64_t n, float *y,
+                float *grad, float *loss);
+
 #ifdef __cplusplus
 }
 #endif

@@ -119,6 +119,9 @@ _SIGNATURES = {
     "sv_autotune": (ct.c_int, [ct.c_void_p, ct.c_float, f32p, ct.c_uint32, u32p, u32p]),
     "sv_set_profiling": (ct.c_int, [ct.c_void_p, ct.c_int]),
     "sv_profile_report": (ct.c_int, [ct.c_void_p, ct.c_char_p, ct.c_uint64]),
+    "sv_mlp_param_count": (ct.c_int, []),
+    "sv_mlp_forward": (ct.c_int, [f32p, f32p, ct.c_uint64, f32p]),
+    "sv_mlp_grad": (ct.c_int, [f32p, f32p, f32p, f32p, ct.c_uint64, f32p, f32p, f32p]),
 }
 
 _lib = None

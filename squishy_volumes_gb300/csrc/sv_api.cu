@@ -303,6 +303,8 @@ void timer_end(sv_handle *h, const char *name, cudaEvent_t start) {
     h->timer.pending.push_back({name, {start, stop}});
 }
 
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+
 }  // namespace sv
 
 extern "C" {

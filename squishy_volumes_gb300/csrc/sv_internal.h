@@ -189,4 +189,7 @@ void timer_end(sv_handle *h, const char *name, cudaEvent_t start);
 
 int sm_count();
 
+// Sets the string sv_last_error_string returns (this thread).
+void set_last_error(const std::string &msg);
+
 }  // namespace sv
