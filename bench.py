@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--autotune", action="store_true",
                     help="time binning interval x CTAs/SM candidates first and keep the fastest (sv_autotune)")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel directly (no CUDA graphs)")
+    ap.add_argument("--closure", default="plain", choices=["plain", "learned"],
+                    help="snow/sand constitutive update: SVD + return map, or the learned closure (trained first)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bound on the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -246,6 +248,27 @@ def run_ours(args, rank, world, local):
     # library (the CUDA graphs of the binning periods are captured on it).
     stream = torch.cuda.Stream(device=dev)
     gpu.set_stream(stream.cuda_stream)
+    closure_info = None
+    if args.closure == "learned":
+        # training data from plain substeps of this scene, then the GPU
+        # training loop; none of this is inside the timed region
+        t0 = time.perf_counter()
+        pool = 0
+        for k in range(8):
+            gpu.step(20, scene.dt, scene.gravity)
+            pool = gpu.closure_harvest(scene.dt, 60000, 0.02, seed=k)
+        t1 = time.perf_counter()
+        loss = gpu.closure_train(4000, 8192, 3e-3, seed=1)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        ev = gpu.closure_evaluate(scene.dt)
+        gpu.closure_set_mode(1)
+        closure_info = {"mode": "learned", "pool": pool, "harvest_s": round(t1 - t0, 3),
+                        "train_s": round(t2 - t1, 3), "train_iterations": 4000, "loss": loss,
+                        "stress_rel_err_learned": ev["stress_err_learned"],
+                        "stress_rel_err_plain_fp32": ev["stress_err_plain32"],
+                        "projected_f_rel_err_learned": ev["f_err_learned"],
+                        "fallback_fraction": ev["fallbacks"] / max(ev["particles"], 1.0)}
     tuned = None
     if args.autotune:
         tuned = gpu.autotune(scene.dt, scene.gravity, 16)
@@ -288,6 +311,20 @@ def run_ours(args, rank, world, local):
     live = stats1["live_particles"]
     value = live * args.steps * world / elapsed
     launches = stats1["kernel_launches"] - stats0["kernel_launches"]
+    if closure_info is not None:
+        # the same K substeps with the return maps, from the state reached
+        closure_info["learned_fraction"] = (stats1["closure_learned"] - stats0["closure_learned"]) / max(
+            1, live * args.steps)
+        gpu.closure_set_mode(0)
+        gpu.step(args.warmup, scene.dt, scene.gravity)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        gpu.step(args.steps, scene.dt, scene.gravity)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        closure_info["plain_value"] = live * args.steps * world / (ev0.elapsed_time(ev1) * 1e-3)
+        closure_info["learned_over_plain"] = value / closure_info["plain_value"]
+        gpu.closure_set_mode(1)
 
     # per-kernel durations: the same K substeps again with CUDA events around
     # every kernel group on the library's stream
@@ -405,6 +442,7 @@ def run_ours(args, rank, world, local):
         "clocks": clocks.summary(),
         "fp64_svd_particles": st["fp64_svd"],
         "error_vs_fp64": error,
+        "closure": closure_info,
     }
     if rank == 0:
         print(json.dumps(line))

@@ -224,6 +224,9 @@ typedef struct sv_stats {
     uint64_t tile_misses;       /* gathers that missed their block's shared tile (low 32 bits) */
     uint64_t graph_replays;     /* binning periods run as CUDA graph replays */
     uint64_t cta_per_sm;        /* CTAs per SM of the particle kernels */
+    uint64_t closure_learned;   /* snow/sand particle-substeps through the learned closure (low 32 bits) */
+    uint64_t closure_fallbacks; /* of the learned mode's snow/sand particle-substeps: return-map fallbacks */
+    uint64_t closure_mode;      /* 0 return maps, 1 learned closure */
 } sv_stats;
 
 /* Whether sv_step runs whole binning periods as CUDA graphs (default on;
@@ -269,6 +272,35 @@ int sv_mlp_param_count(void);
 int sv_mlp_forward(const float *params, const float *x, uint64_t n, float *y);
 int sv_mlp_grad(const float *params, const float *x, const float *t, const float *w, uint64_t n, float *y,
                 float *grad, float *loss);
+
+/* The closure of a handle's snow and sand particles.
+ *
+ * sv_closure_harvest: adds up to max_samples trial deformation gradients
+ *   F + dt C F of the live snow/sand particles of the current state (states
+ *   the plain solver produced) to the handle's training pool (at most 2^22);
+ *   with augment > 0 half of them are multiplied by I + augment R, R
+ *   symmetric with entries in [-1, 1).  *total_out = pool size.
+ * sv_closure_train: labels the pool with the fp64 SVD + return map, records
+ *   the range of the features (the hull outside which the return map is
+ *   used), and runs `iterations` Adam steps (minibatches of `batch`,
+ *   learning rate lr with a cosine decay) on the GPU from the current
+ *   weights (He-initialised from `seed` on the first call).  *loss_out =
+ *   mean squared error over the pool afterwards.
+ * sv_closure_set_mode: 0 = return maps (default), 1 = learned closure in
+ *   sv_step (needs a trained network).
+ * sv_closure_evaluate: on the trial F of the current state, out[0] / out[1]
+ *   = relative Kirchhoff-stress error (Frobenius, over all snow/sand
+ *   particles) of the learned closure (with its fallbacks) / of the fp32
+ *   return map, both against the fp64 return map; out[2] / out[3] the same
+ *   for the projected F; out[4] particles evaluated, out[5] fallbacks,
+ *   out[6] |tau_fp64|, out[7] |F_fp64|.
+ * sv_closure_get_params: the fp32 master weights (sv_mlp_param_count()). */
+int sv_closure_harvest(sv_handle *h, float dt, uint32_t max_samples, float augment, uint32_t seed,
+                       uint64_t *total_out);
+int sv_closure_train(sv_handle *h, uint32_t iterations, uint32_t batch, float lr, uint32_t seed, float *loss_out);
+int sv_closure_set_mode(sv_handle *h, int mode);
+int sv_closure_evaluate(sv_handle *h, float dt, double out[8]);
+int sv_closure_get_params(sv_handle *h, float *params);
 
 #ifdef __cplusplus
 }

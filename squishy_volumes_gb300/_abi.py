@@ -92,6 +92,9 @@ class SvStats(ct.Structure):
         ("tile_misses", ct.c_uint64),
         ("graph_replays", ct.c_uint64),
         ("cta_per_sm", ct.c_uint64),
+        ("closure_learned", ct.c_uint64),
+        ("closure_fallbacks", ct.c_uint64),
+        ("closure_mode", ct.c_uint64),
     ]
 
 
@@ -122,6 +125,12 @@ _SIGNATURES = {
     "sv_mlp_param_count": (ct.c_int, []),
     "sv_mlp_forward": (ct.c_int, [f32p, f32p, ct.c_uint64, f32p]),
     "sv_mlp_grad": (ct.c_int, [f32p, f32p, f32p, f32p, ct.c_uint64, f32p, f32p, f32p]),
+    "sv_closure_harvest": (ct.c_int, [ct.c_void_p, ct.c_float, ct.c_uint32, ct.c_float, ct.c_uint32,
+                                      ct.POINTER(ct.c_uint64)]),
+    "sv_closure_train": (ct.c_int, [ct.c_void_p, ct.c_uint32, ct.c_uint32, ct.c_float, ct.c_uint32, f32p]),
+    "sv_closure_set_mode": (ct.c_int, [ct.c_void_p, ct.c_int]),
+    "sv_closure_evaluate": (ct.c_int, [ct.c_void_p, ct.c_float, ct.POINTER(ct.c_double)]),
+    "sv_closure_get_params": (ct.c_int, [ct.c_void_p, f32p]),
 }
 
 _lib = None

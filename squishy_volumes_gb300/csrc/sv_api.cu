@@ -57,6 +57,7 @@ void free_handle(sv_handle *h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (auto &kv : h->graphs)
         if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    free_closure(h);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
 }
@@ -304,6 +305,8 @@ void timer_end(sv_handle *h, const char *name, cudaEvent_t start) {
 }
 
 void set_last_error(const std::string &msg) { g_last_error = msg; }
+
+void drop_graphs(sv_handle *h) { clear_graphs(h); }
 
 }  // namespace sv
 
@@ -629,6 +632,7 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
         const uint32_t st = h->host_counters[C_STATUS];
         done = h->host_counters[C_SUBSTEPS] - base;
         if (st & ST_OUT_OF_GRID) return fail("sv_step: a live particle left the grid block index");
+        if (h->host_counters[C_CLOSURE_ERR]) return fail("sv_step: a tensor-core wait of the learned closure timed out");
         if (st & (ST_CAPACITY | ST_MOVED_FAR)) {
             if (st & ST_CAPACITY) {
                 // Grow and redo what was skipped (gpu_state.rs:562-599 redoes a
@@ -867,6 +871,9 @@ int sv_get_stats(sv_handle *h, sv_stats *out) {
     out->tile_misses = h->host_counters[C_FALLBACK];
     out->graph_replays = h->graph_launches;
     out->cta_per_sm = h->cta_per_sm;
+    out->closure_learned = h->host_counters[C_CLOSURE];
+    out->closure_fallbacks = h->host_counters[C_CLOSURE_FB];
+    out->closure_mode = (uint64_t)h->closure_mode;
     return 0;
 }
 

@@ -40,6 +40,9 @@ enum Counter : int {
     C_FP64 = 6,      // particles that took the fp64 SVD
     C_STOP = 7,      // STOP_MASK bits latched for the kernels that follow
     C_FALLBACK = 8,  // gathers that missed their segment's shared tile
+    C_CLOSURE = 9,       // snow/sand particle-substeps through the learned closure
+    C_CLOSURE_FB = 10,   // snow/sand particle-substeps that fell back to the return map
+    C_CLOSURE_ERR = 11,  // a tensor-core wait of the learned closure gave up
     C_COUNT = 12,
 };
 
@@ -169,6 +172,22 @@ struct sv_handle {
     std::map<GraphKey, GraphState> graphs;
     bool use_graphs = true;
     uint64_t graph_launches = 0;  // graph replays issued
+
+    // Learned stress closure of snow and sand (sv_closure.cu).
+    int closure_mode = 0;  // 0 return maps (SVD), 1 learned closure
+    bool cl_trained = false;
+    float *cl_params = nullptr, *cl_grad = nullptr, *cl_m = nullptr, *cl_v = nullptr;  // fp32 master + Adam
+    uint8_t *cl_img = nullptr;      // packed bf16 weight image
+    void *cl_hull = nullptr;        // closure::Hull of the training features
+    float *cl_samples = nullptr;    // [cl_cap][CL_SAMPLE]: trial F, plastic J, material index bits
+    uint64_t cl_n = 0, cl_cap = 0;  // harvested samples
+    float *cl_X = nullptr, *cl_Y = nullptr, *cl_W = nullptr;  // features, targets, weights
+    uint64_t cl_xy_cap = 0;
+    int cl_step = 0;                // Adam steps taken
+    float *cl_loss = nullptr;       // device scalar
+    uint32_t *cl_err = nullptr;     // device flag
+    uint64_t *cl_count = nullptr;   // device counter of the harvest
+    double *cl_sums = nullptr;      // device sums of the error evaluation
 };
 
 namespace sv {
@@ -191,5 +210,11 @@ int sm_count();
 
 // Sets the string sv_last_error_string returns (this thread).
 void set_last_error(const std::string &msg);
+
+// Drops the handle's captured CUDA graphs (their launches are stale).
+void drop_graphs(sv_handle *h);
+
+// Frees the learned closure's device buffers (sv_closure.cu).
+void free_closure(sv_handle *h);
 
 }  // namespace sv

@@ -224,6 +224,32 @@ __device__ __forceinline__ void svd3_fast(const m3f &F, m3f &U, float S[3], m3f 
     }
 }
 
+// fp32 SVD of a particle's F with the fp64 redo for flagged particles:
+// policy 1 redoes it when det F < 0.05, policy 2 also when two singular
+// values are closer than 1e-4.
+__device__ __forceinline__ void particle_svd(const m3f &F, m3f &U, float S[3], m3f &V, uint32_t policy,
+                                             uint32_t &fp64_count) {
+    svd3_fast(F, U, S, V);
+    bool redo = false;
+    if (policy >= 1 && det3(F) < 0.05f) redo = true;
+    if (policy >= 2) {
+        float g = fminf(fabsf(S[0] - S[1]), fminf(fabsf(S[1] - S[2]), fabsf(S[0] - S[2])));
+        if (g < 1e-4f) redo = true;
+    }
+    if (redo) {
+        m3d Fd, Ud, Vd;
+        double Sd[3];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Fd.a[k] = (double)F.a[k];
+        svd3<double>(Fd, Ud, Sd, Vd, 12);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) U.a[k] = (float)Ud.a[k], V.a[k] = (float)Vd.a[k];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) S[k] = (float)Sd[k];
+        ++fp64_count;
+    }
+}
+
 // ---------------------------------------------------------------- weights
 // Quadratic B-spline weights of the three nodes base, base+1, base+2 for a
 // particle at fx = x/dx - base in [0.5, 1.5) (rust/crates/cpu/src/kernels.rs:17-26

@@ -29,7 +29,11 @@
 // a particle that leaves the claimed blocks makes the host redo the binning.
 #include <cstdio>
 
+#include <type_traits>
+
+#include "sv_closure.cuh"
 #include "sv_internal.h"
+#include "sv_mlp.cuh"
 #include "sv_sort.cuh"
 
 namespace sv {
@@ -52,7 +56,8 @@ struct Rec {
     float4 p[9];
 };
 
-enum Mode { MODE_P2G = 0, MODE_G2P2G = 1 };
+// MODE_G2P2G_LEARNED is MODE_G2P2G with the learned closure for snow and sand.
+enum Mode { MODE_P2G = 0, MODE_G2P2G = 1, MODE_G2P2G_LEARNED = 2 };
 
 struct StepArgs {
     ParticleArrays in, out;
@@ -67,6 +72,8 @@ struct StepArgs {
     const float4 *grid_cur;
     float4 *grid_next;
     uint32_t *keys_out;  // nullptr: keys not needed after this substep
+    const uint8_t *closure_img;          // packed network weights (learned mode)
+    const closure::Hull *closure_hull;   // training hull of the features (learned mode)
     uint64_t n;
     GridLayout L;
     float dt;
@@ -153,30 +160,6 @@ __device__ __forceinline__ void copy_particle(const ParticleArrays &in, const Pa
     }
     out.energy[dst] = in.energy[src];
     out.orig[dst] = in.orig[src];
-}
-
-// fp32 SVD with the fp64 redo for flagged particles.
-__device__ __forceinline__ void particle_svd(const m3f &F, m3f &U, float S[3], m3f &V, uint32_t policy,
-                                             uint32_t &fp64_count) {
-    svd3_fast(F, U, S, V);
-    bool redo = false;
-    if (policy >= 1 && det3(F) < 0.05f) redo = true;
-    if (policy >= 2) {
-        float g = fminf(fabsf(S[0] - S[1]), fminf(fabsf(S[1] - S[2]), fabsf(S[0] - S[2])));
-        if (g < 1e-4f) redo = true;
-    }
-    if (redo) {
-        m3d Fd, Ud, Vd;
-        double Sd[3];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) Fd.a[k] = (double)F.a[k];
-        svd3<double>(Fd, Ud, Sd, Vd, 12);
-#pragma unroll
-        for (int k = 0; k < 9; ++k) U.a[k] = (float)Ud.a[k], V.a[k] = (float)Vd.a[k];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) S[k] = (float)Sd[k];
-        ++fp64_count;
-    }
 }
 
 // P F^T of the particle's model (the part of scatter_momentum.rs:46-90 that
@@ -592,22 +575,45 @@ __device__ __forceinline__ void gather_global(const StepArgs &A, const int base[
             }
 }
 
+// Shared state of the learned closure (network image, feature hull, TMEM and
+// MMA-completion control); its two operand buffers overlay the records.
+struct SharedLearned {
+    __align__(16) uint8_t img[tc::IMG_BYTES];
+    closure::Hull hull;
+    mlp::Ctl ctl;
+};
+static_assert(sizeof(Rec) * PT >= tc::NIN * PT * 2 + tc::NH * PT * 2, "closure operands overlay the records");
+
 // Five CTAs per SM (at most 102 registers): measured faster than the
-// unconstrained 150-register build despite a few spilled values.
-template <bool CELL, int MODE> __global__ void __launch_bounds__(PT, 5) k_particles(StepArgs A) {
+// unconstrained 150-register build despite a few spilled values.  The
+// learned-closure variant holds the network image as well: four CTAs.
+template <bool CELL, int MODE>
+__global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_particles(StepArgs A) {
+    constexpr bool G2P = MODE != MODE_P2G;
+    constexpr bool LEARNED = MODE == MODE_G2P2G_LEARNED;
     __shared__ Shared sh;
+    __shared__ typename std::conditional<LEARNED, SharedLearned, int>::type shl;
     if (stopped(A.counters)) {
-        if (MODE == MODE_G2P2G) {
+        if (G2P) {
             // Keep the state as it is (identity copy) so the buffer swap is a no-op.
             for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x)
                 copy_particle(A.in, A.out, A.n, i, i, CELL);
         }
         return;
     }
+    mlp::Phase ph;
+    uint32_t n_learned = 0, n_closure_fb = 0;
+    if constexpr (LEARNED) {
+        for (int t = threadIdx.x * 16; t < tc::IMG_BYTES; t += PT * 16)
+            *reinterpret_cast<uint4 *>(shl.img + t) = *reinterpret_cast<const uint4 *>(A.closure_img + t);
+        for (int t = threadIdx.x; t < 2 * tc::NIN; t += PT)
+            (&shl.hull.lo[0])[t] = (&A.closure_hull->lo[0])[t];
+        mlp::ctl_init(shl.ctl, mlp::TMEM_COLS_INFER);
+    }
     const uint32_t nseg = A.counters[C_NSEG];
     const uint32_t nlive = A.counters[C_NLIVE];
     const float dx = A.L.dx;
-    if (MODE == MODE_G2P2G) {
+    if (G2P) {
         // particles that were tombstoned at binning time are carried over
         for (uint64_t i = nlive + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x) {
             copy_particle(A.in, A.out, A.n, A.perm ? A.perm[i] : i, i, CELL);
@@ -624,11 +630,11 @@ template <bool CELL, int MODE> __global__ void __launch_bounds__(PT, 5) k_partic
         if (threadIdx.x < 27) {
             const uint32_t nbk = neighbour27(b, threadIdx.x, A.L);
             sh.slot_next[threadIdx.x] = A.map_next[nbk];
-            if (MODE == MODE_G2P2G) sh.slot_cur[threadIdx.x] = A.map_cur[nbk];
+            if (G2P) sh.slot_cur[threadIdx.x] = A.map_cur[nbk];
         }
         for (int t = threadIdx.x; t < 4 * PLANE; t += PT) (&sh.pt[0][0])[t] = 0.f;
         __syncthreads();
-        if (MODE == MODE_G2P2G) {
+        if (G2P) {
             for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
                 const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
                 const int32_t slot = sh.slot_cur[tile_neighbour(tx, ty, tz)];
@@ -641,22 +647,27 @@ template <bool CELL, int MODE> __global__ void __launch_bounds__(PT, 5) k_partic
             const int count = (int)min((uint32_t)PT, end - c0);
             uint32_t rcell = REC_NONE;
             float rmass = 0.f;
+            // this thread's particle; live across the closure network pass
+            bool work = false;
+            uint32_t p = 0, packed = 0;
+            float4 pos = make_float4(0.f, 0.f, 0.f, 0.f);
+            int4 cell = make_int4(0, 0, 0, 0);
+            m3f F, C;
+            float v[3] = {0.f, 0.f, 0.f};
+            float plastic_j = 1.f;
             if (i < end) {
-                const uint32_t p = A.perm ? A.perm[i] : i;
-                float4 pos = A.in.pos[p];
-                uint32_t packed = __float_as_uint(pos.w);
-                int4 cell = CELL ? A.in.cell[p] : make_int4(0, 0, 0, 0);
+                p = A.perm ? A.perm[i] : i;
+                pos = A.in.pos[p];
+                packed = __float_as_uint(pos.w);
+                if (CELL) cell = A.in.cell[p];
                 if (packed & SV_TOMBSTONED) {
-                    if (MODE == MODE_G2P2G) {
+                    if (G2P) {
                         copy_particle(A.in, A.out, A.n, p, i, CELL);
                         if (A.keys_out) A.keys_out[i] = SENTINEL_KEY;
                     }
                 } else {
-                    const Material mat = A.mats[packed >> MATERIAL_SHIFT];
-                    const uint32_t kind = mat.kind;
-                    m3f F, C;
-                    float v[3];
-                    float plastic_j;
+                    work = true;
+                    const uint32_t kind = A.mats[packed >> MATERIAL_SHIFT].kind;
                     load_mat9(A.in.F, A.n, p, F);
                     if (MODE == MODE_P2G) {
                         load_mat9(A.in.C, A.n, p, C);
@@ -711,14 +722,58 @@ template <bool CELL, int MODE> __global__ void __launch_bounds__(PT, 5) k_partic
                             cell = make_int4(ci[0], ci[1], ci[2], 0);
                         }
                     }
-                    // ---- SVD, plasticity (advance_particles.rs:42-86), energy
-                    m3f U, V;
-                    float S[3] = {1.f, 1.f, 1.f};
-                    const bool need_svd = MODE == MODE_G2P2G ? kind != KIND_NEO_HOOKEAN
-                                                              : (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW);
+                }
+            }
+            // ---- learned closure (snow, sand): closed-form principal
+            // stretches, then one network pass for the whole chunk on the
+            // tensor cores (all threads take part)
+            bool learned = false;
+            float l_sig[3], l_V[9], l_y[tc::NOUT];
+            if constexpr (LEARNED) {
+                float x[tc::NIN];
+                bool want = false;
+                if (work) {
+                    const Material &lm = A.mats[packed >> MATERIAL_SHIFT];
+                    if (closure::applies(lm.kind)) want = closure::learned_features(lm, F, shl.hull, l_sig, l_V, x);
+                }
+                if (!want)
+#pragma unroll
+                    for (int k = 0; k < tc::NIN; ++k) x[k] = 0.f;
+                if (__syncthreads_or(want) && !shl.ctl.abort) {
+                    uint8_t *a0 = reinterpret_cast<uint8_t *>(sh.rec);
+                    const bool ok = mlp::infer_tile(shl.ctl, ph, shl.img, a0, a0 + tc::NIN * PT * 2, x, l_y);
+                    learned = want && ok;
+                }
+            }
+            if (work) {
+                const Material mat = A.mats[packed >> MATERIAL_SHIFT];
+                const uint32_t kind = mat.kind;
+                // ---- SVD, plasticity (advance_particles.rs:42-86), energy
+                m3f U, V;
+                float S[3] = {1.f, 1.f, 1.f};
+                float energy = 0.f;
+                m3f tau_l{};  // learned path: Kirchhoff stress P F^T
+                bool use_l = false;
+                if constexpr (LEARNED) {
+                    if (learned) {
+                        m3f Fn;
+                        float e_l, jp_l, J_l;
+                        if (closure::learned_apply(mat, F, l_sig, l_V, l_y, plastic_j, Fn, tau_l, e_l, jp_l, J_l)) {
+                            use_l = true;
+                            F = Fn;
+                            plastic_j = jp_l;
+                            energy = e_l;
+                        }
+                    }
+                    if (closure::applies(kind)) {
+                        if (use_l) ++n_learned;
+                        else ++n_closure_fb;
+                    }
+                }
+                if (!use_l) {
+                    const bool need_svd = G2P ? kind != KIND_NEO_HOOKEAN : (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW);
                     if (need_svd) particle_svd(F, U, S, V, A.L.svd_policy, fp64_count);
-                    float energy = 0.f;
-                    if (MODE == MODE_G2P2G) {
+                    if (G2P) {
                         if (kind == KIND_SAND) {
                             // Drucker-Prager return map in Hencky strain (advance_particles.rs:48-71)
                             if (mat.mu > 0.f) {
@@ -754,80 +809,82 @@ template <bool CELL, int MODE> __global__ void __launch_bounds__(PT, 5) k_partic
                             F = recompose(U, S, V);
                         }
                     }
-                    const float J = det3(F);
-                    const float hard = kind == KIND_SNOW ? expf(mat.xi * (1.f - plastic_j)) : 1.f;
-                    bool alive = true;
-                    if (MODE == MODE_G2P2G) {
-                        if (kind == KIND_FLUID) {
-                            // util/src/elastic.rs:546-553
-                            const float K = mat.bulk_modulus, gm = (float)mat.exponent;
-                            const float at_rest = K * (1.f - 1.f / (1.f - gm));
-                            energy = K * (J - powi_f(J, 1 - mat.exponent) / (1.f - gm)) - at_rest;
-                        } else if (!(J > 0.f)) {
-                            // try_elastic_energy_neo_hookean: J <= 0 -> FAILED (advance_particles.rs:73-74)
-                            packed |= SV_FAILED;
-                            atomicOr(&A.counters[C_STATUS], ST_INVERTED);
-                        } else if (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW) {
-                            // mu |F - R|^2 + lambda/2 (J - 1)^2 = mu sum (s - 1)^2 + ...
-                            const float d2 = (S[0] - 1.f) * (S[0] - 1.f) + (S[1] - 1.f) * (S[1] - 1.f) + (S[2] - 1.f) * (S[2] - 1.f);
-                            energy = mat.mu * hard * d2 + mat.lambda * hard / 2.f * (J - 1.f) * (J - 1.f);
-                        } else {
-                            // util/src/elastic.rs:233-241
-                            float I2 = 0.f;
+                }
+                const float J = det3(F);
+                const float hard = kind == KIND_SNOW ? expf(mat.xi * (1.f - plastic_j)) : 1.f;
+                bool alive = true;
+                if (G2P) {
+                    if (use_l) {
+                        // energy of the learned projected stretches (J > 0 by construction)
+                    } else if (kind == KIND_FLUID) {
+                        // util/src/elastic.rs:546-553
+                        const float K = mat.bulk_modulus, gm = (float)mat.exponent;
+                        const float at_rest = K * (1.f - 1.f / (1.f - gm));
+                        energy = K * (J - powi_f(J, 1 - mat.exponent) / (1.f - gm)) - at_rest;
+                    } else if (!(J > 0.f)) {
+                        // try_elastic_energy_neo_hookean: J <= 0 -> FAILED (advance_particles.rs:73-74)
+                        packed |= SV_FAILED;
+                        atomicOr(&A.counters[C_STATUS], ST_INVERTED);
+                    } else if (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW) {
+                        // mu |F - R|^2 + lambda/2 (J - 1)^2 = mu sum (s - 1)^2 + ...
+                        const float d2 = (S[0] - 1.f) * (S[0] - 1.f) + (S[1] - 1.f) * (S[1] - 1.f) + (S[2] - 1.f) * (S[2] - 1.f);
+                        energy = mat.mu * hard * d2 + mat.lambda * hard / 2.f * (J - 1.f) * (J - 1.f);
+                    } else {
+                        // util/src/elastic.rs:233-241
+                        float I2 = 0.f;
 #pragma unroll
-                            for (int k = 0; k < 9; ++k) I2 += F.a[k] * F.a[k];
-                            const float lj = logf(J);
-                            energy = mat.mu / 2.f * (I2 - 3.f) - mat.mu * lj + mat.lambda / 2.f * lj * lj;
-                        }
-                        // cull (cull_particles.rs:17-41): strict domain bounds
-                        bool inside;
-                        if (!CELL) {
-                            inside = pos.x > A.L.domain_min[0] && pos.x < A.L.domain_max[0] && pos.y > A.L.domain_min[1] &&
-                                     pos.y < A.L.domain_max[1] && pos.z > A.L.domain_min[2] && pos.z < A.L.domain_max[2];
-                        } else {
-                            // scene-local cell coordinates against the scene's domain
-                            const SceneInfo &sc = A.scenes[mat.scene];
-                            const double q[3] = {(double)(cell.x - sc.off[0]) + pos.x, (double)(cell.y - sc.off[1]) + pos.y,
-                                                 (double)(cell.z - sc.off[2]) + pos.z};
-                            inside = q[0] > sc.dmin[0] && q[0] < sc.dmax[0] && q[1] > sc.dmin[1] && q[1] < sc.dmax[1] &&
-                                     q[2] > sc.dmin[2] && q[2] < sc.dmax[2];
-                        }
-                        if (!inside) packed |= SV_TOMBSTONED;
-                        alive = !(packed & (SV_TOMBSTONED | SV_FAILED));
-                        // write the advanced state in sorted order
-                        pos.w = __uint_as_float(packed);
-                        A.out.pos[i] = pos;
-                        if (CELL) A.out.cell[i] = cell;
-                        A.out.vel[i] = make_float4(v[0], v[1], v[2], plastic_j);
-                        store_mat9(A.out.C, A.n, i, C);
-                        store_mat9(A.out.F, A.n, i, F);
-                        A.out.energy[i] = energy;
-                        A.out.orig[i] = A.in.orig[p];
+                        for (int k = 0; k < 9; ++k) I2 += F.a[k] * F.a[k];
+                        const float lj = logf(J);
+                        energy = mat.mu / 2.f * (I2 - 3.f) - mat.mu * lj + mat.lambda / 2.f * lj * lj;
                     }
-                    int nbase[3];
-                    float nfx[3];
-                    grid_position<CELL>(pos, cell, dx, nbase, nfx);
-                    if (MODE == MODE_G2P2G && A.keys_out) {
-                        uint32_t key = SENTINEL_KEY;
-                        if (!(packed & SV_TOMBSTONED)) {
-                            bool ok;
-                            key = cell_key(nbase[0], nbase[1], nbase[2], A.L, ok);
-                            if (!ok) atomicOr(&A.counters[C_STATUS], ST_OUT_OF_GRID);
-                        }
-                        A.keys_out[i] = key;
+                    // cull (cull_particles.rs:17-41): strict domain bounds
+                    bool inside;
+                    if (!CELL) {
+                        inside = pos.x > A.L.domain_min[0] && pos.x < A.L.domain_max[0] && pos.y > A.L.domain_min[1] &&
+                                 pos.y < A.L.domain_max[1] && pos.z > A.L.domain_min[2] && pos.z < A.L.domain_max[2];
+                    } else {
+                        // scene-local cell coordinates against the scene's domain
+                        const SceneInfo &sc = A.scenes[mat.scene];
+                        const double q[3] = {(double)(cell.x - sc.off[0]) + pos.x, (double)(cell.y - sc.off[1]) + pos.y,
+                                             (double)(cell.z - sc.off[2]) + pos.z};
+                        inside = q[0] > sc.dmin[0] && q[0] < sc.dmax[0] && q[1] > sc.dmin[1] && q[1] < sc.dmax[1] &&
+                                 q[2] > sc.dmin[2] && q[2] < sc.dmax[2];
                     }
-                    if (alive) {
-                        // ---- scatter record of the next substep: external force
-                        // (external_force.rs:17-50) then the momentum of
-                        // scatter_momentum.rs:38-90
-                        v[0] += A.dt * A.gravity.x, v[1] += A.dt * A.gravity.y, v[2] += A.dt * A.gravity.z;
-                        const m3f PFt = stress_times_ft(mat, F, J, U, S, hard);
-                        make_record(mat, C, PFt, J, v, nfx, dx, A.dt, sh.rec[threadIdx.x]);
-                        rmass = mat.mass;
-                        int4 gb;
-                        rcell = tile_cell(nbase, org, gb);
-                        if (rcell == REC_GLOBAL) sh.gbase[threadIdx.x] = gb;
+                    if (!inside) packed |= SV_TOMBSTONED;
+                    alive = !(packed & (SV_TOMBSTONED | SV_FAILED));
+                    // write the advanced state in sorted order
+                    pos.w = __uint_as_float(packed);
+                    A.out.pos[i] = pos;
+                    if (CELL) A.out.cell[i] = cell;
+                    A.out.vel[i] = make_float4(v[0], v[1], v[2], plastic_j);
+                    store_mat9(A.out.C, A.n, i, C);
+                    store_mat9(A.out.F, A.n, i, F);
+                    A.out.energy[i] = energy;
+                    A.out.orig[i] = A.in.orig[p];
+                }
+                int nbase[3];
+                float nfx[3];
+                grid_position<CELL>(pos, cell, dx, nbase, nfx);
+                if (G2P && A.keys_out) {
+                    uint32_t key = SENTINEL_KEY;
+                    if (!(packed & SV_TOMBSTONED)) {
+                        bool ok;
+                        key = cell_key(nbase[0], nbase[1], nbase[2], A.L, ok);
+                        if (!ok) atomicOr(&A.counters[C_STATUS], ST_OUT_OF_GRID);
                     }
+                    A.keys_out[i] = key;
+                }
+                if (alive) {
+                    // ---- scatter record of the next substep: external force
+                    // (external_force.rs:17-50) then the momentum of
+                    // scatter_momentum.rs:38-90
+                    v[0] += A.dt * A.gravity.x, v[1] += A.dt * A.gravity.y, v[2] += A.dt * A.gravity.z;
+                    const m3f PFt = use_l ? tau_l : stress_times_ft(mat, F, J, U, S, hard);
+                    make_record(mat, C, PFt, J, v, nfx, dx, A.dt, sh.rec[threadIdx.x]);
+                    rmass = mat.mass;
+                    int4 gb;
+                    rcell = tile_cell(nbase, org, gb);
+                    if (rcell == REC_GLOBAL) sh.gbase[threadIdx.x] = gb;
                 }
             }
             sh.meta[threadIdx.x] = make_float2(__uint_as_float(rcell), rmass);
@@ -852,11 +909,18 @@ template <bool CELL, int MODE> __global__ void __launch_bounds__(PT, 5) k_partic
     for (int o = 16; o > 0; o >>= 1) {
         fp64_count += __shfl_xor_sync(0xffffffffu, fp64_count, o);
         fallback += __shfl_xor_sync(0xffffffffu, fallback, o);
+        if (LEARNED) {
+            n_learned += __shfl_xor_sync(0xffffffffu, n_learned, o);
+            n_closure_fb += __shfl_xor_sync(0xffffffffu, n_closure_fb, o);
+        }
     }
     if ((threadIdx.x & 31) == 0) {
         if (fp64_count) atomicAdd(&A.counters[C_FP64], fp64_count);
         if (fallback) atomicAdd(&A.counters[C_FALLBACK], fallback);
+        if (n_learned) atomicAdd(&A.counters[C_CLOSURE], n_learned);
+        if (n_closure_fb) atomicAdd(&A.counters[C_CLOSURE_FB], n_closure_fb);
     }
+    if constexpr (LEARNED) mlp::ctl_finish(shl.ctl, mlp::TMEM_COLS_INFER, &A.counters[C_CLOSURE_ERR]);
 }
 
 __global__ void k_finish(uint32_t *counters) {
@@ -893,6 +957,8 @@ StepArgs make_args(sv_handle *h, float dt, float3 g) {
     A.grid_cur = h->grid[h->gcur];
     A.grid_next = h->grid[h->gcur ^ 1];
     A.keys_out = h->keys;
+    A.closure_img = nullptr;
+    A.closure_hull = nullptr;
     A.n = h->n;
     A.L = h->layout;
     A.dt = dt;
@@ -997,8 +1063,16 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 g, bool write_keys, bool
     if (!write_keys) A.keys_out = nullptr;
     if (!use_perm) A.perm = nullptr;
     Scoped s(h, "g2p2g");
-    if (h->layout.position_form) k_particles<true, MODE_G2P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
-    else k_particles<false, MODE_G2P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    if (h->closure_mode == 1 && h->cl_trained) {
+        A.closure_img = h->cl_img;
+        A.closure_hull = reinterpret_cast<const closure::Hull *>(h->cl_hull);
+        if (h->layout.position_form) k_particles<true, MODE_G2P2G_LEARNED><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+        else k_particles<false, MODE_G2P2G_LEARNED><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    } else if (h->layout.position_form) {
+        k_particles<true, MODE_G2P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    } else {
+        k_particles<false, MODE_G2P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    }
     k_finish<<<1, 1, 0, h->stream>>>(h->counters);
     h->launches += 2;
     h->vel_side = h->gcur;

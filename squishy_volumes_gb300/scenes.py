@@ -244,10 +244,37 @@ def batched_64(seed: int = 4, n_scenes: int = 64, median: float = 8e4, sigma: fl
     return scenes_out
 
 
+def snow_sand_2m(seed: int = 6, box_dims=(100, 100, 100), dx: float = 1.0 / 512) -> Scene:
+    """Learned-closure workload: a snow box (E = 1.4e5, nu = 0.2,
+    theta_c = 2.5e-2, theta_s = 7.5e-3, xi = 10) and a Drucker-Prager sand
+    box (E = 3.5e5, nu = 0.3, friction angle 35 deg) of ~1M particles each
+    (2 per cell axis, jittered), moving towards each other at 1 m/s each
+    (2 m/s closing speed) over a 512^3 domain (dx = 1/512).  dt = 5e-5,
+    1000 substeps, sticky ground plane, cell + offset positions."""
+    rng = np.random.default_rng(seed)
+    snow = Material("snow", youngs_modulus=1.4e5, poissons_ratio=0.2, crit_compression=2.5e-2, crit_stretch=7.5e-3,
+                    hardening=10.0)
+    sand = Material("sand", youngs_modulus=3.5e5, poissons_ratio=0.3, friction_angle_deg=35.0)
+    cells = int(round(1.0 / dx))
+    side = box_dims[0] // 2  # cells per box edge
+    gap = max(4, side // 10)
+    x0, y0, z0 = cells // 2 - side - gap // 2, (2 * cells) // 5, 16
+    blocks = [
+        (jittered_box(rng, (x0 * dx, y0 * dx, z0 * dx), box_dims, dx / 2), snow, (1.0, 0.0, 0.0), dx / 2),
+        (jittered_box(rng, ((x0 + side + gap) * dx, y0 * dx, z0 * dx), box_dims, dx / 2), sand, (-1.0, 0.0, 0.0),
+         dx / 2),
+    ]
+    p = build_particles(blocks)
+    consts = InputConsts(grid_node_size=dx, domain_min=(0.0, 0.0, 0.0), domain_max=(1.0, 1.0, 1.0))
+    extras = Extras(ground_mode=1, ground_axis=2, ground_height=8 * dx, position_form=1)
+    return Scene("snow_sand_2m", IoState(0.0, p), consts, extras, dt=5e-5, substeps=1000)
+
+
 SCENES = {
     "cube_64k": cube_64k,
     "three_boxes_1m": three_boxes_1m,
     "dam_break_8m": dam_break_8m,
     "small_mixed": small_mixed,
     "batched_64": batched_64,
+    "snow_sand_2m": snow_sand_2m,
 }

@@ -398,6 +398,35 @@ class CudaState:
         """Queue all work on a caller-owned cudaStream_t (0 = own stream)."""
         check(self._lib.sv_set_stream(self._h, ct.c_void_p(stream_handle or None)))
 
+    # ---- learned closure of snow and sand (an addition; see sv_closure_* in the C header)
+    def closure_harvest(self, dt: float, max_samples: int, augment: float = 0.0, seed: int = 0) -> int:
+        total = ct.c_uint64(0)
+        check(self._lib.sv_closure_harvest(self._h, float(dt), int(max_samples), float(augment), int(seed),
+                                           ct.byref(total)))
+        return int(total.value)
+
+    def closure_train(self, iterations: int, batch: int = 8192, lr: float = 3e-3, seed: int = 0) -> float:
+        loss = ct.c_float(0.0)
+        check(self._lib.sv_closure_train(self._h, int(iterations), int(batch), float(lr), int(seed), ct.byref(loss)))
+        return float(loss.value)
+
+    def closure_set_mode(self, mode: int):
+        check(self._lib.sv_closure_set_mode(self._h, int(mode)))
+
+    def closure_evaluate(self, dt: float) -> dict:
+        out = (ct.c_double * 8)()
+        check(self._lib.sv_closure_evaluate(self._h, float(dt), out))
+        keys = ("stress_err_learned", "stress_err_plain32", "f_err_learned", "f_err_plain32", "particles",
+                "fallbacks", "stress_norm", "f_norm")
+        return {k: float(v) for k, v in zip(keys, out)}
+
+    def closure_params(self) -> np.ndarray:
+        from .closure import param_count
+
+        p = np.zeros(param_count(), np.float32)
+        check(self._lib.sv_closure_get_params(self._h, ptr(p, f32p)))
+        return p
+
     def set_graphs(self, on: bool):
         check(self._lib.sv_set_graphs(self._h, 1 if on else 0))
 
