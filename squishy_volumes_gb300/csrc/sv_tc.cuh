@@ -186,8 +186,11 @@ __host__ __device__ inline void sym_eig3(const float a_in[6], float lam[3], floa
         lam[0] = lam[1] = lam[2] = q * m;
         return;
     }
-    const float c00 = b11 * b22 - a12 * a12, c01 = a01 * b22 - a12 * a02, c02 = a01 * a12 - b11 * a02;
-    const float det = (b00 * c00 - a01 * c01 + a02 * c02) / (p * p * p);
+    // det((A - qI) / p), formed from the divided entries so that a tiny p
+    // (A close to a multiple of I) cannot underflow
+    const float ip = 1.f / p;
+    const float d00 = b00 * ip, d11 = b11 * ip, d22 = b22 * ip, d01 = a01 * ip, d02 = a02 * ip, d12 = a12 * ip;
+    const float det = d00 * (d11 * d22 - d12 * d12) - d01 * (d01 * d22 - d12 * d02) + d02 * (d01 * d12 - d11 * d02);
     const float half = fminf(fmaxf(0.5f * det, -1.f), 1.f);
     const float ang = acosf(half) / 3.f;
     const float two_thirds_pi = 2.09439510239319549f;
@@ -203,9 +206,19 @@ __host__ __device__ inline void sym_eig3(const float a_in[6], float lam[3], floa
     };
     // eigenvector of the eigenvalue `e` that is well separated from the others
     auto vec0 = [&](float e, float out[3]) {
-        const float r0[3] = {A[0][0] - e, A[0][1], A[0][2]};
-        const float r1[3] = {A[1][0], A[1][1] - e, A[1][2]};
-        const float r2[3] = {A[2][0], A[2][1], A[2][2] - e};
+        // rows of A - e I, scaled to a largest entry of 1 so that their cross
+        // products cannot underflow when A is close to a multiple of I
+        float r0[3] = {A[0][0] - e, A[0][1], A[0][2]};
+        float r1[3] = {A[1][0], A[1][1] - e, A[1][2]};
+        float r2[3] = {A[2][0], A[2][1], A[2][2] - e};
+        float rm = 0.f;
+        for (int k = 0; k < 3; ++k) rm = fmaxf(rm, fmaxf(fabsf(r0[k]), fmaxf(fabsf(r1[k]), fabsf(r2[k]))));
+        if (!(rm > 0.f)) {
+            out[0] = 1.f, out[1] = 0.f, out[2] = 0.f;
+            return;
+        }
+        const float irm = 1.f / rm;
+        for (int k = 0; k < 3; ++k) r0[k] *= irm, r1[k] *= irm, r2[k] *= irm;
         float x0[3], x1[3], x2[3];
         cross(r0, r1, x0);
         cross(r0, r2, x1);
@@ -284,7 +297,14 @@ __host__ __device__ inline void sym_eig3(const float a_in[6], float lam[3], floa
         vec1(e0, al[1], e1);
         cross(e0, e1, e2);
     }
-    lam[0] = al[2] * m, lam[1] = al[1] * m, lam[2] = al[0] * m;
+    // eigenvalues as Rayleigh quotients of the eigenvectors: the cubic's
+    // trigonometric roots lose accuracy at a double root, the vectors do not
+    auto rq = [&](const float v[3]) {
+        float s = 0.f;
+        for (int r = 0; r < 3; ++r) s += v[r] * (A[r][0] * v[0] + A[r][1] * v[1] + A[r][2] * v[2]);
+        return s;
+    };
+    lam[0] = rq(e2) * m, lam[1] = rq(e1) * m, lam[2] = rq(e0) * m;
     for (int r = 0; r < 3; ++r) V[r] = e2[r], V[3 + r] = e1[r], V[6 + r] = e0[r];
 }
 
