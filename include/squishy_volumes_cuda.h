@@ -229,6 +229,25 @@ typedef struct sv_stats {
     uint64_t closure_mode;      /* 0 return maps, 1 learned closure */
 } sv_stats;
 
+/* Adaptive time steps: CpuState::produce_next_state with
+ * adaptive_time_steps = true (rust/crates/cpu/src/cpu_state.rs:146-197,
+ * rust/crates/cpu/src/phase/limit_time_step.rs:25-224,
+ * rust/crates/cpu/src/adaptive_time_step_state.rs:13-64).  Substeps run
+ * while *time_inout < target_time; each takes the time step the reference's
+ * AdaptiveTimeStepState allows at each phase (velocity, deformation, sound
+ * speed and isolated-particle limits, the minimum over the last 11 pushed
+ * limits, at most max_time_step).  The limit state persists in the handle
+ * across calls, like the reference's.  *time_inout is advanced by the
+ * substeps run.  Returns 0 (status bits as for sv_step), or -1 on a fatal
+ * error, including a zero allowed time step (the reference's ZeroTimeStep).
+ * sv_time_step_limits: the last substep's steps of external force, scatter
+ * and advance, the velocity, deformation, sound and isolated limits, and the
+ * step allowed now (FLT_MAX = no limit). */
+int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float max_time_step,
+                     const float gravity[3], const volatile int32_t *cancel, uint32_t *status_out,
+                     uint32_t *substeps_done);
+int sv_time_step_limits(sv_handle *h, float out[8]);
+
 /* Whether sv_step runs whole binning periods as CUDA graphs (default on;
  * off, and while profiling, every kernel is launched directly). */
 int sv_set_graphs(sv_handle *h, int enable);

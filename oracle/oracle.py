@@ -98,6 +98,8 @@ def lib() -> ct.CDLL:
             "svo_create": (ct.c_void_p, [ct.POINTER(OParticles), ct.POINTER(OConsts), ct.c_int, ct.c_int]),
             "svo_destroy": (None, [ct.c_void_p]),
             "svo_step": (ct.c_int, [ct.c_void_p, ct.c_uint32, ct.c_float, f32p]),
+            "svo_step_adaptive": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_double), ct.c_double, ct.c_float, f32p,
+                                             u32p, f32p]),
             "svo_download": (None, [ct.c_void_p, ct.POINTER(OParticles)]),
             "svo_grid": (ct.c_uint64, [ct.c_void_p, i32p, f32p, f32p, ct.c_uint64]),
             "svo_p2g_only": (None, [ct.c_void_p, ct.c_float, f32p]),
@@ -251,6 +253,18 @@ class OracleState:
     def step(self, n, dt, gravity):
         g = np.asarray(gravity, np.float32)
         return lib().svo_step(self._h, int(n), float(dt), _p(g, f32p))
+
+    def step_adaptive(self, time, target, max_dt, gravity):
+        """Adaptive substeps until target; returns (rc, substeps, time, limits)
+        with limits = (dt_force, dt_scatter, dt_advance, velocity,
+        deformation, sound, isolated, allowed)."""
+        g = np.asarray(gravity, np.float32)
+        t = ct.c_double(time)
+        n = ct.c_uint32(0)
+        lim = np.zeros(8, np.float32)
+        rc = lib().svo_step_adaptive(self._h, ct.byref(t), float(target), float(max_dt), _p(g, f32p), ct.byref(n),
+                                     _p(lim, f32p))
+        return rc, int(n.value), float(t.value), lim
 
     def p2g_only(self, dt, gravity):
         g = np.asarray(gravity, np.float32)

@@ -30,6 +30,7 @@
 #include <condition_variable>
 #include <cstdint>
 #include <cstring>
+#include <deque>
 #include <functional>
 #include <limits>
 #include <mutex>
@@ -507,6 +508,8 @@ inline bool compatible(uint32_t a, uint32_t b) {
 struct Base {
     virtual ~Base() {}
     virtual int step(uint32_t n, float dt, const float g[3]) = 0;
+    virtual int step_adaptive(double *time, double target, float max_dt, const float g[3], uint32_t *substeps,
+                              float limits[8]) = 0;
     virtual void download(svo_particles *out) = 0;
     virtual uint64_t grid(int32_t *ids, float *m, float *v, uint64_t cap) = 0;
     virtual void p2g_only(float dt, const float g[3]) = 0;
@@ -876,6 +879,182 @@ template <class T> struct State : Base {
         return 0;
     }
 
+    // ---- adaptive time steps
+    // cpu/src/adaptive_time_step_state.rs:13-64: each limit is an Option<f32>
+    // (has_* false = None), the prior limits a deque of at most 11.
+    struct Adaptive {
+        float max_dt = std::numeric_limits<float>::max();
+        bool has_vel = false, has_def = false, has_sound = false, has_iso = false;
+        float vel = 0, def = 0, sound = 0, iso = 0;
+        std::deque<float> prior;
+        float without_prior() const {
+            const float big = std::numeric_limits<float>::max();
+            float r = max_dt;
+            r = std::min(r, has_vel ? vel : big);
+            r = std::min(r, has_def ? def : big);
+            r = std::min(r, has_sound ? sound : big);
+            r = std::min(r, has_iso ? iso : big);
+            return r;
+        }
+        float allowed() const {
+            float r = without_prior();
+            for (float p : prior) r = std::min(r, p);
+            return r;
+        }
+        void push() {
+            if (prior.size() > 10) prior.pop_front();
+            prior.push_back(without_prior());
+        }
+    } ad;
+
+    // singular values of F, descending
+    V3<T> singular_values(const M3<T> &f) const {
+        M3<T> U, V;
+        V3<T> s;
+        svd3(f, U, s, V);
+        return s;
+    }
+
+    // cpu/src/phase/limit_time_step.rs:36-123, in f32 like the reference
+    // (T = f32 there): dx / c, c from the largest of six stiffness terms.
+    static float sound_speed_limit(const Params &q, bool fluid, const float s[3], float dx) {
+        const float x = s[0], y = s[1], z = s[2];
+        const float j = x * y * z;
+        // partial_invariant_3_by_svd and double_partial_invariant_3_by_svd (elastic.rs:123-141)
+        const float g3[3] = {y * z, x * z, x * y};
+        const float h3[3][3] = {{0, z, y}, {z, 0, x}, {y, x, 0}};
+        float first[3], second[3][3];
+        if (!fluid) {
+            // elastic.rs:314-339: dPsi/dI2 = mu / 2, dPsi/dI3 and d2Psi/dI3^2 of 276-295
+            const float e3 = (q.lambda * std::log(j) - q.mu) / j;
+            const float ee3 = (q.lambda * (1.f - std::log(j)) + q.mu) / (j * j);
+            for (int a = 0; a < 3; ++a) {
+                first[a] = q.mu / 2.f * 2.f * s[a] + e3 * g3[a];
+                for (int b = 0; b < 3; ++b) second[a][b] = (a == b ? q.mu / 2.f * 2.f : 0.f) + ee3 * g3[a] * g3[b] + e3 * h3[a][b];
+            }
+        } else {
+            // elastic.rs:555-570 and 630-654
+            const float e3 = q.bulk_modulus * (1.f - 1.f / powi<float>(j, q.exponent));
+            const float ee3 = (float)q.exponent * q.bulk_modulus / powi<float>(j, q.exponent + 1);
+            for (int a = 0; a < 3; ++a) {
+                first[a] = e3 * g3[a];
+                for (int b = 0; b < 3; ++b) second[a][b] = ee3 * g3[a] * g3[b] + e3 * h3[a][b];
+            }
+        }
+        const float sep = 1e-5f;  // util/src/consts.rs:14
+        const bool xy = std::fabs(x - y) < sep, yz = std::fabs(y - z) < sep, zx = std::fabs(z - x) < sep;
+        const float terms[6] = {
+            x * x * second[0][0],
+            y * y * second[1][1],
+            z * z * second[2][2],
+            y * y * (xy ? (first[0] + x * second[0][0] - y * second[1][0]) / 2.f / x : (x * first[0] - y * first[1]) / (x * x - y * y)),
+            y * z * (yz ? (first[1] + y * second[1][1] - z * second[2][1]) / 2.f / y : (y * first[1] - z * first[2]) / (y * y - z * z)),
+            z * x * (zx ? (first[2] + x * second[2][2] - x * second[0][2]) / 2.f / z : (z * first[2] - x * first[0]) / (z * z - x * x)),
+        };
+        float kappa = terms[0];
+        for (int k = 1; k < 6; ++k) kappa = std::max(kappa, terms[k]);
+        kappa /= j;
+        const float density = q.mass / q.initial_volume / j;
+        return dx / std::sqrt(kappa / density);
+    }
+
+    // limit_time_step.rs:126-178
+    static float isolated_limit(const Params &q, bool fluid, float det, float dx) {
+        if (!fluid) {
+            const float xi = 3.f / dx / dx;
+            return std::sqrt(q.mass / (q.initial_volume * xi * (1.f - 1.f / 2.f) * (q.mu + 3.f / 2.f * q.lambda)));
+        }
+        const float rho0 = q.mass / q.initial_volume;
+        const float first = q.bulk_modulus * (1.f - 1.f / powi<float>(det, q.exponent));
+        if (std::fabs(det - 1.f) > 1e-5f) return dx / det * std::sqrt(rho0 * (det - 1.f) / (6.f * first * 3.f));
+        const float second = (float)q.exponent * q.bulk_modulus / powi<float>(det, q.exponent + 1);
+        return dx * std::sqrt(rho0 / (6.f * second * 3.f));
+    }
+
+    // limit_time_step.rs:25-33.  Non-finite candidates are skipped (the
+    // reference's total_cmp would order a NaN first).
+    void limit_time_step_before_force() {
+        const float dxf = (float)dx;
+        float sound = std::numeric_limits<float>::max(), iso = sound;
+        bool any = false;
+        for (size_t p = 0; p < n; ++p) {
+            if (flags[p] & TOMBSTONED) continue;
+            any = true;
+            const bool fluid = (flags[p] & IS_FLUID) != 0;
+            const V3<T> sv = singular_values(F[p]);
+            const float s[3] = {(float)sv[0], (float)sv[1], (float)sv[2]};
+            const float a = sound_speed_limit(params[p], fluid, s, dxf);
+            const float b = isolated_limit(params[p], fluid, (float)det(F[p]), dxf);
+            if (std::isfinite(a) && a > 0) sound = std::min(sound, a);
+            if (std::isfinite(b) && b > 0) iso = std::min(iso, b);
+        }
+        ad.has_sound = any && sound < std::numeric_limits<float>::max(), ad.sound = sound;
+        ad.has_iso = any && iso < std::numeric_limits<float>::max(), ad.iso = iso;
+        ad.push();
+    }
+
+    // limit_time_step.rs:181-222
+    void limit_time_step_before_integrate() {
+        float max_vel = 0, max_c = 0;
+        bool any = false;
+        for (size_t p = 0; p < n; ++p) {
+            if (flags[p] & TOMBSTONED) continue;
+            any = true;
+            const float vx = (float)v[p][0], vy = (float)v[p][1], vz = (float)v[p][2];
+            max_vel = std::max(max_vel, std::sqrt(vx * vx + vy * vy + vz * vz));
+            for (int k = 0; k < 9; ++k) max_c = std::max(max_c, std::fabs((float)C[p].m[k]));
+        }
+        ad.has_vel = any && max_vel != 0.f, ad.vel = ad.has_vel ? 0.5f * (float)dx / max_vel : 0.f;
+        ad.has_def = any, ad.def = 0.2f / std::max(max_c, 1e-8f);
+        ad.push();
+    }
+
+    // cpu/src/cpu_state.rs:146-197 with adaptive_time_steps = true and the
+    // phase order of cpu/src/phase/mod.rs:27-41.  Returns 1 on an energy
+    // error (time not advanced for that substep), 2 on a zero time step.
+    int step_adaptive(double *time, double target, float max_dt, const float g_f[3], uint32_t *substeps,
+                      float limits[8]) override {
+        ad.max_dt = max_dt;
+        const V3<T> g = v3<T>((T)g_f[0], (T)g_f[1], (T)g_f[2]);
+        uint32_t done = 0;
+        int rc = 0;
+        float dt_a = 0, dt_b = 0, dt_c = 0;
+        while (*time < target) {
+            if (ad.allowed() == 0.f) {
+                rc = 2;
+                break;
+            }
+            sort();
+            dt_a = ad.allowed();
+            external_force((T)dt_a, g);
+            update_grid_nodes();
+            limit_time_step_before_force();
+            dt_b = ad.allowed();
+            scatter_momentum((T)dt_b);
+            meld_grid();
+            collect_velocity();
+            limit_time_step_before_integrate();
+            dt_c = ad.allowed();
+            if (advance_particles((T)dt_c) > 0) {
+                rc = 1;
+                ++done;
+                break;
+            }
+            cull_particles();
+            *time += (double)ad.allowed();
+            ++done;
+        }
+        if (substeps) *substeps = done;
+        if (limits) {
+            const float big = std::numeric_limits<float>::max();
+            limits[0] = dt_a, limits[1] = dt_b, limits[2] = dt_c;
+            limits[3] = ad.has_vel ? ad.vel : big, limits[4] = ad.has_def ? ad.def : big;
+            limits[5] = ad.has_sound ? ad.sound : big, limits[6] = ad.has_iso ? ad.iso : big;
+            limits[7] = ad.allowed();
+        }
+        return rc;
+    }
+
     void p2g_only(float dt_f, const float g_f[3]) override {
         T dt = (T)dt_f;
         V3<T> g = v3<T>((T)g_f[0], (T)g_f[1], (T)g_f[2]);
@@ -992,6 +1171,10 @@ void *svo_create(const svo_particles *p, const svo_consts *c, int fp64, int thre
 }
 void svo_destroy(void *s) { delete static_cast<Base *>(s); }
 int svo_step(void *s, uint32_t n, float dt, const float g[3]) { return static_cast<Base *>(s)->step(n, dt, g); }
+int svo_step_adaptive(void *s, double *time, double target, float max_dt, const float g[3], uint32_t *substeps,
+                      float limits[8]) {
+    return static_cast<Base *>(s)->step_adaptive(time, target, max_dt, g, substeps, limits);
+}
 void svo_download(void *s, svo_particles *out) { static_cast<Base *>(s)->download(out); }
 uint64_t svo_grid(void *s, int32_t *ids, float *m, float *v, uint64_t cap) {
     return static_cast<Base *>(s)->grid(ids, m, v, cap);

@@ -93,6 +93,13 @@ void svo_destroy(void *s);
  * (adaptive_time_steps = false).  Returns 0, or 1 when an energy error stopped
  * the run early (a particle got FAILED, advance_particles.rs:73-74). */
 int svo_step(void *s, uint32_t n_substeps, float dt, const float gravity[3]);
+/* Adaptive substeps while *time < target (cpu_state.rs:146-197 with
+ * adaptive_time_steps = true); returns 0, 1 on an energy error, 2 on a zero
+ * time step.  limits: the last substep's dt of external force, scatter and
+ * advance, then the velocity, deformation, sound and isolated limits and the
+ * allowed step (FLT_MAX = none). */
+int svo_step_adaptive(void *s, double *time, double target, float max_dt, const float gravity[3],
+                      uint32_t *substeps, float limits[8]);
 /* Writes the state back in the caller's original particle order
  * (cpu_state.rs:71-135 to_io_state). */
 void svo_download(void *s, svo_particles *out);

@@ -119,6 +119,9 @@ _SIGNATURES = {
     "sv_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(SvStats)]),
     "sv_set_stream": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "sv_set_graphs": (ct.c_int, [ct.c_void_p, ct.c_int]),
+    "sv_step_adaptive": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_double), ct.c_double, ct.c_float, f32p,
+                                    ct.POINTER(ct.c_int32), u32p, u32p]),
+    "sv_time_step_limits": (ct.c_int, [ct.c_void_p, f32p]),
     "sv_autotune": (ct.c_int, [ct.c_void_p, ct.c_float, f32p, ct.c_uint32, u32p, u32p]),
     "sv_set_profiling": (ct.c_int, [ct.c_void_p, ct.c_int]),
     "sv_profile_report": (ct.c_int, [ct.c_void_p, ct.c_char_p, ct.c_uint64]),

@@ -10,6 +10,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "sv_adaptive.cuh"
 #include "sv_internal.h"
 #include "sv_sort.cuh"
 
@@ -58,6 +59,7 @@ void free_handle(sv_handle *h) {
     for (auto &kv : h->graphs)
         if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     free_closure(h);
+    cudaFree(h->adt);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
 }
@@ -670,6 +672,140 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
     h->fp64_total += (uint32_t)(h->host_counters[C_FP64] - fp64_before);
     if (status_out) *status_out = status;
     if (substeps_done) *substeps_done = done;
+    return 0;
+}
+
+// ------------------------------------------------------------------ adaptive time steps
+// CpuState::produce_next_state with adaptive_time_steps = true
+// (cpu_state.rs:146-197): substeps run while time < target_time, each with
+// the phase order of phase/mod.rs:27-41.  The limits need reductions over
+// all particles between the gather and the advance, so the substep is not
+// fused: binning, limits before force, P2G, grid update, G2P, limits before
+// integrate, advance.  The time steps live on the device; a substep that
+// starts at or after the target time is a no-op (stop latch).
+namespace {
+
+int adaptive_substep(sv_handle *h, float3 g) {
+    if (!h->keys_valid) SV_CUDA(launch_keys(h));
+    SV_CUDA(launch_sort_and_segments(h));
+    const int which = h->map_cur ^ 1;
+    SV_CUDA(launch_activate(h, which));
+    h->map_cur = h->map_next = which;
+    SV_CUDA(launch_limits_force(h));
+    SV_CUDA(launch_clear(h, h->gcur, which));
+    SV_CUDA(launch_p2g(h, 0.f, g));
+    SV_CUDA(launch_grid_update(h, false));
+    SV_CUDA(launch_g2p_only(h));
+    SV_CUDA(launch_advance(h));
+    return 0;
+}
+
+}  // namespace
+
+int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float max_time_step,
+                     const float gravity[3], const volatile int32_t *cancel, uint32_t *status_out,
+                     uint32_t *substeps_done) {
+    g_last_error.clear();
+    if (!h || !time_inout) return fail("sv_step_adaptive: NULL argument");
+    if (status_out) *status_out = 0;
+    if (substeps_done) *substeps_done = 0;
+    if (!(max_time_step > 0.f)) return fail("sv_step_adaptive: max_time_step must be positive");
+    float3 g = gravity ? make_float3(gravity[0], gravity[1], gravity[2]) : make_float3(0.f, 0.f, 0.f);
+    adaptive::State st;
+    if (!h->adt) {
+        SV_CUDA(cudaMalloc(&h->adt, sizeof(adaptive::State)));
+        std::memset(&st, 0, sizeof(st));
+        st.vel = st.def = st.sound = st.iso = adaptive::NONE;
+        st.hist_len = 0;
+    } else {
+        SV_CUDA(cudaMemcpyAsync(&st, h->adt, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+        SV_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    st.max_dt = max_time_step;  // cpu_state.rs:162
+    st.time = *time_inout;
+    st.target = target_time;
+    st.red_sound = st.red_iso = 0x7f7fffffu;  // FLT_MAX bits
+    SV_CUDA(cudaMemcpyAsync(h->adt, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
+    if (read_counters(h)) return -1;
+    h->host_counters[C_STATUS] &= ~(ST_INVERTED | ST_TIME_REACHED | ST_ZERO_DT);
+    SV_CUDA(cudaMemcpyAsync(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice, h->stream));
+    // the fused path's pending scatter and binning do not survive this call
+    h->pending_valid = false;
+    h->keys_valid = false;
+    h->since_sort = h->sort_interval;
+    if (!(st.time < target_time)) return 0;
+    const uint32_t base = h->host_counters[C_SUBSTEPS];
+    uint32_t status = 0;
+    h->adaptive_active = true;
+    int rc = 0;
+    while (true) {
+        if (cancel && *cancel) {
+            status |= SV_STATUS_CANCELED;
+            break;
+        }
+        for (int s = 0; s < 16 && rc == 0; ++s) rc = adaptive_substep(h, g);
+        if (rc || read_counters(h)) {
+            rc = -1;
+            break;
+        }
+        const uint32_t stw = h->host_counters[C_STATUS];
+        if (stw & ST_OUT_OF_GRID) {
+            rc = fail("sv_step_adaptive: a live particle left the grid block index");
+            break;
+        }
+        if (stw & ST_ZERO_DT) {
+            rc = fail("sv_step_adaptive: zero time step");  // Error::ZeroTimeStep
+            break;
+        }
+        if (stw & (STOP_MASK & ~ST_TIME_REACHED)) h->keys_valid = false;  // stopped advances copied in place
+        if (stw & ST_CAPACITY) {
+            const uint64_t cap = std::min<uint64_t>(h->layout.total_blocks, h->capacity * 2);
+            if (cap <= h->capacity) {
+                rc = fail("sv_step_adaptive: grid block capacity exhausted");
+                break;
+            }
+            if (alloc_grid(h, cap) != cudaSuccess) {
+                rc = fail("sv_step_adaptive: grid allocation failed");
+                break;
+            }
+            clear_graphs(h);
+            h->host_counters[C_STATUS] &= ~ST_CAPACITY;
+            SV_CUDA(cudaMemcpyAsync(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice,
+                                    h->stream));
+            continue;
+        }
+        if (stw & ST_INVERTED) {
+            status |= SV_STATUS_PARTICLE_INVERTED;
+            break;
+        }
+        if (stw & ST_TIME_REACHED) break;
+    }
+    h->adaptive_active = false;
+    h->keys_valid = false;
+    if (rc) return -1;
+    SV_CUDA(cudaMemcpyAsync(&st, h->adt, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+    SV_CUDA(cudaStreamSynchronize(h->stream));
+    h->host_counters[C_STATUS] &= ~ST_TIME_REACHED;
+    SV_CUDA(cudaMemcpy(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice));
+    const uint32_t done = h->host_counters[C_SUBSTEPS] - base;
+    h->substeps_total += done;
+    *time_inout = st.time;
+    if (status_out) *status_out = status;
+    if (substeps_done) *substeps_done = done;
+    return 0;
+}
+
+int sv_time_step_limits(sv_handle *h, float out[8]) {
+    g_last_error.clear();
+    if (!h || !out) return fail("sv_time_step_limits: NULL argument");
+    for (int k = 0; k < 8; ++k) out[k] = adaptive::NONE;
+    if (!h->adt) return 0;
+    adaptive::State st;
+    SV_CUDA(cudaMemcpyAsync(&st, h->adt, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+    SV_CUDA(cudaStreamSynchronize(h->stream));
+    out[0] = st.dt_a, out[1] = st.dt_b, out[2] = st.dt_c;
+    out[3] = st.vel, out[4] = st.def, out[5] = st.sound, out[6] = st.iso;
+    out[7] = adaptive::allowed(st);
     return 0;
 }
 

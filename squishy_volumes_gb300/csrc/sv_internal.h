@@ -27,7 +27,9 @@ constexpr uint32_t ST_CAPACITY = SV_STATUS_CAPACITY_EXCEEDED;
 constexpr uint32_t ST_INVERTED = SV_STATUS_PARTICLE_INVERTED;
 constexpr uint32_t ST_OUT_OF_GRID = 1u << 4;  // a live particle left the block index
 constexpr uint32_t ST_MOVED_FAR = 1u << 5;    // a particle left the blocks claimed at binning
-constexpr uint32_t STOP_MASK = ST_CAPACITY | ST_INVERTED | ST_OUT_OF_GRID | ST_MOVED_FAR;
+constexpr uint32_t ST_TIME_REACHED = 1u << 6; // adaptive steps: the target time is reached
+constexpr uint32_t ST_ZERO_DT = 1u << 7;      // adaptive steps: the allowed time step is 0
+constexpr uint32_t STOP_MASK = ST_CAPACITY | ST_INVERTED | ST_OUT_OF_GRID | ST_MOVED_FAR | ST_TIME_REACHED | ST_ZERO_DT;
 
 // Device counters (one array so one copy reads them all).
 enum Counter : int {
@@ -173,6 +175,11 @@ struct sv_handle {
     bool use_graphs = true;
     uint64_t graph_launches = 0;  // graph replays issued
 
+    // Adaptive time steps (adaptive::State in device memory, sv_adaptive.cuh);
+    // adaptive_active while sv_step_adaptive runs.
+    void *adt = nullptr;
+    bool adaptive_active = false;
+
     // Learned stress closure of snow and sand (sv_closure.cu).
     int closure_mode = 0;  // 0 return maps (SVD), 1 learned closure
     bool cl_trained = false;
@@ -201,6 +208,10 @@ cudaError_t launch_clear(sv_handle *h, int grid_side, int which);
 cudaError_t launch_p2g(sv_handle *h, float dt, float3 gravity);
 cudaError_t launch_grid_update(sv_handle *h, bool clear_next);
 cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 gravity, bool write_keys, bool use_perm);
+// adaptive time steps (the unfused substep)
+cudaError_t launch_limits_force(sv_handle *h);
+cudaError_t launch_g2p_only(sv_handle *h);
+cudaError_t launch_advance(sv_handle *h);
 
 // Per-kernel timing hooks.
 void timer_begin(sv_handle *h, const char *name, cudaEvent_t *start);

@@ -31,6 +31,7 @@
 
 #include <type_traits>
 
+#include "sv_adaptive.cuh"
 #include "sv_closure.cuh"
 #include "sv_internal.h"
 #include "sv_mlp.cuh"
@@ -56,8 +57,10 @@ struct Rec {
     float4 p[9];
 };
 
-// MODE_G2P2G_LEARNED is MODE_G2P2G with the learned closure for snow and sand.
-enum Mode { MODE_P2G = 0, MODE_G2P2G = 1, MODE_G2P2G_LEARNED = 2 };
+// MODE_G2P2G_LEARNED is MODE_G2P2G with the learned closure for snow and
+// sand.  Adaptive time steps split the fused pass: MODE_G2P_ONLY gathers v
+// and C (written back in place), MODE_ADVANCE advances from them.
+enum Mode { MODE_P2G = 0, MODE_G2P2G = 1, MODE_G2P2G_LEARNED = 2, MODE_G2P_ONLY = 3, MODE_ADVANCE = 4 };
 
 struct StepArgs {
     ParticleArrays in, out;
@@ -74,6 +77,7 @@ struct StepArgs {
     uint32_t *keys_out;  // nullptr: keys not needed after this substep
     const uint8_t *closure_img;          // packed network weights (learned mode)
     const closure::Hull *closure_hull;   // training hull of the features (learned mode)
+    adaptive::State *adt;                // adaptive time steps: device dt and reductions (else nullptr)
     uint64_t n;
     GridLayout L;
     float dt;
@@ -589,8 +593,13 @@ static_assert(sizeof(Rec) * PT >= tc::NIN * PT * 2 + tc::NH * PT * 2, "closure o
 // learned-closure variant holds the network image as well: four CTAs.
 template <bool CELL, int MODE>
 __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_particles(StepArgs A) {
-    constexpr bool G2P = MODE != MODE_P2G;
     constexpr bool LEARNED = MODE == MODE_G2P2G_LEARNED;
+    // what the pass does: gather from the grid, advance the particles (and
+    // write them out in sorted order), scatter into the next grid
+    constexpr bool GATHER = MODE == MODE_G2P2G || LEARNED || MODE == MODE_G2P_ONLY;
+    constexpr bool G2P = MODE == MODE_G2P2G || LEARNED || MODE == MODE_ADVANCE;  // advances
+    constexpr bool SCATTER = MODE == MODE_P2G || MODE == MODE_G2P2G || LEARNED;
+    constexpr bool LOAD_VC = MODE == MODE_P2G || MODE == MODE_ADVANCE;  // v and C from the state
     __shared__ Shared sh;
     __shared__ typename std::conditional<LEARNED, SharedLearned, int>::type shl;
     if (stopped(A.counters)) {
@@ -613,6 +622,12 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
     const uint32_t nseg = A.counters[C_NSEG];
     const uint32_t nlive = A.counters[C_NLIVE];
     const float dx = A.L.dx;
+    // time steps of the external force, the scatter and the advance: one dt,
+    // or the three of the adaptive state's phases
+    float dt_force = A.dt, dt_scatter = A.dt, dt_adv = A.dt;
+    if (A.adt) dt_force = A.adt->dt_a, dt_scatter = A.adt->dt_b, dt_adv = A.adt->dt_c;
+    float red_v = 0.f, red_c = 0.f;  // G2P_ONLY: max |v| and max |C_ij| of live particles
+    bool red_live = false;
     if (G2P) {
         // particles that were tombstoned at binning time are carried over
         for (uint64_t i = nlive + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -630,11 +645,12 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
         if (threadIdx.x < 27) {
             const uint32_t nbk = neighbour27(b, threadIdx.x, A.L);
             sh.slot_next[threadIdx.x] = A.map_next[nbk];
-            if (G2P) sh.slot_cur[threadIdx.x] = A.map_cur[nbk];
+            if (GATHER) sh.slot_cur[threadIdx.x] = A.map_cur[nbk];
         }
-        for (int t = threadIdx.x; t < 4 * PLANE; t += PT) (&sh.pt[0][0])[t] = 0.f;
+        if (SCATTER)
+            for (int t = threadIdx.x; t < 4 * PLANE; t += PT) (&sh.pt[0][0])[t] = 0.f;
         __syncthreads();
-        if (G2P) {
+        if (GATHER) {
             for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
                 const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
                 const int32_t slot = sh.slot_cur[tile_neighbour(tx, ty, tz)];
@@ -668,14 +684,14 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
                 } else {
                     work = true;
                     const uint32_t kind = A.mats[packed >> MATERIAL_SHIFT].kind;
-                    load_mat9(A.in.F, A.n, p, F);
-                    if (MODE == MODE_P2G) {
+                    if (MODE != MODE_G2P_ONLY) load_mat9(A.in.F, A.n, p, F);
+                    if (LOAD_VC) {
                         load_mat9(A.in.C, A.n, p, C);
                         const float4 vel = A.in.vel[p];
                         v[0] = vel.x, v[1] = vel.y, v[2] = vel.z;
                         plastic_j = vel.w;
                     } else {
-                        plastic_j = kind == KIND_SNOW ? A.in.vel[p].w : 1.f;
+                        plastic_j = (kind == KIND_SNOW || MODE == MODE_G2P_ONLY) ? A.in.vel[p].w : 1.f;
                         // ---- G2P (collect_velocity.rs:40-72)
                         int base[3];
                         float fx[3];
@@ -700,16 +716,28 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
                         const float cscale = 4.f / dx / dx;
 #pragma unroll
                         for (int k = 0; k < 9; ++k) C.a[k] *= cscale;
+                    }
+                    if constexpr (MODE == MODE_G2P_ONLY) {
+                        // v and C back into the state, in place; the limits of
+                        // limit_time_step.rs:189-222 reduce over them
+                        A.in.vel[p] = make_float4(v[0], v[1], v[2], plastic_j);
+                        store_mat9(A.in.C, A.n, p, C);
+                        red_v = fmaxf(red_v, sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+#pragma unroll
+                        for (int k = 0; k < 9; ++k) red_c = fmaxf(red_c, fabsf(C.a[k]));
+                        red_live = true;
+                    }
+                    if (G2P) {
                         // ---- advance (advance_particles.rs:39-41): x += v dt, F += C F dt
                         {
                             const m3f CF = mat_mul(C, F);
 #pragma unroll
-                            for (int k = 0; k < 9; ++k) F.a[k] += CF.a[k] * A.dt;
+                            for (int k = 0; k < 9; ++k) F.a[k] += CF.a[k] * dt_adv;
                         }
                         if (!CELL) {
-                            pos.x += v[0] * A.dt, pos.y += v[1] * A.dt, pos.z += v[2] * A.dt;
+                            pos.x += v[0] * dt_adv, pos.y += v[1] * dt_adv, pos.z += v[2] * dt_adv;
                         } else {
-                            float o[3] = {pos.x + v[0] * A.dt / dx, pos.y + v[1] * A.dt / dx, pos.z + v[2] * A.dt / dx};
+                            float o[3] = {pos.x + v[0] * dt_adv / dx, pos.y + v[1] * dt_adv / dx, pos.z + v[2] * dt_adv / dx};
                             int ci[3] = {cell.x, cell.y, cell.z};
 #pragma unroll
                             for (int k = 0; k < 3; ++k) {
@@ -745,7 +773,7 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
                     learned = want && ok;
                 }
             }
-            if (work) {
+            if (work && (G2P || SCATTER)) {
                 const Material mat = A.mats[packed >> MATERIAL_SHIFT];
                 const uint32_t kind = mat.kind;
                 // ---- SVD, plasticity (advance_particles.rs:42-86), energy
@@ -874,39 +902,57 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
                     }
                     A.keys_out[i] = key;
                 }
-                if (alive) {
+                if (SCATTER && alive) {
                     // ---- scatter record of the next substep: external force
                     // (external_force.rs:17-50) then the momentum of
                     // scatter_momentum.rs:38-90
-                    v[0] += A.dt * A.gravity.x, v[1] += A.dt * A.gravity.y, v[2] += A.dt * A.gravity.z;
+                    v[0] += dt_force * A.gravity.x, v[1] += dt_force * A.gravity.y, v[2] += dt_force * A.gravity.z;
                     const m3f PFt = use_l ? tau_l : stress_times_ft(mat, F, J, U, S, hard);
-                    make_record(mat, C, PFt, J, v, nfx, dx, A.dt, sh.rec[threadIdx.x]);
+                    make_record(mat, C, PFt, J, v, nfx, dx, dt_scatter, sh.rec[threadIdx.x]);
                     rmass = mat.mass;
                     int4 gb;
                     rcell = tile_cell(nbase, org, gb);
                     if (rcell == REC_GLOBAL) sh.gbase[threadIdx.x] = gb;
                 }
             }
-            sh.meta[threadIdx.x] = make_float2(__uint_as_float(rcell), rmass);
-            // Warp w replays only its own threads' records, so warp barriers
-            // would do here; measured 2 % slower than keeping the CTA's
-            // warps in step, so the CTA barriers stay.
-            __syncthreads();
-            scatter_records(sh, count, A);
-            __syncthreads();
-        }
-        // flush the tile of grid_next
-        for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
-            const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
-            const int s = tx * PX + ty * PY + tz;
-            const float m = sh.pt[0][s], px = sh.pt[1][s], py = sh.pt[2][s], pz = sh.pt[3][s];
-            if (m != 0.f || px != 0.f || py != 0.f || pz != 0.f) {
-                const int32_t slot = sh.slot_next[tile_neighbour(tx, ty, tz)];
-                if (slot >= 0) atomicAdd(&A.grid_next[(uint64_t)slot * 64 + tile_local(tx, ty, tz)], make_float4(px, py, pz, m));
-                else atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR);
+            if (SCATTER) {
+                sh.meta[threadIdx.x] = make_float2(__uint_as_float(rcell), rmass);
+                // Warp w replays only its own threads' records, so warp
+                // barriers would do here; measured 2 % slower than keeping the
+                // CTA's warps in step, so the CTA barriers stay.
+                __syncthreads();
+                scatter_records(sh, count, A);
+                __syncthreads();
             }
         }
+        // flush the tile of grid_next
+        if (SCATTER)
+            for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
+                const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
+                const int s = tx * PX + ty * PY + tz;
+                const float m = sh.pt[0][s], px = sh.pt[1][s], py = sh.pt[2][s], pz = sh.pt[3][s];
+                if (m != 0.f || px != 0.f || py != 0.f || pz != 0.f) {
+                    const int32_t slot = sh.slot_next[tile_neighbour(tx, ty, tz)];
+                    if (slot >= 0)
+                        atomicAdd(&A.grid_next[(uint64_t)slot * 64 + tile_local(tx, ty, tz)], make_float4(px, py, pz, m));
+                    else
+                        atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR);
+                }
+            }
         __syncthreads();
+    }
+    if constexpr (MODE == MODE_G2P_ONLY) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            red_v = fmaxf(red_v, __shfl_xor_sync(0xffffffffu, red_v, o));
+            red_c = fmaxf(red_c, __shfl_xor_sync(0xffffffffu, red_c, o));
+        }
+        const bool any = __any_sync(0xffffffffu, red_live);
+        if ((threadIdx.x & 31) == 0 && any) {
+            atomicMax(&A.adt->red_max_v, __float_as_uint(red_v));
+            atomicMax(&A.adt->red_max_c, __float_as_uint(red_c));
+            atomicOr(&A.adt->red_live, 1u);
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -928,6 +974,84 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
 
 __global__ void k_finish(uint32_t *counters) {
     if (!counters[C_STOP]) counters[C_SUBSTEPS] += 1;
+}
+
+// ------------------------------------------------------------------ adaptive time steps
+// limit_time_step.rs:25-33 (LimitTimeStepBeforeForce): the sound-speed and
+// isolated-particle limits over the live particles' current F, reduced as
+// float bits (positive values order like their bits).
+__global__ void __launch_bounds__(ELEM_THREADS)
+    k_limits_force(ParticleArrays s, const Material *mats, uint64_t n, float dx, adaptive::State *st,
+                   const uint32_t *counters) {
+    if (stopped(counters)) return;
+    float ls = adaptive::NONE, li = adaptive::NONE;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t packed = __float_as_uint(s.pos[i].w);
+        if (packed & SV_TOMBSTONED) continue;
+        const Material m = mats[packed >> MATERIAL_SHIFT];
+        m3f F, U, V;
+        load_mat9(s.F, n, i, F);
+        float S[3];
+        uint32_t dummy = 0;
+        particle_svd(F, U, S, V, 0, dummy);
+        // descending, as the reference's SVD returns them
+        if (S[0] < S[1]) { const float t = S[0]; S[0] = S[1], S[1] = t; }
+        if (S[1] < S[2]) { const float t = S[1]; S[1] = S[2], S[2] = t; }
+        if (S[0] < S[1]) { const float t = S[0]; S[0] = S[1], S[1] = t; }
+        const bool fluid = m.kind == KIND_FLUID;
+        const float a = adaptive::sound_limit<float>(fluid, m.mu, m.lambda, m.bulk_modulus, m.exponent, m.mass,
+                                                     m.initial_volume, S, dx);
+        const float b = adaptive::isolated_limit<float>(fluid, m.mu, m.lambda, m.bulk_modulus, m.exponent, m.mass,
+                                                        m.initial_volume, det3(F), dx);
+        if (a > 0.f && a < adaptive::NONE) ls = fminf(ls, a);
+        if (b > 0.f && b < adaptive::NONE) li = fminf(li, b);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ls = fminf(ls, __shfl_xor_sync(0xffffffffu, ls, o));
+        li = fminf(li, __shfl_xor_sync(0xffffffffu, li, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (ls < adaptive::NONE) atomicMin(&st->red_sound, __float_as_uint(ls));
+        if (li < adaptive::NONE) atomicMin(&st->red_iso, __float_as_uint(li));
+    }
+}
+
+// ExternalForce takes the step allowed before LimitTimeStepBeforeForce
+// pushes its limits; ScatterMomentum the one after (limit_time_step.rs:25-33,
+// adaptive_time_step_state.rs:35-63).
+__global__ void k_dt_force(adaptive::State *st, uint32_t *counters) {
+    if (counters[C_STOP]) return;
+    st->dt_a = adaptive::allowed(*st);
+    st->sound = __uint_as_float(st->red_sound);
+    st->iso = __uint_as_float(st->red_iso);
+    adaptive::push(*st);
+    st->dt_b = adaptive::allowed(*st);
+    st->red_max_v = 0u, st->red_max_c = 0u, st->red_live = 0u;
+    if (!(st->dt_a > 0.f) || !(st->dt_b > 0.f)) counters[C_STATUS] |= ST_ZERO_DT;
+}
+
+// limit_time_step.rs:181-222 (LimitTimeStepBeforeIntegrate) from the
+// reductions of the G2P pass; AdvanceParticles takes the step after the push.
+__global__ void k_dt_integrate(adaptive::State *st, uint32_t *counters, float dx) {
+    if (counters[C_STOP]) return;
+    const float mv = __uint_as_float(st->red_max_v), mc = __uint_as_float(st->red_max_c);
+    st->vel = mv != 0.f ? 0.5f * dx / mv : adaptive::NONE;
+    st->def = st->red_live ? 0.2f / fmaxf(mc, 1e-8f) : adaptive::NONE;
+    adaptive::push(*st);
+    st->dt_c = adaptive::allowed(*st);
+    st->red_sound = __float_as_uint(adaptive::NONE), st->red_iso = __float_as_uint(adaptive::NONE);
+    if (!(st->dt_c > 0.f)) counters[C_STATUS] |= ST_ZERO_DT;
+}
+
+// cpu_state.rs:186-189: the substep's time step is added to the time; the
+// run stops (ST_TIME_REACHED latches) once the target time is reached.
+__global__ void k_adaptive_finish(adaptive::State *st, uint32_t *counters) {
+    if (counters[C_STOP] || (counters[C_STATUS] & STOP_MASK)) return;
+    st->time += (double)st->dt_c;
+    st->substeps += 1;
+    counters[C_SUBSTEPS] += 1;
+    if (st->time >= st->target) counters[C_STATUS] |= ST_TIME_REACHED;
 }
 
 unsigned elem_blocks(uint64_t work) {
@@ -962,6 +1086,7 @@ StepArgs make_args(sv_handle *h, float dt, float3 g) {
     A.keys_out = h->keys;
     A.closure_img = nullptr;
     A.closure_hull = nullptr;
+    A.adt = nullptr;
     A.n = h->n;
     A.L = h->layout;
     A.dt = dt;
@@ -1039,11 +1164,49 @@ cudaError_t launch_clear(sv_handle *h, int grid_side, int which) {
     return cudaGetLastError();
 }
 
+cudaError_t launch_limits_force(sv_handle *h) {
+    Scoped s(h, "limits_force");
+    auto *st = reinterpret_cast<adaptive::State *>(h->adt);
+    k_limits_force<<<elem_blocks(h->n), ELEM_THREADS, 0, h->stream>>>(h->side[h->cur], h->materials, h->n,
+                                                                       h->layout.dx, st, h->counters);
+    k_dt_force<<<1, 1, 0, h->stream>>>(st, h->counters);
+    h->launches += 2;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_g2p_only(sv_handle *h) {
+    StepArgs A = make_args(h, 0.f, make_float3(0.f, 0.f, 0.f));
+    A.adt = reinterpret_cast<adaptive::State *>(h->adt);
+    A.keys_out = nullptr;
+    Scoped s(h, "g2p");
+    if (h->layout.position_form) k_particles<true, MODE_G2P_ONLY><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    else k_particles<false, MODE_G2P_ONLY><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    k_dt_integrate<<<1, 1, 0, h->stream>>>(A.adt, h->counters, h->layout.dx);
+    h->launches += 2;
+    h->vel_side = h->gcur;
+    h->vel_map = h->map_cur;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advance(sv_handle *h) {
+    StepArgs A = make_args(h, 0.f, make_float3(0.f, 0.f, 0.f));
+    A.adt = reinterpret_cast<adaptive::State *>(h->adt);
+    Scoped s(h, "advance");
+    if (h->layout.position_form) k_particles<true, MODE_ADVANCE><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    else k_particles<false, MODE_ADVANCE><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    k_adaptive_finish<<<1, 1, 0, h->stream>>>(A.adt, h->counters);
+    h->launches += 2;
+    h->cur ^= 1;
+    h->keys_valid = true;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_p2g(sv_handle *h, float dt, float3 g) {
     StepArgs A = make_args(h, dt, g);
     A.map_next = h->blockmap[h->map_cur];
     A.grid_next = h->grid[h->gcur];
     A.keys_out = nullptr;
+    if (h->adaptive_active) A.adt = reinterpret_cast<adaptive::State *>(h->adt);
     Scoped s(h, "p2g");
     if (h->layout.position_form) k_particles<true, MODE_P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
     else k_particles<false, MODE_P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);

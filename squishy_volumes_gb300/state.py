@@ -192,8 +192,7 @@ class FrameInput:
 
 @dataclass
 class RunParameters:
-    """CpuRunParameters (cpu_state.rs:137-142).  Only adaptive_time_steps =
-    False is implemented by this backend."""
+    """CpuRunParameters (cpu_state.rs:137-142)."""
 
     target_time: float
     max_time_step: float
@@ -292,13 +291,45 @@ class CudaState:
                                 ct.byref(done)))
         return int(status.value), int(done.value)
 
+    def step_adaptive(self, target_time: float, max_time_step: float, gravity, harness: Optional[Harness] = None,
+                      time: Optional[float] = None):
+        """Adaptive substeps from `time` (default self.time) until target_time;
+        returns (status bits, substeps done, time reached)."""
+        g = np.asarray(gravity, dtype=np.float32)
+        t = ct.c_double(self.time if time is None else time)
+        status = ct.c_uint32(0)
+        done = ct.c_uint32(0)
+        cancel = ct.byref(harness._flag) if harness is not None else None
+        rc = self._lib.sv_step_adaptive(self._h, ct.byref(t), float(target_time), float(max_time_step), ptr(g, f32p),
+                                        cancel, ct.byref(status), ct.byref(done))
+        if rc < 0:
+            msg = self._lib.sv_last_error_string().decode()
+            if "zero time step" in msg:
+                raise ZeroTimeStep("The time step ended up being 0")
+            check(rc)
+        return int(status.value), int(done.value), float(t.value)
+
+    def time_step_limits(self) -> dict:
+        out = np.zeros(8, np.float32)
+        check(self._lib.sv_time_step_limits(self._h, ptr(out, f32p)))
+        keys = ("dt_force", "dt_scatter", "dt_advance", "velocity", "deformation", "sound", "isolated", "allowed")
+        return {k: float(v) for k, v in zip(keys, out)}
+
     def produce_next_state(self, harness: Harness, frame_input: FrameInput, params: RunParameters):
         """cpu_state.rs:146-197: advance to target_time in substeps of
         max_time_step; returns (IoState, error-or-None) where the error is a
         buffered EnergyError (state still valid).  Canceled / ZeroTimeStep
         are raised, like the reference's outer Result."""
         if params.adaptive_time_steps:
-            raise NotImplementedError("adaptive time steps are not part of this backend")
+            status, done, t = self.step_adaptive(params.target_time, params.max_time_step, frame_input.gravity,
+                                                 harness)
+            self.time = t
+            error = None
+            if status & _abi.SV_STATUS_PARTICLE_INVERTED:
+                error = EnergyError("The position gradient has negative determinant")
+            if status & _abi.SV_STATUS_CANCELED:
+                raise Canceled("The computation was canceled")
+            return self.to_io_state(params.store_grid), error
         dt = np.float32(params.max_time_step)
         if dt == 0:
             raise ZeroTimeStep("The time step ended up being 0")

@@ -1,0 +1,106 @@
+"""Adaptive time steps (the reference's limit_time_step.rs and
+AdaptiveTimeStepState) through the C ABI against the fp32 oracle: the same
+number of substeps to the target time, the same time steps per phase, the
+same limits, and the same state within the whole-substep tolerances."""
+
+import numpy as np
+import pytest
+
+from squishy_volumes_gb300 import CudaState, Extras, FrameInput, Harness, IoState, RunParameters, scenes
+from squishy_volumes_gb300._abi import SV_TOMBSTONED, SvError
+
+from test_gpu_parity import compare_states
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"positions": 1e-5, "velocities": 1e-3, "position_gradients": 1e-4, "elastic_energies": 1e-2}
+
+
+def _limits_close(gpu_lim, ref_lim, rel=1e-4):
+    keys = ("dt_force", "dt_scatter", "dt_advance", "velocity", "deformation", "sound", "isolated", "allowed")
+    for k, r in zip(keys, ref_lim):
+        g = gpu_lim[k]
+        assert abs(g - r) <= rel * abs(r), (k, g, r)
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_adaptive_run_matches_oracle(cuda_lib, oracle_mod, form):
+    s = scenes.small_mixed()
+    target, max_dt = 0.02, 1e-2
+    gpu = CudaState.from_io_state(s.io_state, s.consts, Extras(position_form=form))
+    status, done, t = gpu.step_adaptive(target, max_dt, s.gravity, time=0.0)
+    ref = oracle_mod.OracleState(s.io_state.particles, s.consts, None, fp64=False)
+    rc, n_ref, t_ref, lim_ref = ref.step_adaptive(0.0, target, max_dt, s.gravity)
+    assert (status, rc) == (0, 0)
+    assert done == n_ref and done > 3
+    assert abs(t - t_ref) <= 1e-5 * t_ref
+    _limits_close(gpu.time_step_limits(), lim_ref)
+    out, exp = gpu.download(), ref.download()
+    np.testing.assert_array_equal(out.flags, exp.flags)
+    live = (exp.flags & SV_TOMBSTONED) == 0
+    compare_states(out, exp, live, tol=TOL, dx=s.consts.grid_node_size)
+    gpu.close()
+
+
+def test_limit_history_persists_across_calls(cuda_lib, oracle_mod):
+    """Two calls (0 -> 0.01 -> 0.02) against the oracle doing the same: the
+    prior limits carry over, as in the reference's state."""
+    s = scenes.small_mixed()
+    gpu = CudaState.from_io_state(s.io_state, s.consts)
+    ref = oracle_mod.OracleState(s.io_state.particles, s.consts, None, fp64=False)
+    t, tr = 0.0, 0.0
+    for target in (0.01, 0.02):
+        _, done, t = gpu.step_adaptive(target, 1e-2, s.gravity, time=t)
+        _, n_ref, tr, lim_ref = ref.step_adaptive(tr, target, 1e-2, s.gravity)
+        assert done == n_ref
+        assert abs(t - tr) <= 1e-5 * tr
+        _limits_close(gpu.time_step_limits(), lim_ref)
+    gpu.close()
+
+
+def test_velocity_limit_governs_fast_particles(cuda_lib, oracle_mod):
+    """Particles at 40 m/s: 0.5 dx / |v| is the smallest limit."""
+    s = scenes.small_mixed()
+    p = s.io_state.particles.copy()
+    p.velocities[:] = np.array([40.0, 0.0, 0.0], np.float32)
+    p.velocity_gradients[:] = 0
+    gpu = CudaState.from_io_state(IoState(0.0, p), s.consts)
+    ref = oracle_mod.OracleState(p, s.consts, None, fp64=False)
+    _, done, t = gpu.step_adaptive(3e-3, 1e-2, (0, 0, 0), time=0.0)
+    _, n_ref, tr, lim_ref = ref.step_adaptive(0.0, 3e-3, 1e-2, (0, 0, 0))
+    lim = gpu.time_step_limits()
+    assert done == n_ref
+    assert lim["velocity"] < min(lim["sound"], lim["isolated"], lim["deformation"])
+    _limits_close(lim, lim_ref)
+    gpu.close()
+
+
+def test_target_already_reached_runs_nothing(cuda_lib):
+    s = scenes.small_mixed()
+    gpu = CudaState.from_io_state(s.io_state, s.consts)
+    before = gpu.download()
+    assert gpu.step_adaptive(0.5, 1e-2, s.gravity, time=0.5) == (0, 0, 0.5)
+    after = gpu.download()
+    np.testing.assert_array_equal(before.positions, after.positions)
+    with pytest.raises(SvError):
+        gpu.step_adaptive(1.0, 0.0, s.gravity, time=0.0)  # no positive step
+    gpu.close()
+
+
+def test_produce_next_state_adaptive_and_back_to_fixed(cuda_lib, oracle_mod):
+    """produce_next_state with adaptive_time_steps, then fixed steps on the
+    same handle: the fused path picks up the state the adaptive path left."""
+    s = scenes.small_mixed()
+    gpu = CudaState.from_io_state(s.io_state, s.consts)
+    io, err = gpu.produce_next_state(Harness(), FrameInput(s.consts, s.gravity),
+                                     RunParameters(target_time=0.01, max_time_step=1e-2, adaptive_time_steps=True))
+    assert err is None and gpu.time >= 0.01
+    ref = oracle_mod.OracleState(s.io_state.particles, s.consts, None, fp64=False)
+    _, _, tr, _ = ref.step_adaptive(0.0, 0.01, 1e-2, s.gravity)
+    assert abs(gpu.time - tr) <= 1e-5 * tr
+    assert gpu.step(5, 1e-3, s.gravity) == (0, 5)
+    assert ref.step(5, 1e-3, s.gravity) == 0
+    out, exp = gpu.download(), ref.download()
+    live = (exp.flags & SV_TOMBSTONED) == 0
+    compare_states(out, exp, live, tol=TOL, dx=s.consts.grid_node_size)
+    gpu.close()
