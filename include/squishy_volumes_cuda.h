@@ -248,6 +248,49 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
                      uint32_t *substeps_done);
 int sv_time_step_limits(sv_handle *h, float out[8]);
 
+/* ------------------------------------------------------------------ frame input and colliders
+ * The inputs of frames a and b (rust/crates/xpu/src/frame_input.rs:33-65),
+ * interpolated linearly inside the frame at the start of every substep
+ * (rust/crates/cpu/src/phase/interpolate_input.rs:18-106):
+ *   - gravity (replaces the gravity argument of sv_step / sv_step_adaptive);
+ *   - particle goals: a particle whose flags carry HAS_GOAL in both frames
+ *     gets v = (goal - x) / dt instead of gravity (external_force.rs:17-50);
+ *     goal_flags_* [n], goal_positions_* [n][3] in the caller's particle
+ *     order, NULL for no goals;
+ *   - colliders: closed or open triangle meshes, up to 16 (the collider of
+ *     each triangle in triangle_collider), vertices [n_vertices][3] at
+ *     frames a and b, triangles [n_triangles][3], friction and damping per
+ *     triangle.  Every substep runs the reference's Collide
+ *     (rust/crates/cpu/src/phase/collide.rs:21-206) and keeps the grid's
+ *     (node, collider bits) variants apart (update_grid_nodes.rs,
+ *     meld_grid.rs).  leaf_size is the reference's InputConsts::leaf_size.
+ * *_b arrays are ignored when has_b == 0 (frame b = a).  Substeps must start
+ * inside `frame` (time * frames_per_second in [frame, frame + 1)), else
+ * sv_step fails as the reference's WrongFrameLoaded; load the next frame
+ * with another sv_set_frame_input.  NULL removes the frame input.  Not for
+ * batched handles. */
+typedef struct sv_frame_input {
+    uint32_t frames_per_second;
+    uint32_t frame;
+    uint32_t has_b;
+    float gravity_a[3], gravity_b[3];
+    const uint32_t *goal_flags_a, *goal_flags_b;
+    const float *goal_positions_a, *goal_positions_b;
+    uint32_t n_vertices, n_triangles;
+    const uint32_t *triangles;
+    const uint32_t *triangle_collider;
+    const float *vertex_positions_a, *vertex_positions_b;
+    const float *friction_a, *friction_b;
+    const float *damping_a, *damping_b;
+    float leaf_size;
+} sv_frame_input;
+
+int sv_set_frame_input(sv_handle *h, const sv_frame_input *in);
+/* Simulation time of the state (CpuState::time); sv_step advances it by dt
+ * per substep, sv_step_adaptive by its steps. */
+int sv_set_time(sv_handle *h, double time);
+int sv_get_time(sv_handle *h, double *time);
+
 /* Whether sv_step runs whole binning periods as CUDA graphs (default on;
  * off, and while profiling, every kernel is launched directly). */
 int sv_set_graphs(sv_handle *h, int enable);

@@ -61,6 +61,33 @@ class OConsts(ct.Structure):
     ]
 
 
+class OFrameInput(ct.Structure):
+    """svo_frame_input (sv_oracle.h)."""
+
+    _fields_ = [
+        ("frames_per_second", ct.c_uint32),
+        ("frame", ct.c_uint32),
+        ("has_b", ct.c_uint32),
+        ("gravity_a", ct.c_float * 3),
+        ("gravity_b", ct.c_float * 3),
+        ("goal_flags_a", u32p),
+        ("goal_flags_b", u32p),
+        ("goal_positions_a", f32p),
+        ("goal_positions_b", f32p),
+        ("n_vertices", ct.c_uint32),
+        ("n_triangles", ct.c_uint32),
+        ("triangles", u32p),
+        ("triangle_collider", u32p),
+        ("vertex_positions_a", f32p),
+        ("vertex_positions_b", f32p),
+        ("friction_a", f32p),
+        ("friction_b", f32p),
+        ("damping_a", f32p),
+        ("damping_b", f32p),
+        ("leaf_size", ct.c_float),
+    ]
+
+
 def build() -> Path:
     """Builds the oracle with its Makefile (g++ only)."""
     r = subprocess.run(["make", "-C", str(HERE), "-s"], capture_output=True, text=True)
@@ -100,6 +127,9 @@ def lib() -> ct.CDLL:
             "svo_step": (ct.c_int, [ct.c_void_p, ct.c_uint32, ct.c_float, f32p]),
             "svo_step_adaptive": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_double), ct.c_double, ct.c_float, f32p,
                                              u32p, f32p]),
+            "svo_set_frame_input": (ct.c_int, [ct.c_void_p, ct.POINTER(OFrameInput)]),
+            "svo_set_time": (None, [ct.c_void_p, ct.c_double]),
+            "svo_get_time": (ct.c_double, [ct.c_void_p]),
             "svo_download": (None, [ct.c_void_p, ct.POINTER(OParticles)]),
             "svo_grid": (ct.c_uint64, [ct.c_void_p, i32p, f32p, f32p, ct.c_uint64]),
             "svo_p2g_only": (None, [ct.c_void_p, ct.c_float, f32p]),
@@ -249,6 +279,21 @@ class OracleState:
             typ = dict(OParticles._fields_)[name]
             setattr(s, name, _p(arr, typ))
         return s
+
+    def set_frame_input(self, frame):
+        """frame: squishy_volumes_gb300.state.FrameData (its arrays are copied)."""
+        s, keep = frame.to_struct(OFrameInput)
+        rc = lib().svo_set_frame_input(self._h, ct.byref(s))
+        if rc != 0:
+            raise ValueError("invalid frame input")
+
+    @property
+    def time(self):
+        return float(lib().svo_get_time(self._h))
+
+    @time.setter
+    def time(self, t):
+        lib().svo_set_time(self._h, float(t))
 
     def step(self, n, dt, gravity):
         g = np.asarray(gravity, np.float32)

@@ -32,6 +32,7 @@
 #include <cstring>
 #include <deque>
 #include <functional>
+#include <map>
 #include <limits>
 #include <mutex>
 #include <thread>
@@ -507,6 +508,9 @@ inline bool compatible(uint32_t a, uint32_t b) {
 
 struct Base {
     virtual ~Base() {}
+    virtual int set_frame_input(const svo_frame_input *in) = 0;
+    virtual void set_time(double t) = 0;
+    virtual double get_time() const = 0;
     virtual int step(uint32_t n, float dt, const float g[3]) = 0;
     virtual int step_adaptive(double *time, double target, float max_dt, const float g[3], uint32_t *substeps,
                               float limits[8]) = 0;
@@ -603,13 +607,27 @@ template <class T> struct State : Base {
         for (size_t cur = 0; cur < n; ++cur) reverse_sort_map[sort_map[cur]] = (uint32_t)cur;
     }
 
-    // cpu/src/phase/external_force.rs:17-50 (gravity only; goals are not part
-    // of this restatement).
+    // cpu/src/phase/external_force.rs:17-50: gravity, or the velocity that
+    // reaches the interpolated goal in one step when both frames give the
+    // particle a goal.
     void external_force(T dt, const V3<T> &g) {
         pool.run(n, [&](size_t b, size_t e, int) {
-            for (size_t p = b; p < e; ++p)
-                if (!(flags[p] & TOMBSTONED)) v[p] = v[p] + g * dt;
+            for (size_t p = b; p < e; ++p) {
+                if (flags[p] & TOMBSTONED) continue;
+                const uint32_t o = sort_map[p];
+                if (fin.goals && (fin.gflag_a[o] & HAS_GOAL) && (fin.gflag_b[o] & HAS_GOAL)) {
+                    for (int a = 0; a < 3; ++a) v[p][a] = ((T)igoal[3 * o + a] - x[p][a]) / dt;
+                } else {
+                    v[p] = v[p] + g * dt;
+                }
+            }
         });
+    }
+
+    // gravity of the substep: the interpolated input's, else the argument
+    V3<T> substep_gravity(const float g_f[3]) const {
+        if (fin.set) return v3<T>((T)ig[0], (T)ig[1], (T)ig[2]);
+        return v3<T>((T)g_f[0], (T)g_f[1], (T)g_f[2]);
     }
 
     // cpu/src/kernels.rs:46-49 position_to_shift_quadratic.
@@ -865,9 +883,11 @@ template <class T> struct State : Base {
     // have no inputs here: gravity is passed in, there are no colliders).
     int step(uint32_t nsub, float dt_f, const float g_f[3]) override {
         T dt = (T)dt_f;
-        V3<T> g = v3<T>((T)g_f[0], (T)g_f[1], (T)g_f[2]);
         for (uint32_t s = 0; s < nsub; ++s) {
+            if (fin.set && interpolate_input()) return -2;
+            const V3<T> g = substep_gravity(g_f);
             sort();
+            collide(dt);
             external_force(dt, g);
             update_grid_nodes();
             scatter_momentum(dt);
@@ -875,8 +895,355 @@ template <class T> struct State : Base {
             collect_velocity();
             if (advance_particles(dt) > 0) return 1;
             cull_particles();
+            time += (double)dt_f;
         }
         return 0;
+    }
+
+    // ---- frame input (xpu/src/frame_input.rs:33-65) and its interpolation
+    struct FrameIn {
+        bool set = false;
+        uint32_t fps = 24, frame = 0;
+        bool has_b = false;
+        float g_a[3] = {0, 0, 0}, g_b[3] = {0, 0, 0};
+        bool goals = false;
+        std::vector<uint32_t> gflag_a, gflag_b;
+        std::vector<float> goal_a, goal_b;
+        uint32_t nv = 0, nt = 0;
+        std::vector<uint32_t> tri, tri_col;
+        std::vector<float> va, vb, fr_a, fr_b, dm_a, dm_b;
+        float leaf = 1.f;
+        std::vector<uint32_t> opp;                 // mesh_util/src/mesh.rs:71-94: ab, bc, ca neighbours
+        std::vector<std::vector<uint32_t>> vtris;  // mesh.rs:106-135: emptied where the mesh is not closed
+        std::vector<float> vvel;                   // frame_input.rs:329-343 linear_vertex_velocities
+        std::vector<int32_t> lmin, lmax;           // frame_input.rs:345-390 padded leaf boxes
+    } fin;
+    double time = 0;
+    // InterpolatedInput (cpu/src/interpolated_input.rs:12-23)
+    float ig[3] = {0, 0, 0};
+    std::vector<float> igoal, ivpos, ivnorm, itnorm, ifric, idamp;
+
+    float forget_distance() const { return (float)dx * 2.2f; }  // file_input/src/header.rs:60-66
+    float accept_distance() const { return (float)dx * 2.f; }
+
+    void set_time(double t) override { time = t; }
+    double get_time() const override { return time; }
+
+    int set_frame_input(const svo_frame_input *in) override {
+        FrameIn f;
+        f.set = true;
+        f.fps = in->frames_per_second, f.frame = in->frame, f.has_b = in->has_b != 0;
+        for (int a = 0; a < 3; ++a) f.g_a[a] = in->gravity_a[a], f.g_b[a] = f.has_b ? in->gravity_b[a] : in->gravity_a[a];
+        f.goals = in->goal_flags_a && in->goal_positions_a;
+        if (f.goals) {
+            f.gflag_a.assign(in->goal_flags_a, in->goal_flags_a + n);
+            f.goal_a.assign(in->goal_positions_a, in->goal_positions_a + 3 * n);
+            const bool hb = f.has_b && in->goal_flags_b && in->goal_positions_b;
+            f.gflag_b = hb ? std::vector<uint32_t>(in->goal_flags_b, in->goal_flags_b + n) : f.gflag_a;
+            f.goal_b = hb ? std::vector<float>(in->goal_positions_b, in->goal_positions_b + 3 * n) : f.goal_a;
+        }
+        f.nv = in->n_vertices, f.nt = in->n_triangles, f.leaf = in->leaf_size;
+        if (f.nt) {
+            f.tri.assign(in->triangles, in->triangles + 3 * f.nt);
+            f.tri_col.assign(in->triangle_collider, in->triangle_collider + f.nt);
+            f.va.assign(in->vertex_positions_a, in->vertex_positions_a + 3 * f.nv);
+            f.vb = f.has_b ? std::vector<float>(in->vertex_positions_b, in->vertex_positions_b + 3 * f.nv) : f.va;
+            f.fr_a.assign(in->friction_a, in->friction_a + f.nt);
+            f.dm_a.assign(in->damping_a, in->damping_a + f.nt);
+            f.fr_b = f.has_b ? std::vector<float>(in->friction_b, in->friction_b + f.nt) : f.fr_a;
+            f.dm_b = f.has_b ? std::vector<float>(in->damping_b, in->damping_b + f.nt) : f.dm_a;
+            for (uint32_t t = 0; t < f.nt; ++t) {
+                if (f.tri_col[t] >= 16) return -1;
+                for (int k = 0; k < 3; ++k)
+                    if (f.tri[3 * t + k] >= f.nv) return -1;  // mesh.rs:37-47
+            }
+            // edge -> triangles (mesh.rs:49-68), opposites (mesh.rs:71-94)
+            std::map<std::pair<uint32_t, uint32_t>, std::vector<uint32_t>> edges;
+            auto edge = [](uint32_t a, uint32_t b) { return a < b ? std::make_pair(a, b) : std::make_pair(b, a); };
+            for (uint32_t t = 0; t < f.nt; ++t)
+                for (int k = 0; k < 3; ++k) edges[edge(f.tri[3 * t + k], f.tri[3 * t + (k + 1) % 3])].push_back(t);
+            for (auto &e : edges)
+                if (e.second.size() > 2) return -1;  // NonManifoldEdge
+            f.opp.assign(3 * f.nt, 0xFFFFFFFFu);
+            for (uint32_t t = 0; t < f.nt; ++t)
+                for (int k = 0; k < 3; ++k)
+                    for (uint32_t o : edges[edge(f.tri[3 * t + k], f.tri[3 * t + (k + 1) % 3])])
+                        if (o != t) f.opp[3 * t + k] = o;
+            // vertex -> triangles, emptied at vertices whose neighbour counts are not all 2
+            f.vtris.assign(f.nv, {});
+            for (uint32_t t = 0; t < f.nt; ++t)
+                for (int k = 0; k < 3; ++k) f.vtris[f.tri[3 * t + k]].push_back(t);
+            for (uint32_t v = 0; v < f.nv; ++v) {
+                std::map<uint32_t, int> count;
+                for (uint32_t t : f.vtris[v])
+                    for (int k = 0; k < 3; ++k)
+                        if (f.tri[3 * t + k] != v) ++count[f.tri[3 * t + k]];
+                for (auto &c : count)
+                    if (c.second != 2) {
+                        f.vtris[v].clear();
+                        break;
+                    }
+            }
+            f.vvel.assign(3 * f.nv, 0.f);
+            if (f.has_b)
+                for (uint32_t k = 0; k < 3 * f.nv; ++k) f.vvel[k] = (f.vb[k] - f.va[k]) * (float)f.fps;
+            const float margin = forget_distance();
+            f.lmin.resize(3 * f.nt), f.lmax.resize(3 * f.nt);
+            for (uint32_t t = 0; t < f.nt; ++t)
+                for (int a = 0; a < 3; ++a) {
+                    float lo = std::numeric_limits<float>::max(), hi = -lo;
+                    for (int k = 0; k < 3; ++k) {
+                        const uint32_t v = f.tri[3 * t + k];
+                        lo = std::min(lo, f.va[3 * v + a]), hi = std::max(hi, f.va[3 * v + a]);
+                        if (f.has_b) lo = std::min(lo, f.vb[3 * v + a]), hi = std::max(hi, f.vb[3 * v + a]);
+                    }
+                    f.lmin[3 * t + a] = (int32_t)std::floor((lo - margin) / f.leaf);
+                    f.lmax[3 * t + a] = (int32_t)std::ceil((hi + margin) / f.leaf);
+                }
+        }
+        fin = std::move(f);
+        return 0;
+    }
+
+    static void f3_cross(const float a[3], const float b[3], float o[3]) {
+        o[0] = a[1] * b[2] - a[2] * b[1], o[1] = a[2] * b[0] - a[0] * b[2], o[2] = a[0] * b[1] - a[1] * b[0];
+    }
+    static float f3_dot(const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+    static float f3_norm(const float a[3]) { return std::sqrt(f3_dot(a, a)); }
+    // nalgebra try_normalize(1e-5) (util/src/consts.rs:11 NORMALIZATION_EPS), zero on failure
+    static void f3_normalize_or_zero(float a[3]) {
+        const float nn = f3_norm(a);
+        if (nn <= 1e-5f) a[0] = a[1] = a[2] = 0.f;
+        else a[0] /= nn, a[1] /= nn, a[2] /= nn;
+    }
+
+    // cpu/src/phase/interpolate_input.rs:18-106 at the state's time
+    int interpolate_input() {
+        const double ft = time * (double)fin.fps;
+        const double low = std::floor(ft);
+        if ((int64_t)low != (int64_t)fin.frame) return -2;  // xpu frame_input.rs:266-278 WrongFrameLoaded
+        const float fb = (float)std::fmod(ft, 1.0), fa = 1.f - fb;
+        for (int a = 0; a < 3; ++a) ig[a] = fa * fin.g_a[a] + fb * fin.g_b[a];
+        if (fin.goals) {
+            igoal.resize(3 * n);
+            for (size_t k = 0; k < 3 * n; ++k) igoal[k] = fa * fin.goal_a[k] + fb * fin.goal_b[k];
+        }
+        if (!fin.nt) return 0;
+        ivpos.resize(3 * fin.nv);
+        for (size_t k = 0; k < 3 * fin.nv; ++k) ivpos[k] = fa * fin.va[k] + fb * fin.vb[k];
+        itnorm.assign(3 * fin.nt, 0.f);
+        for (uint32_t t = 0; t < fin.nt; ++t) {
+            const float *A = &ivpos[3 * fin.tri[3 * t]], *B = &ivpos[3 * fin.tri[3 * t + 1]], *C = &ivpos[3 * fin.tri[3 * t + 2]];
+            const float ab[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]}, ac[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
+            f3_cross(ab, ac, &itnorm[3 * t]);
+            f3_normalize_or_zero(&itnorm[3 * t]);
+        }
+        ivnorm.assign(3 * fin.nv, 0.f);
+        for (uint32_t v = 0; v < fin.nv; ++v) {
+            float s[3] = {0, 0, 0};
+            for (uint32_t t : fin.vtris[v]) {
+                uint32_t others[2], m = 0;
+                for (int k = 0; k < 3; ++k)
+                    if (fin.tri[3 * t + k] != v && m < 2) others[m++] = fin.tri[3 * t + k];
+                const float *P = &ivpos[3 * v], *A = &ivpos[3 * others[0]], *B = &ivpos[3 * others[1]];
+                const float pa[3] = {A[0] - P[0], A[1] - P[1], A[2] - P[2]}, pb[3] = {B[0] - P[0], B[1] - P[1], B[2] - P[2]};
+                // nalgebra angle: acos of the clamped cosine, 0 for a zero vector
+                const float na = f3_norm(pa), nb = f3_norm(pb);
+                float ang = 0.f;
+                if (na != 0.f && nb != 0.f) {
+                    const float c = f3_dot(pa, pb) / (na * nb);
+                    ang = c > 1.f ? 0.f : (c < -1.f ? 3.14159265358979f : std::acos(c));
+                }
+                for (int a = 0; a < 3; ++a) s[a] += ang * itnorm[3 * t + a];
+            }
+            f3_normalize_or_zero(s);
+            for (int a = 0; a < 3; ++a) ivnorm[3 * v + a] = s[a];
+        }
+        ifric.resize(fin.nt), idamp.resize(fin.nt);
+        for (uint32_t t = 0; t < fin.nt; ++t)
+            ifric[t] = fa * fin.fr_a[t] + fb * fin.fr_b[t], idamp[t] = fa * fin.dm_a[t] + fb * fin.dm_b[t];
+        return 0;
+    }
+
+    // mesh_util/src/mesh.rs:247-308
+    struct DistanceResult {
+        float distance, to_p[3], normal[3];
+    };
+    static DistanceResult segment_result(const float p[3], const float s[3], const float e[3], const float sn[3],
+                                         const float segn[3], const float en[3]) {
+        const float seg[3] = {e[0] - s[0], e[1] - s[1], e[2] - s[2]};
+        const float ps[3] = {p[0] - s[0], p[1] - s[1], p[2] - s[2]};
+        const float along = f3_dot(ps, seg) / f3_dot(seg, seg);
+        DistanceResult r;
+        const float *nn;
+        if (along < 0.f) {
+            for (int a = 0; a < 3; ++a) r.to_p[a] = ps[a];
+            nn = sn;
+        } else if (along < 1.f) {
+            for (int a = 0; a < 3; ++a) r.to_p[a] = p[a] - s[a] - seg[a] * along;
+            nn = segn;
+        } else {
+            for (int a = 0; a < 3; ++a) r.to_p[a] = p[a] - e[a];
+            nn = en;
+        }
+        r.distance = f3_norm(r.to_p);
+        for (int a = 0; a < 3; ++a) r.normal[a] = nn[a];
+        return r;
+    }
+    static float segment_distance(const float p[3], const float s[3], const float e[3]) {
+        const float z[3] = {0, 0, 0};
+        return segment_result(p, s, e, z, z, z).distance;
+    }
+    static float triangle_distance(const float p[3], const float A[3], const float B[3], const float C[3],
+                                   const float nrm[3]) {
+        const float ab[3] = {A[0] - B[0], A[1] - B[1], A[2] - B[2]};
+        const float bc[3] = {B[0] - C[0], B[1] - C[1], B[2] - C[2]};
+        const float ca[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
+        const float cp[3] = {C[0] - p[0], C[1] - p[1], C[2] - p[2]};
+        const float ap[3] = {A[0] - p[0], A[1] - p[1], A[2] - p[2]};
+        const float bp[3] = {B[0] - p[0], B[1] - p[1], B[2] - p[2]};
+        float x[3];
+        f3_cross(bc, cp, x);
+        const bool sa = f3_dot(nrm, x) > 0.f;
+        f3_cross(ca, ap, x);
+        const bool sb = f3_dot(nrm, x) > 0.f;
+        f3_cross(ab, bp, x);
+        const bool sc = f3_dot(nrm, x) > 0.f;
+        if (sa && sb && sc) {
+            const float pa[3] = {p[0] - A[0], p[1] - A[1], p[2] - A[2]};
+            return std::fabs(f3_dot(pa, nrm));
+        }
+        float d = std::numeric_limits<float>::max();
+        if (!sa) d = std::min(d, segment_distance(p, B, C));
+        if (!sb) d = std::min(d, segment_distance(p, C, A));
+        if (!sc) d = std::min(d, segment_distance(p, A, B));
+        return d;
+    }
+
+    // util/src/collider_bits.rs:9-38
+    static bool cb_near(uint32_t b, int c) { return (b & (0x00010000u << c)) != 0; }
+    static bool cb_side(uint32_t b, int c) { return (b & (0x00000001u << c)) != 0; }
+    static void cb_set(uint32_t &b, int c, int side) {  // side: -1 None, 0 false, 1 true
+        b &= ~(0x00010001u << c);
+        if (side == 1) b |= 0x00010001u << c;
+        else if (side == 0) b |= 0x00010000u << c;
+    }
+
+    // cpu/src/phase/collide.rs:21-206.  The BVH query of the reference
+    // returns a superset of the triangles whose padded leaf box holds the
+    // particle's leaf cell; here that set itself is scanned, in index order.
+    void collide(T dt_t) {
+        if (!fin.nt) return;
+        const float dt = (float)dt_t, forget = forget_distance(), accept = accept_distance();
+        pool.run(n, [&](size_t b, size_t e, int) {
+            for (size_t p = b; e > p; ++p) {
+                if (flags[p] & TOMBSTONED) continue;
+                const float P[3] = {(float)x[p][0], (float)x[p][1], (float)x[p][2]};
+                int32_t leaf[3];
+                for (int a = 0; a < 3; ++a) leaf[a] = (int32_t)std::floor(P[a] / fin.leaf);
+                uint32_t closest[16];
+                float mind[16];
+                bool any = false;
+                for (int c = 0; c < 16; ++c) closest[c] = 0xFFFFFFFFu, mind[c] = std::numeric_limits<float>::max();
+                for (uint32_t t = 0; t < fin.nt; ++t) {
+                    bool in = true;
+                    for (int a = 0; a < 3; ++a) in = in && fin.lmin[3 * t + a] <= leaf[a] && leaf[a] <= fin.lmax[3 * t + a];
+                    if (!in) continue;
+                    any = true;
+                    const float *nrm = &itnorm[3 * t];
+                    if (nrm[0] == 0.f && nrm[1] == 0.f && nrm[2] == 0.f) continue;
+                    const float *A = &ivpos[3 * fin.tri[3 * t]], *B = &ivpos[3 * fin.tri[3 * t + 1]], *C = &ivpos[3 * fin.tri[3 * t + 2]];
+                    const float d = triangle_distance(P, A, B, C, nrm);
+                    if (d >= forget) continue;
+                    const uint32_t c = fin.tri_col[t];
+                    if (d < mind[c]) mind[c] = d, closest[c] = t;
+                }
+                if (!any) {
+                    collider_bits[p] = 0;
+                    continue;
+                }
+                float vel[3] = {(float)v[p][0], (float)v[p][1], (float)v[p][2]};
+                uint32_t bits = collider_bits[p];
+                for (int c = 0; c < 16; ++c) {
+                    if (closest[c] == 0xFFFFFFFFu) {
+                        cb_set(bits, c, -1);
+                        continue;
+                    }
+                    const uint32_t t = closest[c];
+                    const uint32_t ia = fin.tri[3 * t], ib = fin.tri[3 * t + 1], ic = fin.tri[3 * t + 2];
+                    const float *nrm = &itnorm[3 * t];
+                    const float *A = &ivpos[3 * ia], *B = &ivpos[3 * ib], *C = &ivpos[3 * ic];
+                    float abn[3] = {0, 0, 0}, bcn[3] = {0, 0, 0}, can[3] = {0, 0, 0};
+                    const uint32_t *o = &fin.opp[3 * t];
+                    if (o[0] != 0xFFFFFFFFu)
+                        for (int a = 0; a < 3; ++a) abn[a] = nrm[a] + itnorm[3 * o[0] + a];
+                    if (o[1] != 0xFFFFFFFFu)
+                        for (int a = 0; a < 3; ++a) bcn[a] = nrm[a] + itnorm[3 * o[1] + a];
+                    if (o[2] != 0xFFFFFFFFu)
+                        for (int a = 0; a < 3; ++a) can[a] = nrm[a] + itnorm[3 * o[2] + a];
+                    const float ab[3] = {A[0] - B[0], A[1] - B[1], A[2] - B[2]};
+                    const float bc[3] = {B[0] - C[0], B[1] - C[1], B[2] - C[2]};
+                    const float ca[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
+                    float x1[3];
+                    f3_cross(ca, ab, x1);
+                    const float area2 = f3_dot(nrm, x1);
+                    const float cp[3] = {C[0] - P[0], C[1] - P[1], C[2] - P[2]};
+                    const float ap[3] = {A[0] - P[0], A[1] - P[1], A[2] - P[2]};
+                    const float bp[3] = {B[0] - P[0], B[1] - P[1], B[2] - P[2]};
+                    f3_cross(bc, cp, x1);
+                    const float ba = f3_dot(nrm, x1) / area2;
+                    f3_cross(ca, ap, x1);
+                    const float bb = f3_dot(nrm, x1) / area2;
+                    f3_cross(ab, bp, x1);
+                    const float bcb = f3_dot(nrm, x1) / area2;
+                    DistanceResult r;
+                    if (ba > 0.f && bb > 0.f && bcb > 0.f) {
+                        const float pa[3] = {P[0] - A[0], P[1] - A[1], P[2] - A[2]};
+                        const float h = f3_dot(pa, nrm);
+                        r.distance = std::fabs(h);
+                        for (int a = 0; a < 3; ++a) r.to_p[a] = nrm[a] * h, r.normal[a] = nrm[a];
+                    } else {
+                        const float *na = &ivnorm[3 * ia], *nb = &ivnorm[3 * ib], *nc = &ivnorm[3 * ic];
+                        const DistanceResult r1 = segment_result(P, A, B, na, abn, nb);
+                        const DistanceResult r2 = segment_result(P, B, C, nb, bcn, nc);
+                        const DistanceResult r3 = segment_result(P, C, A, nc, can, na);
+                        r = r1;  // min_by(total_cmp): the first of equal distances
+                        if (r2.distance < r.distance) r = r2;
+                        if (r3.distance < r.distance) r = r3;
+                    }
+                    if (r.normal[0] == 0.f && r.normal[1] == 0.f && r.normal[2] == 0.f) {
+                        cb_set(bits, c, -1);
+                        continue;
+                    }
+                    const bool new_side = 0.f <= f3_dot(r.to_p, r.normal);
+                    if (!cb_near(bits, c)) {
+                        if (r.distance < accept) cb_set(bits, c, new_side ? 1 : 0);
+                        continue;
+                    }
+                    if (cb_side(bits, c) == new_side) continue;
+                    if (r.distance > 1e-5f) {
+                        float cv[3], rel[3], cn[3], nv[3], tv[3];
+                        for (int a = 0; a < 3; ++a) {
+                            cv[a] = fin.vvel[3 * ia + a] * ba + fin.vvel[3 * ib + a] * bb + fin.vvel[3 * ic + a] * bcb;
+                            rel[a] = vel[a] - cv[a];
+                            cn[a] = r.to_p[a] / r.distance;
+                        }
+                        const float rn = f3_dot(rel, cn);
+                        for (int a = 0; a < 3; ++a) nv[a] = cn[a] * rn, tv[a] = rel[a] - nv[a];
+                        const float tvn = f3_norm(tv);
+                        if (tvn > 1e-5f) {
+                            const float mag = std::min(ifric[t] * r.distance / dt, tvn);
+                            for (int a = 0; a < 3; ++a) vel[a] -= tv[a] / tvn * mag;
+                        }
+                        const float dmp = std::min(idamp[t], 1.f);
+                        for (int a = 0; a < 3; ++a) vel[a] -= dmp * nv[a];
+                    }
+                    for (int a = 0; a < 3; ++a) vel[a] -= r.to_p[a] / dt;
+                }
+                collider_bits[p] = bits;
+                for (int a = 0; a < 3; ++a) v[p][a] = (T)vel[a];
+            }
+        });
     }
 
     // ---- adaptive time steps
@@ -1015,17 +1382,24 @@ template <class T> struct State : Base {
     int step_adaptive(double *time, double target, float max_dt, const float g_f[3], uint32_t *substeps,
                       float limits[8]) override {
         ad.max_dt = max_dt;
-        const V3<T> g = v3<T>((T)g_f[0], (T)g_f[1], (T)g_f[2]);
         uint32_t done = 0;
         int rc = 0;
         float dt_a = 0, dt_b = 0, dt_c = 0;
+        this->time = *time;
         while (*time < target) {
             if (ad.allowed() == 0.f) {
                 rc = 2;
                 break;
             }
+            this->time = *time;
+            if (fin.set && interpolate_input()) {
+                rc = -2;
+                break;
+            }
+            const V3<T> g = substep_gravity(g_f);
             sort();
             dt_a = ad.allowed();
+            collide((T)dt_a);
             external_force((T)dt_a, g);
             update_grid_nodes();
             limit_time_step_before_force();
@@ -1042,6 +1416,7 @@ template <class T> struct State : Base {
             }
             cull_particles();
             *time += (double)ad.allowed();
+            this->time = *time;
             ++done;
         }
         if (substeps) *substeps = done;
@@ -1175,6 +1550,9 @@ int svo_step_adaptive(void *s, double *time, double target, float max_dt, const 
                       float limits[8]) {
     return static_cast<Base *>(s)->step_adaptive(time, target, max_dt, g, substeps, limits);
 }
+int svo_set_frame_input(void *s, const svo_frame_input *in) { return static_cast<Base *>(s)->set_frame_input(in); }
+void svo_set_time(void *s, double time) { static_cast<Base *>(s)->set_time(time); }
+double svo_get_time(void *s) { return static_cast<Base *>(s)->get_time(); }
 void svo_download(void *s, svo_particles *out) { static_cast<Base *>(s)->download(out); }
 uint64_t svo_grid(void *s, int32_t *ids, float *m, float *v, uint64_t cap) {
     return static_cast<Base *>(s)->grid(ids, m, v, cap);

@@ -67,6 +67,30 @@ typedef struct svo_consts {
     float ground_height;
 } svo_consts;
 
+/* The inputs of frames a and b (xpu/src/frame_input.rs:33-65): gravity,
+ * particle goals and collider meshes, interpolated linearly inside the
+ * frame every substep (cpu/src/phase/interpolate_input.rs:18-106).
+ * goal_flags_* are the frames' particle flags (only HAS_GOAL is read),
+ * goal_positions_* [n][3]; both NULL for no goals.  Colliders: triangles
+ * [n_triangles][3] into the vertex arrays [n_vertices][3], the collider
+ * (0..15) of each triangle, per-triangle friction and damping.  Every *_b
+ * array is ignored when has_b == 0 (b = a, as at the end of the input). */
+typedef struct svo_frame_input {
+    uint32_t frames_per_second;
+    uint32_t frame;
+    uint32_t has_b;
+    float gravity_a[3], gravity_b[3];
+    const uint32_t *goal_flags_a, *goal_flags_b;
+    const float *goal_positions_a, *goal_positions_b;
+    uint32_t n_vertices, n_triangles;
+    const uint32_t *triangles;
+    const uint32_t *triangle_collider;
+    const float *vertex_positions_a, *vertex_positions_b;
+    const float *friction_a, *friction_b;
+    const float *damping_a, *damping_b;
+    float leaf_size;
+} svo_frame_input;
+
 /* Scalar constitutive functions in double precision (util/src/elastic.rs). */
 double svo_mu(double youngs_modulus, double poissons_ratio);
 double svo_lambda(double youngs_modulus, double poissons_ratio);
@@ -93,6 +117,14 @@ void svo_destroy(void *s);
  * (adaptive_time_steps = false).  Returns 0, or 1 when an energy error stopped
  * the run early (a particle got FAILED, advance_particles.rs:73-74). */
 int svo_step(void *s, uint32_t n_substeps, float dt, const float gravity[3]);
+/* With a frame input set (copied), every substep starts with the input
+ * interpolation at the state's time and runs Collide; gravity then comes from
+ * the input and the gravity arguments are ignored.  svo_step advances the
+ * time by dt per substep.  Returns -2 from a substep whose time lies outside
+ * the loaded frame (the reference's WrongFrameLoaded). */
+int svo_set_frame_input(void *s, const svo_frame_input *in);
+void svo_set_time(void *s, double time);
+double svo_get_time(void *s);
 /* Adaptive substeps while *time < target (cpu_state.rs:146-197 with
  * adaptive_time_steps = true); returns 0, 1 on an energy error, 2 on a zero
  * time step.  limits: the last substep's dt of external force, scatter and

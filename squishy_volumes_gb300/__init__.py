@@ -10,6 +10,7 @@ from .state import (  # noqa: F401
     CudaState,
     EnergyError,
     Extras,
+    FrameData,
     FrameInput,
     GridNodes,
     Harness,

@@ -98,6 +98,31 @@ class SvStats(ct.Structure):
     ]
 
 
+class SvFrameInput(ct.Structure):
+    _fields_ = [
+        ("frames_per_second", ct.c_uint32),
+        ("frame", ct.c_uint32),
+        ("has_b", ct.c_uint32),
+        ("gravity_a", ct.c_float * 3),
+        ("gravity_b", ct.c_float * 3),
+        ("goal_flags_a", u32p),
+        ("goal_flags_b", u32p),
+        ("goal_positions_a", f32p),
+        ("goal_positions_b", f32p),
+        ("n_vertices", ct.c_uint32),
+        ("n_triangles", ct.c_uint32),
+        ("triangles", u32p),
+        ("triangle_collider", u32p),
+        ("vertex_positions_a", f32p),
+        ("vertex_positions_b", f32p),
+        ("friction_a", f32p),
+        ("friction_b", f32p),
+        ("damping_a", f32p),
+        ("damping_b", f32p),
+        ("leaf_size", ct.c_float),
+    ]
+
+
 _SIGNATURES = {
     "sv_create": (ct.c_int, [ct.POINTER(SvConsts), ct.POINTER(SvParticles), ct.POINTER(ct.c_void_p)]),
     "sv_step": (
@@ -122,6 +147,9 @@ _SIGNATURES = {
     "sv_step_adaptive": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_double), ct.c_double, ct.c_float, f32p,
                                     ct.POINTER(ct.c_int32), u32p, u32p]),
     "sv_time_step_limits": (ct.c_int, [ct.c_void_p, f32p]),
+    "sv_set_frame_input": (ct.c_int, [ct.c_void_p, ct.POINTER(SvFrameInput)]),
+    "sv_set_time": (ct.c_int, [ct.c_void_p, ct.c_double]),
+    "sv_get_time": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_double)]),
     "sv_autotune": (ct.c_int, [ct.c_void_p, ct.c_float, f32p, ct.c_uint32, u32p, u32p]),
     "sv_set_profiling": (ct.c_int, [ct.c_void_p, ct.c_int]),
     "sv_profile_report": (ct.c_int, [ct.c_void_p, ct.c_char_p, ct.c_uint64]),

@@ -59,6 +59,7 @@ void free_handle(sv_handle *h) {
     for (auto &kv : h->graphs)
         if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     free_closure(h);
+    free_frame(h);
     cudaFree(h->adt);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
@@ -183,6 +184,10 @@ int standalone_p2g(sv_handle *h, float dt, float3 g) {
     SV_CUDA(launch_activate(h, which));
     h->map_cur = h->map_next = which;
     SV_CUDA(launch_clear(h, h->gcur, which));
+    if (h->fin_active) {
+        SV_CUDA(launch_interpolate(h, h->time));
+        SV_CUDA(launch_clear_variants(h, h->gcur));
+    }
     SV_CUDA(launch_p2g(h, dt, g));
     h->pending_valid = true;
     h->pending_dt = dt;
@@ -192,9 +197,25 @@ int standalone_p2g(sv_handle *h, float dt, float3 g) {
     return 0;
 }
 
+bool in_frame(const sv_handle *h, double t) {
+    return (long long)std::floor(t * (double)h->fin_fps) == (long long)h->fin_frame;
+}
+
 // One substep: (every sort_interval substeps) binning sort and block claims
-// for the next grid, grid update, fused gather/advance/scatter.
-int fused_substep(sv_handle *h, float dt, float3 g) {
+// for the next grid, grid update, fused gather/advance/scatter.  With a
+// frame input the scatter belongs to the substep starting at t_next: the
+// input is interpolated there first, and when t_next lies outside the loaded
+// frame the substep only gathers and advances (the next call scatters once
+// the next frame is loaded).
+int fused_substep(sv_handle *h, float dt, float3 g, double t_next = 0.0) {
+    if (h->fin_active && !in_frame(h, t_next)) {
+        SV_CUDA(launch_grid_update(h, false));
+        SV_CUDA(launch_g2p_advance(h, dt));
+        h->need_perm = false;
+        h->since_sort = h->sort_interval;
+        h->pending_valid = false;
+        return 0;
+    }
     if (h->since_sort >= h->sort_interval) {
         if (!h->keys_valid) SV_CUDA(launch_keys(h));
         SV_CUDA(launch_sort_and_segments(h));
@@ -205,6 +226,10 @@ int fused_substep(sv_handle *h, float dt, float3 g) {
         h->since_sort = 0;
     } else {
         h->map_next = h->map_cur;
+    }
+    if (h->fin_active) {
+        SV_CUDA(launch_interpolate(h, t_next));
+        SV_CUDA(launch_clear_variants(h, h->gcur ^ 1));
     }
     SV_CUDA(launch_grid_update(h, true));
     const bool write_keys = h->since_sort + 1 >= h->sort_interval;
@@ -347,9 +372,10 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
             return fail("sv_create_batched: scenes must share grid_node_size, ground plane and SVD policy");
         if (batched && cc.ground_mode != 0 && cc.ground_axis != 2)
             return fail("sv_create_batched: the ground plane must be on axis 2 (scenes are laid out in x and y)");
-        for (uint64_t i = 0; i < p->n; ++i)
-            if (p->collider_bits && p->collider_bits[i] != 0)
-                return fail("sv_create: collider bits are set but colliders are not supported by this backend");
+        if (batched)
+            for (uint64_t i = 0; i < p->n; ++i)
+                if (p->collider_bits && p->collider_bits[i] != 0)
+                    return fail("sv_create_batched: batched scenes have no colliders; collider bits must be 0");
         first[s + 1] = first[s] + p->n;
     }
     n = first[n_scenes];
@@ -569,6 +595,7 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
             return cuda_fail(e, "upload");
     }
     h->collider_bits.assign(n, 0);
+    if (!batched && ps[0].collider_bits) h->collider_bits.assign(ps[0].collider_bits, ps[0].collider_bits + n);
     h->keys_valid = false;
     *out = h;
     return 0;
@@ -602,14 +629,16 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
         SV_CUDA(cudaMemcpyAsync(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice, h->stream));
         h->pending_valid = false;
     }
-    const bool same_inputs = h->pending_valid && h->pending_dt == dt && h->pending_g[0] == g.x &&
-                             h->pending_g[1] == g.y && h->pending_g[2] == g.z;
+    // with a frame input, gravity comes from the input and the pending
+    // scatter was made for the substep starting at h->time
+    const bool same_inputs = h->pending_valid && h->pending_dt == dt &&
+                             (h->fin_active || (h->pending_g[0] == g.x && h->pending_g[1] == g.y && h->pending_g[2] == g.z));
     if (!same_inputs) h->pending_valid = false;
     const uint32_t base = h->host_counters[C_SUBSTEPS];
     const uint32_t fp64_before = h->host_counters[C_FP64];
     uint32_t fallback_before = h->host_counters[C_FALLBACK];
     uint32_t status = 0;
-    uint32_t done = 0;
+    uint32_t done = 0, timed = 0;
     const uint32_t chunk = 64;
     while (done < n_substeps) {
         if (cancel && *cancel) {
@@ -617,24 +646,33 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
             break;
         }
         const uint32_t todo = std::min(chunk, n_substeps - done);
-        if (!h->pending_valid && standalone_p2g(h, dt, g)) return -1;
+        if (!h->pending_valid) {
+            if (h->fin_active && !in_frame(h, h->time))
+                return fail("sv_step: the substep's time lies outside the loaded frame input (wrong frame loaded)");
+            if (standalone_p2g(h, dt, g)) return -1;
+        }
+        double t_q = h->time;  // start time of the substep after the one launched
         for (uint32_t s = 0; s < todo;) {
             // whole binning periods go through CUDA graphs once the binning
             // keys come from the previous substep (steady state)
-            if (h->use_graphs && !h->profiling && h->since_sort >= h->sort_interval && h->keys_valid &&
-                todo - s >= h->sort_interval) {
+            if (h->use_graphs && !h->fin_active && !h->profiling && h->since_sort >= h->sort_interval &&
+                h->keys_valid && todo - s >= h->sort_interval) {
                 if (run_period_graph(h, dt, g)) return -1;
                 s += h->sort_interval;
             } else {
-                if (fused_substep(h, dt, g)) return -1;
+                t_q += (double)dt;
+                if (fused_substep(h, dt, g, t_q)) return -1;
                 s += 1;
+                if (!h->pending_valid) break;  // the frame's last substep: nothing pending
             }
         }
         if (read_counters(h)) return -1;
         const uint32_t st = h->host_counters[C_STATUS];
         done = h->host_counters[C_SUBSTEPS] - base;
+        for (; timed < done; ++timed) h->time += (double)dt;  // cpu_state.rs:186-189
         if (st & ST_OUT_OF_GRID) return fail("sv_step: a live particle left the grid block index");
         if (h->host_counters[C_CLOSURE_ERR]) return fail("sv_step: a tensor-core wait of the learned closure timed out");
+        if (st & ST_VARIANT_FULL) return fail("sv_step: the collider variant table is full");
         if (st & (ST_CAPACITY | ST_MOVED_FAR)) {
             if (st & ST_CAPACITY) {
                 // Grow and redo what was skipped (gpu_state.rs:562-599 redoes a
@@ -665,6 +703,8 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
         if (st & ST_INVERTED) {
             status |= SV_STATUS_PARTICLE_INVERTED;
             h->pending_valid = false;
+            // the failed substep does not advance the time (cpu_state.rs:178-183)
+            if (done > 0) h->time -= (double)dt;
             break;
         }
     }
@@ -691,6 +731,10 @@ int adaptive_substep(sv_handle *h, float3 g) {
     const int which = h->map_cur ^ 1;
     SV_CUDA(launch_activate(h, which));
     h->map_cur = h->map_next = which;
+    if (h->fin_active) {
+        SV_CUDA(launch_interpolate(h, 0.0));  // at the device time of the substep
+        SV_CUDA(launch_clear_variants(h, h->gcur));
+    }
     SV_CUDA(launch_limits_force(h));
     SV_CUDA(launch_clear(h, h->gcur, which));
     SV_CUDA(launch_p2g(h, 0.f, g));
@@ -757,6 +801,14 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
             rc = fail("sv_step_adaptive: zero time step");  // Error::ZeroTimeStep
             break;
         }
+        if (stw & ST_WRONG_FRAME) {
+            rc = fail("sv_step_adaptive: the substep's time lies outside the loaded frame input (wrong frame loaded)");
+            break;
+        }
+        if (stw & ST_VARIANT_FULL) {
+            rc = fail("sv_step_adaptive: the collider variant table is full");
+            break;
+        }
         if (stw & (STOP_MASK & ~ST_TIME_REACHED)) h->keys_valid = false;  // stopped advances copied in place
         if (stw & ST_CAPACITY) {
             const uint64_t cap = std::min<uint64_t>(h->layout.total_blocks, h->capacity * 2);
@@ -790,6 +842,7 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
     const uint32_t done = h->host_counters[C_SUBSTEPS] - base;
     h->substeps_total += done;
     *time_inout = st.time;
+    h->time = st.time;
     if (status_out) *status_out = status;
     if (substeps_done) *substeps_done = done;
     return 0;
@@ -843,6 +896,11 @@ int sv_download(sv_handle *h, sv_particles *o) {
     SV_CUDA(cudaMemcpy(F.data(), a.F, 9 * n * 4, cudaMemcpyDeviceToHost));
     SV_CUDA(cudaMemcpy(en.data(), a.energy, n * 4, cudaMemcpyDeviceToHost));
     SV_CUDA(cudaMemcpy(orig.data(), a.orig, n * 4, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> cbits;
+    if (a.cbits_done) {
+        cbits.resize(n);
+        SV_CUDA(cudaMemcpy(cbits.data(), a.cbits_done, n * 4, cudaMemcpyDeviceToHost));
+    }
     const double dx = h->layout.dx;
     for (uint64_t s = 0; s < n; ++s) {
         const uint64_t i = orig[s];
@@ -869,7 +927,12 @@ int sv_download(sv_handle *h, sv_particles *o) {
             if (o->velocity_gradients) o->velocity_gradients[9 * i + k] = C[(uint64_t)k * n + s];
         }
         if (o->elastic_energies) o->elastic_energies[i] = en[s];
-        if (o->collider_bits) o->collider_bits[i] = h->collider_bits[i];
+        if (o->collider_bits) {
+            // without colliders every substep's Collide clears a live
+            // particle's bits (collide.rs:53-56)
+            if (!cbits.empty()) o->collider_bits[i] = cbits[s];
+            else o->collider_bits[i] = (h->substeps_total > 0 && !(packed & SV_TOMBSTONED)) ? 0u : h->collider_bits[i];
+        }
     }
     return 0;
 }

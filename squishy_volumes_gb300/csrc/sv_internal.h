@@ -29,7 +29,10 @@ constexpr uint32_t ST_OUT_OF_GRID = 1u << 4;  // a live particle left the block 
 constexpr uint32_t ST_MOVED_FAR = 1u << 5;    // a particle left the blocks claimed at binning
 constexpr uint32_t ST_TIME_REACHED = 1u << 6; // adaptive steps: the target time is reached
 constexpr uint32_t ST_ZERO_DT = 1u << 7;      // adaptive steps: the allowed time step is 0
-constexpr uint32_t STOP_MASK = ST_CAPACITY | ST_INVERTED | ST_OUT_OF_GRID | ST_MOVED_FAR | ST_TIME_REACHED | ST_ZERO_DT;
+constexpr uint32_t ST_VARIANT_FULL = 1u << 9; // the collider-variant table or a node's variant slots are full
+constexpr uint32_t ST_WRONG_FRAME = 1u << 10; // a substep's time lies outside the loaded frame input
+constexpr uint32_t STOP_MASK = ST_CAPACITY | ST_INVERTED | ST_OUT_OF_GRID | ST_MOVED_FAR | ST_TIME_REACHED | ST_ZERO_DT |
+                               ST_VARIANT_FULL | ST_WRONG_FRAME;
 
 // Device counters (one array so one copy reads them all).
 enum Counter : int {
@@ -60,6 +63,10 @@ struct ParticleArrays {
     float *F;        // [9][n] position gradient
     float *energy;   // [n]
     uint32_t *orig;  // [n] original particle index (the reference's sort_map)
+    // collider bits (allocated once a frame input is set): the bits in
+    // effect for the next gather (after the pending scatter's Collide) and
+    // the bits after the last completed substep
+    uint32_t *cbits = nullptr, *cbits_done = nullptr;
 };
 
 struct GridLayout {
@@ -180,6 +187,33 @@ struct sv_handle {
     void *adt = nullptr;
     bool adaptive_active = false;
 
+    // Simulation time of the completed state (the reference's CpuState::time),
+    // used to interpolate the frame input.
+    double time = 0.0;
+
+    // Frame input and colliders (sv_collide.cuh, set by sv_set_frame_input).
+    bool fin_active = false;
+    uint32_t fin_fps = 24, fin_frame = 0;
+    bool fin_has_b = false;
+    float fin_g_a[3] = {0, 0, 0}, fin_g_b[3] = {0, 0, 0};
+    uint32_t fin_nv = 0, fin_nt = 0;
+    float *fin_scalars = nullptr;    // device: gravity[3], factor
+    uint32_t *fin_goal_both = nullptr;
+    float *fin_goal_a = nullptr, *fin_goal_b = nullptr;
+    uint32_t *fin_tri = nullptr, *fin_tri_col = nullptr, *fin_opp = nullptr;
+    float *fin_va = nullptr, *fin_vb = nullptr, *fin_vvel = nullptr;
+    float *fin_fr_a = nullptr, *fin_fr_b = nullptr, *fin_dm_a = nullptr, *fin_dm_b = nullptr;
+    uint32_t *fin_vt_start = nullptr, *fin_vt_list = nullptr;  // vertex -> triangles (CSR)
+    uint32_t *fin_leaf_start = nullptr, *fin_leaf_list = nullptr;
+    int32_t fin_leaf_lo[3] = {0, 0, 0}, fin_leaf_dim[3] = {0, 0, 0};
+    float fin_leaf_size = 1.f;
+    float *fin_vpos = nullptr, *fin_vnorm = nullptr, *fin_tnorm = nullptr, *fin_fric = nullptr, *fin_damp = nullptr;
+    // collider-variant tables (two, swapped with the grids)
+    unsigned long long *var_key[2] = {nullptr, nullptr};
+    uint32_t *var_bits[2] = {nullptr, nullptr};
+    float4 *var_acc[2] = {nullptr, nullptr}, *var_vel[2] = {nullptr, nullptr};
+    uint32_t var_cap = 0;
+
     // Learned stress closure of snow and sand (sv_closure.cu).
     int closure_mode = 0;  // 0 return maps (SVD), 1 learned closure
     bool cl_trained = false;
@@ -212,6 +246,12 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 gravity, bool write_keys
 cudaError_t launch_limits_force(sv_handle *h);
 cudaError_t launch_g2p_only(sv_handle *h);
 cudaError_t launch_advance(sv_handle *h);
+// frame input: interpolation at `time` (adaptive: the device time), the
+// gather + advance without the scatter of the next substep, clearing the
+// variant table the next scatter fills
+cudaError_t launch_interpolate(sv_handle *h, double time);
+cudaError_t launch_g2p_advance(sv_handle *h, float dt);
+cudaError_t launch_clear_variants(sv_handle *h, int which);
 
 // Per-kernel timing hooks.
 void timer_begin(sv_handle *h, const char *name, cudaEvent_t *start);
@@ -227,5 +267,8 @@ void drop_graphs(sv_handle *h);
 
 // Frees the learned closure's device buffers (sv_closure.cu).
 void free_closure(sv_handle *h);
+
+// Frees the frame input, the collider bits and the variant tables (sv_frame.cu).
+void free_frame(sv_handle *h);
 
 }  // namespace sv

@@ -33,6 +33,7 @@
 
 #include "sv_adaptive.cuh"
 #include "sv_closure.cuh"
+#include "sv_collide.cuh"
 #include "sv_internal.h"
 #include "sv_mlp.cuh"
 #include "sv_sort.cuh"
@@ -49,6 +50,7 @@ constexpr int TN = 8;  // tile edge in nodes: block nodes 4b..4b+3 plus 1 below,
 constexpr int TILE_NODES = TN * TN * TN;
 constexpr uint32_t REC_NONE = 0xFFFFFFFFu;
 constexpr uint32_t REC_GLOBAL = 0x80000000u;
+constexpr uint32_t REC_VARIANT = 0x80000001u;  // non-zero collider bits: the variant table
 
 // Scatter record of one particle: for stencil offset (i, j, k) the node gets
 // mass w m and momentum w (p0[i] + p1[j] + p2[k]) with w = p0[i].w p1[j].w
@@ -60,7 +62,14 @@ struct Rec {
 // MODE_G2P2G_LEARNED is MODE_G2P2G with the learned closure for snow and
 // sand.  Adaptive time steps split the fused pass: MODE_G2P_ONLY gathers v
 // and C (written back in place), MODE_ADVANCE advances from them.
-enum Mode { MODE_P2G = 0, MODE_G2P2G = 1, MODE_G2P2G_LEARNED = 2, MODE_G2P_ONLY = 3, MODE_ADVANCE = 4 };
+enum Mode {
+    MODE_P2G = 0,
+    MODE_G2P2G = 1,
+    MODE_G2P2G_LEARNED = 2,
+    MODE_G2P_ONLY = 3,
+    MODE_ADVANCE = 4,
+    MODE_G2P_ADVANCE = 5,  // the fused pass without the next scatter (the next substep's input is not loaded)
+};
 
 struct StepArgs {
     ParticleArrays in, out;
@@ -78,6 +87,8 @@ struct StepArgs {
     const uint8_t *closure_img;          // packed network weights (learned mode)
     const closure::Hull *closure_hull;   // training hull of the features (learned mode)
     adaptive::State *adt;                // adaptive time steps: device dt and reductions (else nullptr)
+    col::FrameArgs fa;                   // frame input (kernels instantiated with FIN only)
+    col::VariantTable vcur, vnext;       // collider variants gathered from / scattered into
     uint64_t n;
     GridLayout L;
     float dt;
@@ -164,6 +175,7 @@ __device__ __forceinline__ void copy_particle(const ParticleArrays &in, const Pa
     }
     out.energy[dst] = in.energy[src];
     out.orig[dst] = in.orig[src];
+    if (in.cbits) out.cbits[dst] = in.cbits[src], out.cbits_done[dst] = in.cbits_done[src];
 }
 
 // P F^T of the particle's model (the part of scatter_momentum.rs:46-90 that
@@ -385,7 +397,7 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_clear_grid(float4 *grid, uint6
 // (slots of map `wn`) for the scatter that follows.
 __global__ void __launch_bounds__(ELEM_THREADS)
     k_grid_update(float4 *grid_cur, const uint32_t *active_cur, float4 *grid_next, uint64_t capacity, GridLayout L,
-                  uint32_t *counters, int wc, int wn) {
+                  uint32_t *counters, int wc, int wn, col::VariantTable var) {
     if (stopped(counters)) return;
     uint64_t sc = counters[C_NSLOT0 + wc], sn = grid_next ? counters[C_NSLOT0 + wn] : 0;
     if (sc > capacity) sc = capacity;
@@ -394,6 +406,20 @@ __global__ void __launch_bounds__(ELEM_THREADS)
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
         if (i < sc * 64) {
             float4 g = grid_cur[i];
+            if (var.key) {
+                // meld_grid.rs:29-58: bits 0 is compatible with every variant
+                int bx, by, bz;
+                block_coords(active_cur[i >> 6], L, bx, by, bz);
+                const int l = (int)(i & 63);
+                const int64_t e = col::node_entry(var, L.origin[0] + 4 * bx + (l >> 4), L.origin[1] + 4 * by + ((l >> 2) & 3),
+                                                  L.origin[2] + 4 * bz + (l & 3));
+                if (e >= 0)
+                    for (int j = 0; j < col::VK; ++j)
+                        if (var.bits[e * col::VK + j]) {
+                            const float4 a = var.acc[e * col::VK + j];
+                            g.x += a.x, g.y += a.y, g.z += a.z, g.w += a.w;
+                        }
+            }
             // meld_grid.rs:61-66: v = p / m, or 0 when m <= 0
             float m = g.w;
             float vx = 0.f, vy = 0.f, vz = 0.f;
@@ -415,6 +441,120 @@ __global__ void __launch_bounds__(ELEM_THREADS)
             grid_cur[i] = make_float4(vx, vy, vz, m);
         }
         if (i < sn * 64) grid_next[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// Melds the collider variants (meld_grid.rs:16-69): variant (node, bits) gets
+// its own momentum, the node's bits-0 momentum from the dense grid (still
+// raw: this runs before k_grid_update) and every compatible variant's; then
+// v = p / m and the boundary plane as in k_grid_update.
+__global__ void __launch_bounds__(ELEM_THREADS)
+    k_variant_meld(col::VariantTable var, const float4 *grid_raw, const int32_t *map, GridLayout L,
+                   const uint32_t *counters) {
+    if (stopped(counters)) return;
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < var.cap; e += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long k = var.key[e];
+        if (k == 0ull) continue;
+        const unsigned long long q = k - 1ull;
+        const int node[3] = {(int)((q >> 42) & 0x1FFFFFull) - (1 << 20), (int)((q >> 21) & 0x1FFFFFull) - (1 << 20),
+                             (int)(q & 0x1FFFFFull) - (1 << 20)};
+        int local;
+        const int32_t slot = node_slot(map, node[0], node[1], node[2], L, local);
+        const float4 base = slot >= 0 ? grid_raw[(uint64_t)slot * 64 + local] : make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t b[col::VK];
+        float4 a[col::VK];
+        for (int j = 0; j < col::VK; ++j) b[j] = var.bits[e * col::VK + j], a[j] = var.acc[e * col::VK + j];
+        for (int j = 0; j < col::VK; ++j) {
+            if (!b[j]) continue;
+            float4 g = make_float4(a[j].x + base.x, a[j].y + base.y, a[j].z + base.z, a[j].w + base.w);
+            for (int o = 0; o < col::VK; ++o)
+                if (o != j && b[o] && col::compatible(b[j], b[o])) g.x += a[o].x, g.y += a[o].y, g.z += a[o].z, g.w += a[o].w;
+            const float m = g.w;
+            float vx = 0.f, vy = 0.f, vz = 0.f;
+            if (m > 0.f) vx = g.x / m, vy = g.y / m, vz = g.z / m;
+            if (L.ground_mode != 0 && (float)node[L.ground_axis] * L.dx <= L.ground_height) {
+                if (L.ground_mode == 1) vx = vy = vz = 0.f;
+                else if (L.ground_axis == 0) vx = fmaxf(vx, 0.f);
+                else if (L.ground_axis == 1) vy = fmaxf(vy, 0.f);
+                else vz = fmaxf(vz, 0.f);
+            }
+            var.vel[e * col::VK + j] = make_float4(vx, vy, vz, m);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ frame input interpolation
+// interpolate_input.rs:18-106 at `time` (or the adaptive state's time):
+// factor of frame b, gravity, vertex positions, frictions, dampings.
+struct FinDev {
+    uint32_t fps, frame, nv, nt;
+    float g_a[3], g_b[3];
+    const float *va, *vb, *fr_a, *fr_b, *dm_a, *dm_b;
+    const uint32_t *tri, *vt_start, *vt_list;
+    float *scalars;  // gravity[3], factor
+    float *vpos, *vnorm, *tnorm, *fric, *damp;
+};
+
+__global__ void k_interp_factor(FinDev f, double time, const adaptive::State *st, uint32_t *counters) {
+    if (st && stopped(counters)) return;
+    const double t = st ? st->time : time;
+    const double ft = t * (double)f.fps;
+    if ((long long)floor(ft) != (long long)f.frame) {  // frame_input.rs:266-278 WrongFrameLoaded
+        atomicOr(&counters[C_STATUS], ST_WRONG_FRAME);
+        return;
+    }
+    const float fb = (float)fmod(ft, 1.0), fa = 1.f - fb;
+    for (int a = 0; a < 3; ++a) f.scalars[a] = fa * f.g_a[a] + fb * f.g_b[a];
+    f.scalars[3] = fb;
+}
+
+__global__ void __launch_bounds__(ELEM_THREADS) k_interp_vertices(FinDev f, const uint32_t *counters) {
+    const float fb = f.scalars[3], fa = 1.f - fb;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < 3ull * f.nv; k += (uint64_t)gridDim.x * blockDim.x)
+        f.vpos[k] = fa * f.va[k] + fb * f.vb[k];
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < f.nt; t += (uint64_t)gridDim.x * blockDim.x)
+        f.fric[t] = fa * f.fr_a[t] + fb * f.fr_b[t], f.damp[t] = fa * f.dm_a[t] + fb * f.dm_b[t];
+}
+
+__device__ inline void normalize_or_zero(float a[3]) {  // nalgebra try_normalize(1e-5)
+    const float nn = sqrtf(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    if (nn <= col::EPS) a[0] = a[1] = a[2] = 0.f;
+    else a[0] /= nn, a[1] /= nn, a[2] /= nn;
+}
+
+__global__ void __launch_bounds__(ELEM_THREADS) k_interp_triangles(FinDev f) {
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < f.nt; t += (uint64_t)gridDim.x * blockDim.x) {
+        const float *A = f.vpos + 3 * f.tri[3 * t], *B = f.vpos + 3 * f.tri[3 * t + 1], *C = f.vpos + 3 * f.tri[3 * t + 2];
+        const float ab[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]}, ac[3] = {C[0] - A[0], C[1] - A[1], C[2] - A[2]};
+        float n[3];
+        col::cross3(ab, ac, n);
+        normalize_or_zero(n);
+        for (int a = 0; a < 3; ++a) f.tnorm[3 * t + a] = n[a];
+    }
+}
+
+// angle-weighted vertex normals (interpolate_input.rs:56-79)
+__global__ void __launch_bounds__(ELEM_THREADS) k_interp_vertex_normals(FinDev f) {
+    for (uint64_t v = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < f.nv; v += (uint64_t)gridDim.x * blockDim.x) {
+        float s[3] = {0.f, 0.f, 0.f};
+        const float *P = f.vpos + 3 * v;
+        for (uint32_t k = f.vt_start[v]; k < f.vt_start[v + 1]; ++k) {
+            const uint32_t t = f.vt_list[k];
+            uint32_t others[2] = {0, 0}, m = 0;
+            for (int c = 0; c < 3; ++c)
+                if (f.tri[3 * t + c] != (uint32_t)v && m < 2) others[m++] = f.tri[3 * t + c];
+            const float *A = f.vpos + 3 * others[0], *B = f.vpos + 3 * others[1];
+            const float pa[3] = {A[0] - P[0], A[1] - P[1], A[2] - P[2]}, pb[3] = {B[0] - P[0], B[1] - P[1], B[2] - P[2]};
+            const float na = sqrtf(col::dot3(pa, pa)), nb = sqrtf(col::dot3(pb, pb));
+            float ang = 0.f;
+            if (na != 0.f && nb != 0.f) {
+                const float c = col::dot3(pa, pb) / (na * nb);
+                ang = c > 1.f ? 0.f : (c < -1.f ? 3.14159265358979f : acosf(c));
+            }
+            for (int a = 0; a < 3; ++a) s[a] += ang * f.tnorm[3 * t + a];
+        }
+        normalize_or_zero(s);
+        for (int a = 0; a < 3; ++a) f.vnorm[3 * v + a] = s[a];
     }
 }
 
@@ -462,11 +602,12 @@ __device__ __forceinline__ void scatter_records(Shared &sh, int count, const Ste
     const uint32_t key = __float_as_uint(me.x);
     const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
     const uint32_t next = __shfl_down_sync(0xffffffffu, key, 1);
-    const bool valid = key != REC_NONE && key != REC_GLOBAL;
+    const bool valid = key < REC_GLOBAL;  // a tile index
     const uint32_t start = __ballot_sync(0xffffffffu, valid && (lane == 0 || prev != key));
     const uint32_t end = __ballot_sync(0xffffffffu, valid && (lane == 31 || next != key));
     const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
     const uint32_t gmask = __ballot_sync(0xffffffffu, key == REC_GLOBAL);
+    const uint32_t cmask = __ballot_sync(0xffffffffu, key == REC_VARIANT);
     float2 amx = make_float2(0.f, 0.f), ayz = make_float2(0.f, 0.f);
     // unrolled by 8: the whole-warp unroll grows the kernel past the
     // instruction cache for no gain
@@ -509,6 +650,43 @@ __device__ __forceinline__ void scatter_records(Shared &sh, int count, const Ste
                 atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR);
         }
     }
+    // records of particles with collider bits: their (node, bits) variants
+    // (update_grid_nodes.rs:94-118)
+    for (uint32_t g = cmask; g; g &= g - 1) {
+        const int r = __ffs(g) - 1;
+        const float4 p0 = sh.rec[r0 + r].p[li], p1 = sh.rec[r0 + r].p[3 + lj], p2 = sh.rec[r0 + r].p[6 + lk];
+        const float w = p0.w * p1.w * p2.w;
+        const float m = sh.meta[r0 + r].y;
+        const int4 gb = sh.gbase[r0 + r];
+        if (active) {
+            const int64_t s = col::variant_slot(A.vnext, gb.x + li, gb.y + lj, gb.z + lk, (uint32_t)gb.w, true);
+            if (s >= 0)
+                atomicAdd(&A.vnext.acc[s],
+                          make_float4(w * (p0.x + p1.x + p2.x), w * (p0.y + p1.y + p2.y), w * (p0.z + p1.z + p2.z), w * m));
+            else
+                atomicOr(&A.counters[C_STATUS], ST_VARIANT_FULL);
+        }
+    }
+}
+
+// G2P of a particle with collider bits from its (node, bits) variants.
+__device__ __forceinline__ void gather_variant(const StepArgs &A, const int base[3], uint32_t bits, const float w[3][3],
+                                               const float d[3][3], float v[3], m3f &C) {
+    v[0] = v[1] = v[2] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) C.a[k] = 0.f;
+    for (int ii = 0; ii < 3; ++ii)
+        for (int jj = 0; jj < 3; ++jj)
+            for (int kk = 0; kk < 3; ++kk) {
+                const float wt = w[0][ii] * w[1][jj] * w[2][kk];
+                const int64_t s = col::variant_slot(A.vcur, base[0] + ii, base[1] + jj, base[2] + kk, bits, false);
+                const float4 g = s >= 0 ? A.vcur.vel[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float gx = g.x * wt, gy = g.y * wt, gz = g.z * wt;
+                v[0] += gx, v[1] += gy, v[2] += gz;
+                C.a[0] += gx * d[0][ii], C.a[1] += gy * d[0][ii], C.a[2] += gz * d[0][ii];
+                C.a[3] += gx * d[1][jj], C.a[4] += gy * d[1][jj], C.a[5] += gz * d[1][jj];
+                C.a[6] += gx * d[2][kk], C.a[7] += gy * d[2][kk], C.a[8] += gz * d[2][kk];
+            }
 }
 
 // Record key for a particle scattering from base cell `base` into the tile
@@ -591,13 +769,15 @@ static_assert(sizeof(Rec) * PT >= tc::NIN * PT * 2 + tc::NH * PT * 2, "closure o
 // Five CTAs per SM (at most 102 registers): measured faster than the
 // unconstrained 150-register build despite a few spilled values.  The
 // learned-closure variant holds the network image as well: four CTAs.
-template <bool CELL, int MODE>
-__global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_particles(StepArgs A) {
+// FIN: a frame input is loaded -- interpolated gravity and goals, Collide
+// (collide.rs:21-206) before the scatter, collider bits and their variants.
+template <bool CELL, int MODE, bool FIN = false>
+__global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 5) k_particles(StepArgs A) {
     constexpr bool LEARNED = MODE == MODE_G2P2G_LEARNED;
     // what the pass does: gather from the grid, advance the particles (and
     // write them out in sorted order), scatter into the next grid
-    constexpr bool GATHER = MODE == MODE_G2P2G || LEARNED || MODE == MODE_G2P_ONLY;
-    constexpr bool G2P = MODE == MODE_G2P2G || LEARNED || MODE == MODE_ADVANCE;  // advances
+    constexpr bool GATHER = MODE == MODE_G2P2G || LEARNED || MODE == MODE_G2P_ONLY || MODE == MODE_G2P_ADVANCE;
+    constexpr bool G2P = MODE == MODE_G2P2G || LEARNED || MODE == MODE_ADVANCE || MODE == MODE_G2P_ADVANCE;  // advances
     constexpr bool SCATTER = MODE == MODE_P2G || MODE == MODE_G2P2G || LEARNED;
     constexpr bool LOAD_VC = MODE == MODE_P2G || MODE == MODE_ADVANCE;  // v and C from the state
     __shared__ Shared sh;
@@ -671,6 +851,10 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
             m3f F, C;
             float v[3] = {0.f, 0.f, 0.f};
             float plastic_j = 1.f;
+            // collider bits in effect for this pass (FIN): for a gather the
+            // bits the particle scattered with, for a standalone scatter the
+            // bits after the last completed substep
+            uint32_t bits_in = 0;
             if (i < end) {
                 p = A.perm ? A.perm[i] : i;
                 pos = A.in.pos[p];
@@ -684,6 +868,7 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
                 } else {
                     work = true;
                     const uint32_t kind = A.mats[packed >> MATERIAL_SHIFT].kind;
+                    if constexpr (FIN) bits_in = MODE == MODE_P2G ? A.in.cbits_done[p] : A.in.cbits[p];
                     if (MODE != MODE_G2P_ONLY) load_mat9(A.in.F, A.n, p, F);
                     if (LOAD_VC) {
                         load_mat9(A.in.C, A.n, p, C);
@@ -707,7 +892,9 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
                             for (int k = 0; k < 3; ++k) d[a][k] = ((float)k - fx[a]) * dx;
                         const int tx = base[0] - org[0], ty = base[1] - org[1], tz = base[2] - org[2];
                         const bool in_tile = tx >= 0 && ty >= 0 && tz >= 0 && tx <= TN - 3 && ty <= TN - 3 && tz <= TN - 3;
-                        if (in_tile) {
+                        if (FIN && bits_in != 0u) {
+                            gather_variant(A, base, bits_in, w, d, v, C);  // collect_velocity.rs:61-62 keyed by bits
+                        } else if (in_tile) {
                             gather_tile(sh.gv, tx * 64 + ty * 8 + tz, w, d, v, C);
                         } else {
                             ++fallback;
@@ -889,6 +1076,12 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
                     store_mat9(A.out.F, A.n, i, F);
                     A.out.energy[i] = energy;
                     A.out.orig[i] = A.in.orig[p];
+                    if constexpr (FIN) {
+                        // the bits of the completed substep; the next
+                        // scatter's Collide (below) replaces the ones in effect
+                        A.out.cbits_done[i] = bits_in;
+                        A.out.cbits[i] = bits_in;
+                    }
                 }
                 int nbase[3];
                 float nfx[3];
@@ -903,16 +1096,43 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 4 : 5) k_part
                     A.keys_out[i] = key;
                 }
                 if (SCATTER && alive) {
-                    // ---- scatter record of the next substep: external force
-                    // (external_force.rs:17-50) then the momentum of
-                    // scatter_momentum.rs:38-90
-                    v[0] += dt_force * A.gravity.x, v[1] += dt_force * A.gravity.y, v[2] += dt_force * A.gravity.z;
+                    // ---- scatter record of the next substep: Collide
+                    // (collide.rs:21-206), external force (external_force.rs:17-50),
+                    // then the momentum of scatter_momentum.rs:38-90
+                    uint32_t bits_new = 0u;
+                    if constexpr (FIN) {
+                        const float P[3] = {CELL ? ((float)cell.x + pos.x) * dx : pos.x,
+                                            CELL ? ((float)cell.y + pos.y) * dx : pos.y,
+                                            CELL ? ((float)cell.z + pos.z) * dx : pos.z};
+                        bits_new = bits_in;
+                        if (A.fa.nt) col::collide_particle(A.fa, P, v, bits_new, dt_force);
+                        else bits_new = 0u;  // nothing to check (collide.rs:53-56)
+                        const uint32_t o = A.in.orig[p];
+                        if (A.fa.goal_both && A.fa.goal_both[o]) {
+                            // both frames give a goal: reach it in one step
+                            const float fb = A.fa.factor[0], fa_ = 1.f - fb;
+#pragma unroll
+                            for (int a = 0; a < 3; ++a)
+                                v[a] = (fa_ * A.fa.goal_a[3 * o + a] + fb * A.fa.goal_b[3 * o + a] - P[a]) / dt_force;
+                        } else {
+#pragma unroll
+                            for (int a = 0; a < 3; ++a) v[a] += dt_force * A.fa.gravity[a];
+                        }
+                        if (G2P) A.out.cbits[i] = bits_new;
+                        else A.in.cbits[p] = bits_new;
+                    } else {
+                        v[0] += dt_force * A.gravity.x, v[1] += dt_force * A.gravity.y, v[2] += dt_force * A.gravity.z;
+                    }
                     const m3f PFt = use_l ? tau_l : stress_times_ft(mat, F, J, U, S, hard);
                     make_record(mat, C, PFt, J, v, nfx, dx, dt_scatter, sh.rec[threadIdx.x]);
                     rmass = mat.mass;
                     int4 gb;
                     rcell = tile_cell(nbase, org, gb);
-                    if (rcell == REC_GLOBAL) sh.gbase[threadIdx.x] = gb;
+                    if (FIN && bits_new != 0u) {
+                        rcell = REC_VARIANT;
+                        gb = make_int4(nbase[0], nbase[1], nbase[2], (int)bits_new);
+                    }
+                    if (rcell == REC_GLOBAL || rcell == REC_VARIANT) sh.gbase[threadIdx.x] = gb;
                 }
             }
             if (SCATTER) {
@@ -1087,6 +1307,33 @@ StepArgs make_args(sv_handle *h, float dt, float3 g) {
     A.closure_img = nullptr;
     A.closure_hull = nullptr;
     A.adt = nullptr;
+    A.fa = col::FrameArgs{};
+    A.vcur = col::VariantTable{};
+    A.vnext = col::VariantTable{};
+    if (h->fin_active) {
+        col::FrameArgs &f = A.fa;
+        f.gravity = h->fin_scalars;
+        f.factor = h->fin_scalars + 3;
+        f.goal_both = h->fin_goal_both;
+        f.goal_a = h->fin_goal_a, f.goal_b = h->fin_goal_b;
+        f.nt = h->fin_nt;
+        f.tri = h->fin_tri, f.tri_col = h->fin_tri_col, f.opp = h->fin_opp;
+        f.vpos = h->fin_vpos, f.vnorm = h->fin_vnorm, f.tnorm = h->fin_tnorm, f.vvel = h->fin_vvel;
+        f.fric = h->fin_fric, f.damp = h->fin_damp;
+        f.leaf_start = h->fin_leaf_start, f.leaf_list = h->fin_leaf_list;
+        for (int a = 0; a < 3; ++a) f.leaf_lo[a] = h->fin_leaf_lo[a], f.leaf_dim[a] = h->fin_leaf_dim[a];
+        f.leaf_size = h->fin_leaf_size;
+        f.forget = h->layout.dx * 2.2f;
+        f.accept = h->layout.dx * 2.f;
+        auto table = [&](int s) {
+            col::VariantTable t;
+            t.key = h->var_key[s], t.bits = h->var_bits[s], t.acc = h->var_acc[s], t.vel = h->var_vel[s];
+            t.cap = h->var_cap;
+            return t;
+        };
+        A.vcur = table(h->gcur);
+        A.vnext = table(h->gcur ^ 1);
+    }
     A.n = h->n;
     A.L = h->layout;
     A.dt = dt;
@@ -1095,6 +1342,23 @@ StepArgs make_args(sv_handle *h, float dt, float3 g) {
 }
 
 unsigned particle_blocks(const sv_handle *h) { return (unsigned)sm_count() * (h->cta_per_sm ? h->cta_per_sm : 8); }
+
+// Launches the particle kernel of MODE in the handle's position form, with
+// the frame-input variant when one is loaded.
+template <int MODE> void launch_particles(sv_handle *h, const StepArgs &A) {
+    const unsigned blocks = particle_blocks(h);
+    if constexpr (MODE != MODE_G2P2G_LEARNED) {
+        if (h->fin_active) {
+            if (h->layout.position_form) k_particles<true, MODE, true><<<blocks, PT, 0, h->stream>>>(A);
+            else k_particles<false, MODE, true><<<blocks, PT, 0, h->stream>>>(A);
+            return;
+        }
+    }
+    if constexpr (MODE != MODE_G2P_ADVANCE) {
+        if (h->layout.position_form) k_particles<true, MODE><<<blocks, PT, 0, h->stream>>>(A);
+        else k_particles<false, MODE><<<blocks, PT, 0, h->stream>>>(A);
+    }
+}
 
 }  // namespace
 
@@ -1179,8 +1443,7 @@ cudaError_t launch_g2p_only(sv_handle *h) {
     A.adt = reinterpret_cast<adaptive::State *>(h->adt);
     A.keys_out = nullptr;
     Scoped s(h, "g2p");
-    if (h->layout.position_form) k_particles<true, MODE_G2P_ONLY><<<particle_blocks(h), PT, 0, h->stream>>>(A);
-    else k_particles<false, MODE_G2P_ONLY><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    launch_particles<MODE_G2P_ONLY>(h, A);
     k_dt_integrate<<<1, 1, 0, h->stream>>>(A.adt, h->counters, h->layout.dx);
     h->launches += 2;
     h->vel_side = h->gcur;
@@ -1192,8 +1455,7 @@ cudaError_t launch_advance(sv_handle *h) {
     StepArgs A = make_args(h, 0.f, make_float3(0.f, 0.f, 0.f));
     A.adt = reinterpret_cast<adaptive::State *>(h->adt);
     Scoped s(h, "advance");
-    if (h->layout.position_form) k_particles<true, MODE_ADVANCE><<<particle_blocks(h), PT, 0, h->stream>>>(A);
-    else k_particles<false, MODE_ADVANCE><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    launch_particles<MODE_ADVANCE>(h, A);
     k_adaptive_finish<<<1, 1, 0, h->stream>>>(A.adt, h->counters);
     h->launches += 2;
     h->cur ^= 1;
@@ -1206,21 +1468,76 @@ cudaError_t launch_p2g(sv_handle *h, float dt, float3 g) {
     A.map_next = h->blockmap[h->map_cur];
     A.grid_next = h->grid[h->gcur];
     A.keys_out = nullptr;
+    A.vnext = A.vcur;  // the standalone scatter fills the current grid and variants
     if (h->adaptive_active) A.adt = reinterpret_cast<adaptive::State *>(h->adt);
     Scoped s(h, "p2g");
-    if (h->layout.position_form) k_particles<true, MODE_P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
-    else k_particles<false, MODE_P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+    launch_particles<MODE_P2G>(h, A);
     h->launches += 1;
     return cudaGetLastError();
 }
 
 cudaError_t launch_grid_update(sv_handle *h, bool clear_next) {
     Scoped s(h, "grid_update");
+    col::VariantTable var{};
+    if (h->fin_active) {
+        var.key = h->var_key[h->gcur], var.bits = h->var_bits[h->gcur];
+        var.acc = h->var_acc[h->gcur], var.vel = h->var_vel[h->gcur], var.cap = h->var_cap;
+        k_variant_meld<<<elem_blocks(h->var_cap), ELEM_THREADS, 0, h->stream>>>(var, h->grid[h->gcur],
+                                                                                h->blockmap[h->map_cur], h->layout,
+                                                                                h->counters);
+        h->launches += 1;
+    }
     k_grid_update<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(
         h->grid[h->gcur], h->active[h->map_cur], clear_next ? h->grid[h->gcur ^ 1] : nullptr, h->capacity, h->layout,
-        h->counters, h->map_cur, h->map_next);
+        h->counters, h->map_cur, h->map_next, var);
     k_latch<<<1, 1, 0, h->stream>>>(h->counters, -1, -1, h->capacity);
     h->launches += 2;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_clear_variants(sv_handle *h, int which) {
+    if (!h->fin_active) return cudaSuccess;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(h->var_key[which], 0, (size_t)h->var_cap * sizeof(unsigned long long), h->stream)) ||
+        (e = cudaMemsetAsync(h->var_bits[which], 0, (size_t)h->var_cap * col::VK * sizeof(uint32_t), h->stream)) ||
+        (e = cudaMemsetAsync(h->var_acc[which], 0, (size_t)h->var_cap * col::VK * sizeof(float4), h->stream)))
+        return e;
+    return cudaSuccess;
+}
+
+cudaError_t launch_interpolate(sv_handle *h, double time) {
+    if (!h->fin_active) return cudaSuccess;
+    Scoped s(h, "interpolate");
+    FinDev f;
+    f.fps = h->fin_fps, f.frame = h->fin_frame, f.nv = h->fin_nv, f.nt = h->fin_nt;
+    for (int a = 0; a < 3; ++a) f.g_a[a] = h->fin_g_a[a], f.g_b[a] = h->fin_g_b[a];
+    f.va = h->fin_va, f.vb = h->fin_vb, f.fr_a = h->fin_fr_a, f.fr_b = h->fin_fr_b, f.dm_a = h->fin_dm_a, f.dm_b = h->fin_dm_b;
+    f.tri = h->fin_tri, f.vt_start = h->fin_vt_start, f.vt_list = h->fin_vt_list;
+    f.scalars = h->fin_scalars;
+    f.vpos = h->fin_vpos, f.vnorm = h->fin_vnorm, f.tnorm = h->fin_tnorm, f.fric = h->fin_fric, f.damp = h->fin_damp;
+    const adaptive::State *st = h->adaptive_active ? reinterpret_cast<const adaptive::State *>(h->adt) : nullptr;
+    k_interp_factor<<<1, 1, 0, h->stream>>>(f, time, st, h->counters);
+    h->launches += 1;
+    if (h->fin_nt) {
+        const unsigned b = elem_blocks(std::max<uint64_t>(3ull * h->fin_nv, h->fin_nt));
+        k_interp_vertices<<<b, ELEM_THREADS, 0, h->stream>>>(f, h->counters);
+        k_interp_triangles<<<elem_blocks(h->fin_nt), ELEM_THREADS, 0, h->stream>>>(f);
+        k_interp_vertex_normals<<<elem_blocks(h->fin_nv), ELEM_THREADS, 0, h->stream>>>(f);
+        h->launches += 3;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_g2p_advance(sv_handle *h, float dt) {
+    StepArgs A = make_args(h, dt, make_float3(0.f, 0.f, 0.f));
+    Scoped s(h, "g2p_advance");
+    launch_particles<MODE_G2P_ADVANCE>(h, A);
+    k_finish<<<1, 1, 0, h->stream>>>(h->counters);
+    h->launches += 2;
+    h->vel_side = h->gcur;
+    h->vel_map = h->map_cur;
+    h->cur ^= 1;
+    h->keys_valid = true;
     return cudaGetLastError();
 }
 
@@ -1229,15 +1546,12 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 g, bool write_keys, bool
     if (!write_keys) A.keys_out = nullptr;
     if (!use_perm) A.perm = nullptr;
     Scoped s(h, "g2p2g");
-    if (h->closure_mode == 1 && h->cl_trained) {
+    if (h->closure_mode == 1 && h->cl_trained && !h->fin_active) {
         A.closure_img = h->cl_img;
         A.closure_hull = reinterpret_cast<const closure::Hull *>(h->cl_hull);
-        if (h->layout.position_form) k_particles<true, MODE_G2P2G_LEARNED><<<particle_blocks(h), PT, 0, h->stream>>>(A);
-        else k_particles<false, MODE_G2P2G_LEARNED><<<particle_blocks(h), PT, 0, h->stream>>>(A);
-    } else if (h->layout.position_form) {
-        k_particles<true, MODE_G2P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+        launch_particles<MODE_G2P2G_LEARNED>(h, A);
     } else {
-        k_particles<false, MODE_G2P2G><<<particle_blocks(h), PT, 0, h->stream>>>(A);
+        launch_particles<MODE_G2P2G>(h, A);
     }
     k_finish<<<1, 1, 0, h->stream>>>(h->counters);
     h->launches += 2;

@@ -167,6 +167,72 @@ class InputConsts:
 
 
 @dataclass
+class FrameData:
+    """The inputs of frames a and b (xpu/src/frame_input.rs:33-65): gravity,
+    particle goals and triangle-mesh colliders.  Arrays in the caller's
+    particle order; b fields None means frame b = a (end of the input)."""
+
+    frames_per_second: int
+    frame: int
+    gravity_a: tuple = (0.0, 0.0, -9.8)
+    gravity_b: Optional[tuple] = None
+    goal_flags_a: Optional[np.ndarray] = None      # [n] u32 (HAS_GOAL read)
+    goal_flags_b: Optional[np.ndarray] = None
+    goal_positions_a: Optional[np.ndarray] = None  # [n, 3]
+    goal_positions_b: Optional[np.ndarray] = None
+    triangles: Optional[np.ndarray] = None         # [t, 3] u32
+    triangle_collider: Optional[np.ndarray] = None  # [t] u32 (0..15)
+    vertex_positions_a: Optional[np.ndarray] = None  # [v, 3]
+    vertex_positions_b: Optional[np.ndarray] = None
+    friction_a: Optional[np.ndarray] = None        # [t]
+    friction_b: Optional[np.ndarray] = None
+    damping_a: Optional[np.ndarray] = None         # [t]
+    damping_b: Optional[np.ndarray] = None
+    leaf_size: float = 1.0
+
+    @property
+    def has_b(self) -> bool:
+        return self.gravity_b is not None
+
+    def to_struct(self, cls):
+        """The C struct (sv_frame_input or the oracle's twin) and the arrays
+        it points into (keep them alive while the struct is used)."""
+        keep = {}
+
+        def arr(name, dtype, shape_last=None):
+            a = getattr(self, name)
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype)
+            keep[name] = a
+            return a
+
+        s = cls()
+        s.frames_per_second = int(self.frames_per_second)
+        s.frame = int(self.frame)
+        s.has_b = 1 if self.has_b else 0
+        for k in range(3):
+            s.gravity_a[k] = float(self.gravity_a[k])
+            s.gravity_b[k] = float((self.gravity_b or self.gravity_a)[k])
+        u32 = ct.POINTER(ct.c_uint32)
+        f32 = ct.POINTER(ct.c_float)
+        for name, dtype, typ in (("goal_flags_a", np.uint32, u32), ("goal_flags_b", np.uint32, u32),
+                                 ("goal_positions_a", np.float32, f32), ("goal_positions_b", np.float32, f32),
+                                 ("triangles", np.uint32, u32), ("triangle_collider", np.uint32, u32),
+                                 ("vertex_positions_a", np.float32, f32), ("vertex_positions_b", np.float32, f32),
+                                 ("friction_a", np.float32, f32), ("friction_b", np.float32, f32),
+                                 ("damping_a", np.float32, f32), ("damping_b", np.float32, f32)):
+            a = arr(name, dtype)
+            setattr(s, name, a.ctypes.data_as(typ) if a is not None else ct.cast(None, typ))
+        tri = keep.get("triangles")
+        s.n_triangles = 0 if tri is None else tri.size // 3
+        v = keep.get("vertex_positions_a")
+        s.n_vertices = 0 if v is None else v.size // 3
+        s.leaf_size = float(self.leaf_size)
+        return s, keep
+
+
+@dataclass
 class Extras:
     """Options the reference does not have: a grid boundary plane, the
     int32-cell + fp32-offset position form, the fp64 SVD policy and the grid
@@ -235,11 +301,35 @@ class CudaState:
         self._lib = _abi.load()
         self._h = handle
         self.n = n
-        self.time = time
         self.consts = consts
         self.extras = extras
         self._initial_positions = initial_positions
         self._template = template
+        self._frame_keep = None
+        self.time = time
+
+    # the simulation time lives in the handle (sv_step advances it)
+    @property
+    def time(self) -> float:
+        t = ct.c_double(0.0)
+        check(self._lib.sv_get_time(self._h, ct.byref(t)))
+        return float(t.value)
+
+    @time.setter
+    def time(self, t: float):
+        if float(t) != self.time:
+            check(self._lib.sv_set_time(self._h, float(t)))
+
+    def set_frame_input(self, frame: Optional["FrameData"]):
+        """Loads the inputs of frames a and b (gravity, goals, colliders);
+        None removes them.  See sv_set_frame_input in the C header."""
+        if frame is None:
+            check(self._lib.sv_set_frame_input(self._h, None))
+            self._frame_keep = None
+            return
+        s, keep = frame.to_struct(_abi.SvFrameInput)
+        check(self._lib.sv_set_frame_input(self._h, ct.byref(s)))
+        self._frame_keep = keep
 
     # -- from_io_state (cpu_state.rs:25-66)
     @staticmethod
@@ -323,7 +413,6 @@ class CudaState:
         if params.adaptive_time_steps:
             status, done, t = self.step_adaptive(params.target_time, params.max_time_step, frame_input.gravity,
                                                  harness)
-            self.time = t
             error = None
             if status & _abi.SV_STATUS_PARTICLE_INVERTED:
                 error = EnergyError("The position gradient has negative determinant")
@@ -333,7 +422,8 @@ class CudaState:
         dt = np.float32(params.max_time_step)
         if dt == 0:
             raise ZeroTimeStep("The time step ended up being 0")
-        # the reference accumulates time in f64 one substep at a time
+        # the reference accumulates time in f64 one substep at a time; the
+        # handle does the same (and does not count a failed substep)
         t = self.time
         n = 0
         while t < params.target_time:
@@ -342,13 +432,7 @@ class CudaState:
         status, done = self.step(n, float(dt), frame_input.gravity, harness)
         error = None
         if status & _abi.SV_STATUS_PARTICLE_INVERTED:
-            # time is not advanced for the substep that failed (cpu_state.rs:178-183)
-            for _ in range(max(done - 1, 0)):
-                self.time += float(dt)
             error = EnergyError("The position gradient has negative determinant")
-        else:
-            for _ in range(done):
-                self.time += float(dt)
         if status & _abi.SV_STATUS_CANCELED:
             raise Canceled("The computation was canceled")
         return self.to_io_state(params.store_grid), error
