@@ -55,6 +55,25 @@ def test_struct_layouts_match_c(tmp_path):
                                                  SvParticles.plastic_j.offset]
 
 
+def test_frame_input_layout_matches_c_and_the_oracle(tmp_path):
+    from oracle.oracle import OFrameInput
+    from squishy_volumes_gb300._abi import SvFrameInput
+
+    fields = [f[0] for f in SvFrameInput._fields_]
+    assert fields == [f[0] for f in OFrameInput._fields_]
+    src = tmp_path / "frame.c"
+    lines = "".join(f'  printf("%zu ", offsetof(sv_frame_input, {f}));\n' for f in fields)
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "squishy_volumes_cuda.h"\n'
+                   "int main(void) {\n" + lines + '  printf("%zu\\n", sizeof(sv_frame_input));\n  return 0;\n}\n')
+    exe = tmp_path / "frame"
+    r = subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("gcc unavailable: " + r.stderr)
+    vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    assert vals[:-1] == [getattr(SvFrameInput, f).offset for f in fields]
+    assert vals[-1] == ct.sizeof(SvFrameInput) == ct.sizeof(OFrameInput)
+
+
 def test_oracle_is_not_linked_by_the_product():
     """The product library must not depend on the CPU oracle."""
     from squishy_volumes_gb300 import build
