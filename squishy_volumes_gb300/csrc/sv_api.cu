@@ -189,6 +189,9 @@ int standalone_p2g(sv_handle *h, float dt, float3 g) {
         SV_CUDA(launch_clear_variants(h, h->gcur));
     }
     SV_CUDA(launch_p2g(h, dt, g));
+    // a scatter that failed (e.g. a record outside the claimed blocks) stops
+    // the passes that would gather from it
+    SV_CUDA(launch_latch(h));
     h->pending_valid = true;
     h->pending_dt = dt;
     h->pending_g[0] = g.x, h->pending_g[1] = g.y, h->pending_g[2] = g.z;
@@ -231,7 +234,9 @@ int fused_substep(sv_handle *h, float dt, float3 g, double t_next = 0.0) {
         SV_CUDA(launch_interpolate(h, t_next));
         SV_CUDA(launch_clear_variants(h, h->gcur ^ 1));
     }
-    SV_CUDA(launch_grid_update(h, true));
+    // the plain pass latches its own stop bits, so after it (or after the
+    // binning's block claims) the grid update needs no latch of its own
+    SV_CUDA(launch_grid_update(h, true, !h->stop_latched));
     const bool write_keys = h->since_sort + 1 >= h->sort_interval;
     SV_CUDA(launch_g2p2g(h, dt, g, write_keys, h->need_perm));
     h->need_perm = false;
@@ -258,7 +263,7 @@ int run_period_graph(sv_handle *h, float dt, float3 g) {
         // host bookkeeping before the period, put back if the capture fails
         const int cur0 = h->cur, gcur0 = h->gcur, map_cur0 = h->map_cur, map_next0 = h->map_next;
         const int vel_side0 = h->vel_side, vel_map0 = h->vel_map;
-        const bool keys_valid0 = h->keys_valid, need_perm0 = h->need_perm;
+        const bool keys_valid0 = h->keys_valid, need_perm0 = h->need_perm, stop_latched0 = h->stop_latched;
         const uint32_t since0 = h->since_sort;
         const uint64_t l0 = h->launches, sorts0 = h->sorts;
         cudaGraph_t graph = nullptr;
@@ -280,6 +285,7 @@ int run_period_graph(sv_handle *h, float dt, float3 g) {
             h->cur = cur0, h->gcur = gcur0, h->map_cur = map_cur0, h->map_next = map_next0;
             h->vel_side = vel_side0, h->vel_map = vel_map0;
             h->keys_valid = keys_valid0, h->need_perm = need_perm0, h->since_sort = since0;
+            h->stop_latched = stop_latched0;
             h->launches = l0, h->sorts = sorts0;
             h->use_graphs = false;
             for (uint32_t s = 0; s < key.period; ++s)
@@ -291,6 +297,7 @@ int run_period_graph(sv_handle *h, float dt, float3 g) {
         st.cur = h->cur, st.gcur = h->gcur, st.map_cur = h->map_cur, st.map_next = h->map_next;
         st.vel_side = h->vel_side, st.vel_map = h->vel_map;
         st.keys_valid = h->keys_valid, st.need_perm = h->need_perm, st.since_sort = h->since_sort;
+        st.stop_latched = h->stop_latched;
         st.launches = h->launches - l0;
         it = h->graphs.emplace(key, st).first;
         h->launches = l0;
@@ -301,6 +308,7 @@ int run_period_graph(sv_handle *h, float dt, float3 g) {
     h->cur = st.cur, h->gcur = st.gcur, h->map_cur = st.map_cur, h->map_next = st.map_next;
     h->vel_side = st.vel_side, h->vel_map = st.vel_map;
     h->keys_valid = st.keys_valid, h->need_perm = st.need_perm, h->since_sort = st.since_sort;
+    h->stop_latched = st.stop_latched;
     h->launches += st.launches;
     h->sorts += 1;
     h->graph_launches += 1;
@@ -670,6 +678,9 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
         const uint32_t st = h->host_counters[C_STATUS];
         done = h->host_counters[C_SUBSTEPS] - base;
         for (; timed < done; ++timed) h->time += (double)dt;  // cpu_state.rs:186-189
+        // passes that ran stopped left the state as it was but wrote no
+        // binning keys: the next binning computes them afresh
+        if (st & STOP_MASK) h->keys_valid = false;
         if (st & ST_OUT_OF_GRID) return fail("sv_step: a live particle left the grid block index");
         if (h->host_counters[C_CLOSURE_ERR]) return fail("sv_step: a tensor-core wait of the learned closure timed out");
         if (st & ST_VARIANT_FULL) return fail("sv_step: the collider variant table is full");
@@ -690,7 +701,8 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
                                     h->stream));
             SV_CUDA(cudaStreamSynchronize(h->stream));
             h->pending_valid = false;
-            continue;
+            // an inversion in the same substeps is still reported below
+            if (!(st & ST_INVERTED)) continue;
         }
         if (h->adaptive_interval && todo > 0) {
             // Bin more often when many gathers miss their shared tile, less
@@ -824,7 +836,7 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
             h->host_counters[C_STATUS] &= ~ST_CAPACITY;
             SV_CUDA(cudaMemcpyAsync(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice,
                                     h->stream));
-            continue;
+            if (!(stw & ST_INVERTED)) continue;
         }
         if (stw & ST_INVERTED) {
             status |= SV_STATUS_PARTICLE_INVERTED;

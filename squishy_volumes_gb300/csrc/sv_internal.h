@@ -48,7 +48,8 @@ enum Counter : int {
     C_CLOSURE = 9,       // snow/sand particle-substeps through the learned closure
     C_CLOSURE_FB = 10,   // snow/sand particle-substeps that fell back to the return map
     C_CLOSURE_ERR = 11,  // a tensor-core wait of the learned closure gave up
-    C_COUNT = 12,
+    C_CTA_DONE = 12,     // CTAs of a self-latching particle pass that have finished
+    C_COUNT = 13,
 };
 
 // One side of the particle state (ping-pong).  Structure of arrays: pos and
@@ -82,6 +83,25 @@ struct GridLayout {
     uint32_t svd_policy;
     int key_bits;
 };
+
+// Grid node velocity from its momentum (meld_grid.rs:61-66: v = p / m, or 0
+// when m <= 0), then the boundary plane (an addition, not in the reference)
+// at global node (x, y, z).  Shared by the grid update and the variant meld.
+__host__ __device__ inline float4 node_velocity(float4 g, int x, int y, int z, const GridLayout &L) {
+    const float m = g.w;
+    float vx = 0.f, vy = 0.f, vz = 0.f;
+    if (m > 0.f) vx = g.x / m, vy = g.y / m, vz = g.z / m;
+    if (L.ground_mode != 0) {
+        const int node[3] = {x, y, z};
+        if ((float)node[L.ground_axis] * L.dx <= L.ground_height) {
+            if (L.ground_mode == 1) vx = vy = vz = 0.f;
+            else if (L.ground_axis == 0) vx = fmaxf(vx, 0.f);
+            else if (L.ground_axis == 1) vy = fmaxf(vy, 0.f);
+            else vz = fmaxf(vz, 0.f);
+        }
+    }
+    return make_float4(vx, vy, vz, m);
+}
 
 struct KernelTimer {
     std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -140,6 +160,9 @@ struct sv_handle {
 
     uint32_t *counters = nullptr;       // device [C_COUNT]
     uint32_t *host_counters = nullptr;  // pinned mirror
+    // C_STOP will hold the stop bits of every kernel queued so far (the last
+    // status-setting launch was a latch or a self-latching particle pass)
+    bool stop_latched = false;
 
     cudaStream_t stream = nullptr;      // stream all work is queued on
     cudaStream_t own_stream = nullptr;  // the handle's own stream
@@ -174,7 +197,7 @@ struct sv_handle {
     struct GraphState {  // host-side state after the period
         cudaGraphExec_t exec = nullptr;
         int cur, gcur, map_cur, map_next, vel_side, vel_map;
-        bool keys_valid, need_perm;
+        bool keys_valid, need_perm, stop_latched;
         uint32_t since_sort;
         uint64_t launches;
     };
@@ -239,8 +262,14 @@ cudaError_t launch_keys(sv_handle *h);
 cudaError_t launch_sort_and_segments(sv_handle *h);
 cudaError_t launch_activate(sv_handle *h, int which);
 cudaError_t launch_clear(sv_handle *h, int grid_side, int which);
+// latches the status word's stop bits for the kernels that follow
+cudaError_t launch_latch(sv_handle *h);
 cudaError_t launch_p2g(sv_handle *h, float dt, float3 gravity);
-cudaError_t launch_grid_update(sv_handle *h, bool clear_next);
+// latch = false: the stop bits are already latched (by the particle pass
+// before it, or by the binning's block claims)
+cudaError_t launch_grid_update(sv_handle *h, bool clear_next, bool latch = true);
+// Without a frame input the pass latches the stop bits and counts the
+// substep itself (its last CTA), so no k_latch / k_finish launches follow.
 cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 gravity, bool write_keys, bool use_perm);
 // adaptive time steps (the unfused substep)
 cudaError_t launch_limits_force(sv_handle *h);

@@ -89,6 +89,7 @@ struct StepArgs {
     adaptive::State *adt;                // adaptive time steps: device dt and reductions (else nullptr)
     col::FrameArgs fa;                   // frame input (kernels instantiated with FIN only)
     col::VariantTable vcur, vnext;       // collider variants gathered from / scattered into
+    bool self_latch;                     // the last CTA latches the stop bits and counts the substep
     uint64_t n;
     GridLayout L;
     float dt;
@@ -420,25 +421,14 @@ __global__ void __launch_bounds__(ELEM_THREADS)
                             g.x += a.x, g.y += a.y, g.z += a.z, g.w += a.w;
                         }
             }
-            // meld_grid.rs:61-66: v = p / m, or 0 when m <= 0
-            float m = g.w;
-            float vx = 0.f, vy = 0.f, vz = 0.f;
-            if (m > 0.f) vx = g.x / m, vy = g.y / m, vz = g.z / m;
+            int x = 0, y = 0, z = 0;
             if (L.ground_mode != 0) {
-                // Addition (not in the reference): boundary plane at node height.
                 int bx, by, bz;
                 block_coords(active_cur[i >> 6], L, bx, by, bz);
-                int l = (int)(i & 63);
-                int node[3] = {L.origin[0] + 4 * bx + (l >> 4), L.origin[1] + 4 * by + ((l >> 2) & 3),
-                               L.origin[2] + 4 * bz + (l & 3)};
-                if ((float)node[L.ground_axis] * L.dx <= L.ground_height) {
-                    if (L.ground_mode == 1) vx = vy = vz = 0.f;
-                    else if (L.ground_axis == 0) vx = fmaxf(vx, 0.f);
-                    else if (L.ground_axis == 1) vy = fmaxf(vy, 0.f);
-                    else vz = fmaxf(vz, 0.f);
-                }
+                const int l = (int)(i & 63);
+                x = L.origin[0] + 4 * bx + (l >> 4), y = L.origin[1] + 4 * by + ((l >> 2) & 3), z = L.origin[2] + 4 * bz + (l & 3);
             }
-            grid_cur[i] = make_float4(vx, vy, vz, m);
+            grid_cur[i] = node_velocity(g, x, y, z, L);
         }
         if (i < sn * 64) grid_next[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
@@ -469,16 +459,7 @@ __global__ void __launch_bounds__(ELEM_THREADS)
             float4 g = make_float4(a[j].x + base.x, a[j].y + base.y, a[j].z + base.z, a[j].w + base.w);
             for (int o = 0; o < col::VK; ++o)
                 if (o != j && b[o] && col::compatible(b[j], b[o])) g.x += a[o].x, g.y += a[o].y, g.z += a[o].z, g.w += a[o].w;
-            const float m = g.w;
-            float vx = 0.f, vy = 0.f, vz = 0.f;
-            if (m > 0.f) vx = g.x / m, vy = g.y / m, vz = g.z / m;
-            if (L.ground_mode != 0 && (float)node[L.ground_axis] * L.dx <= L.ground_height) {
-                if (L.ground_mode == 1) vx = vy = vz = 0.f;
-                else if (L.ground_axis == 0) vx = fmaxf(vx, 0.f);
-                else if (L.ground_axis == 1) vy = fmaxf(vy, 0.f);
-                else vz = fmaxf(vz, 0.f);
-            }
-            var.vel[e * col::VK + j] = make_float4(vx, vy, vz, m);
+            var.vel[e * col::VK + j] = node_velocity(g, node[0], node[1], node[2], L);
         }
     }
 }
@@ -766,6 +747,28 @@ struct SharedLearned {
 };
 static_assert(sizeof(Rec) * PT >= tc::NIN * PT * 2 + tc::NH * PT * 2, "closure operands overlay the records");
 
+// End of a self-latching pass (one call per CTA, by all its threads): the
+// last CTA to finish latches the stop bits for the kernels that follow and
+// counts the substep unless the pass started stopped -- the work of k_latch
+// and k_finish without their launches.  Every status bit of the CTA is set
+// before the barrier; thread 0's fence then orders them before its ticket.
+__device__ __forceinline__ void cta_done(const StepArgs &A, uint32_t stop_at_start) {
+    if (!A.self_latch) return;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const uint32_t ticket = atomicAdd(&A.counters[C_CTA_DONE], 1u);
+        if (ticket == gridDim.x - 1) {
+            __threadfence();
+            const uint32_t status = *(volatile uint32_t *)&A.counters[C_STATUS];
+            A.counters[C_STOP] = status & STOP_MASK;
+            if (!stop_at_start) A.counters[C_SUBSTEPS] += 1;
+            A.counters[C_CTA_DONE] = 0;
+        }
+    }
+}
+
 // Five CTAs per SM (at most 102 registers): measured faster than the
 // unconstrained 150-register build despite a few spilled values.  The
 // learned-closure variant holds the network image as well: four CTAs.
@@ -782,12 +785,14 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
     constexpr bool LOAD_VC = MODE == MODE_P2G || MODE == MODE_ADVANCE;  // v and C from the state
     __shared__ Shared sh;
     __shared__ typename std::conditional<LEARNED, SharedLearned, int>::type shl;
-    if (stopped(A.counters)) {
+    const uint32_t stop_at_start = stopped(A.counters);
+    if (stop_at_start) {
         if (G2P) {
             // Keep the state as it is (identity copy) so the buffer swap is a no-op.
             for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x)
                 copy_particle(A.in, A.out, A.n, i, i, CELL);
         }
+        cta_done(A, stop_at_start);
         return;
     }
     mlp::Phase ph;
@@ -1190,6 +1195,7 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
         if (n_closure_fb) atomicAdd(&A.counters[C_CLOSURE_FB], n_closure_fb);
     }
     if constexpr (LEARNED) mlp::ctl_finish(shl.ctl, mlp::TMEM_COLS_INFER, &A.counters[C_CLOSURE_ERR]);
+    cta_done(A, 0u);
 }
 
 __global__ void k_finish(uint32_t *counters) {
@@ -1303,6 +1309,7 @@ StepArgs make_args(sv_handle *h, float dt, float3 g) {
     A.map_next = h->blockmap[h->map_next];
     A.grid_cur = h->grid[h->gcur];
     A.grid_next = h->grid[h->gcur ^ 1];
+    A.self_latch = false;
     A.keys_out = h->keys;
     A.closure_img = nullptr;
     A.closure_hull = nullptr;
@@ -1347,6 +1354,7 @@ unsigned particle_blocks(const sv_handle *h) { return (unsigned)sm_count() * (h-
 // the frame-input variant when one is loaded.
 template <int MODE> void launch_particles(sv_handle *h, const StepArgs &A) {
     const unsigned blocks = particle_blocks(h);
+    h->stop_latched = A.self_latch;
     if constexpr (MODE != MODE_G2P2G_LEARNED) {
         if (h->fin_active) {
             if (h->layout.position_form) k_particles<true, MODE, true><<<blocks, PT, 0, h->stream>>>(A);
@@ -1379,6 +1387,7 @@ cudaError_t launch_keys(sv_handle *h) {
     if (h->layout.position_form) k_keys<true><<<elem_blocks(h->n), ELEM_THREADS, 0, h->stream>>>(A);
     else k_keys<false><<<elem_blocks(h->n), ELEM_THREADS, 0, h->stream>>>(A);
     h->keys_valid = true;
+    h->stop_latched = false;  // may set ST_OUT_OF_GRID
     h->launches += 1;
     return cudaGetLastError();
 }
@@ -1418,6 +1427,14 @@ cudaError_t launch_activate(sv_handle *h, int which) {
         h->seg_block, h->blockmap[which], h->active[which], h->capacity, h->layout, h->counters, which);
     k_latch<<<1, 1, 0, h->stream>>>(h->counters, -1, which, h->capacity);
     h->launches += 4;
+    h->stop_latched = true;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_latch(sv_handle *h) {
+    k_latch<<<1, 1, 0, h->stream>>>(h->counters, -1, -1, h->capacity);
+    h->launches += 1;
+    h->stop_latched = true;
     return cudaGetLastError();
 }
 
@@ -1476,7 +1493,7 @@ cudaError_t launch_p2g(sv_handle *h, float dt, float3 g) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_grid_update(sv_handle *h, bool clear_next) {
+cudaError_t launch_grid_update(sv_handle *h, bool clear_next, bool latch) {
     Scoped s(h, "grid_update");
     col::VariantTable var{};
     if (h->fin_active) {
@@ -1490,8 +1507,12 @@ cudaError_t launch_grid_update(sv_handle *h, bool clear_next) {
     k_grid_update<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(
         h->grid[h->gcur], h->active[h->map_cur], clear_next ? h->grid[h->gcur ^ 1] : nullptr, h->capacity, h->layout,
         h->counters, h->map_cur, h->map_next, var);
-    k_latch<<<1, 1, 0, h->stream>>>(h->counters, -1, -1, h->capacity);
-    h->launches += 2;
+    h->launches += 1;
+    if (latch) {
+        k_latch<<<1, 1, 0, h->stream>>>(h->counters, -1, -1, h->capacity);
+        h->launches += 1;
+        h->stop_latched = true;
+    }
     return cudaGetLastError();
 }
 
@@ -1545,6 +1566,7 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 g, bool write_keys, bool
     StepArgs A = make_args(h, dt, g);
     if (!write_keys) A.keys_out = nullptr;
     if (!use_perm) A.perm = nullptr;
+    A.self_latch = !h->fin_active;
     Scoped s(h, "g2p2g");
     if (h->closure_mode == 1 && h->cl_trained && !h->fin_active) {
         A.closure_img = h->cl_img;
@@ -1553,8 +1575,11 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 g, bool write_keys, bool
     } else {
         launch_particles<MODE_G2P2G>(h, A);
     }
-    k_finish<<<1, 1, 0, h->stream>>>(h->counters);
-    h->launches += 2;
+    h->launches += 1;
+    if (!A.self_latch) {
+        k_finish<<<1, 1, 0, h->stream>>>(h->counters);
+        h->launches += 1;
+    }
     h->vel_side = h->gcur;
     h->vel_map = h->map_cur;
     h->cur ^= 1;
