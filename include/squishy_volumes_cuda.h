@@ -364,6 +364,89 @@ int sv_closure_set_mode(sv_handle *h, int mode);
 int sv_closure_evaluate(sv_handle *h, float dt, double out[8]);
 int sv_closure_get_params(sv_handle *h, float *params);
 
+/* ---- Frame files and the frame cache ----------------------------------
+ *
+ *   reference                                                  | entry point here
+ *   -----------------------------------------------------------+-----------------------------
+ *   IoState::write / IoState::read (file_frame/src/io_state.rs:31-75),
+ *     magic and version (file_util/src/lib.rs:27-99)            | sv_frame_write, sv_frame_read
+ *   StoreThread::new / store / check / drop
+ *     (cache/src/store_thread.rs:27-110), frame_path (cache/src/util.rs:9-11) |
+ *                                                              | sv_cache_open, sv_cache_store,
+ *                                                              | sv_cache_store_frame, sv_cache_check,
+ *                                                              | sv_cache_flush, sv_cache_close
+ *
+ * A frame file is the reference's: 32 magic bytes, 64 version bytes (the
+ * version string, zero padded; the reader demands the same string), then
+ * IoState { time, particles, grid_nodes } serialised by bincode 1.3.3 with
+ * its default options (little endian, fixed-width integers, u64 sequence
+ * lengths, u32 enum variant indices, u8 Option tags).  `version` NULL means
+ * SV_FRAME_VERSION, the reference's file_util crate version.
+ *
+ * sv_frame describes one IoState.  ParticleParameters (particles.rs:55-90) is
+ * spread into arrays: viscosity is Some where flags has SV_USE_VISCOSITY,
+ * the variant is Fluid { exponent, bulk_modulus } where flags has
+ * SV_IS_FLUID and Solid { mu, lambda, sand_alpha } otherwise, sand_alpha
+ * Some where flags has SV_USE_SAND_ALPHA.  (The file has no room for this
+ * library's additional models: it stores their mu and lambda as a Solid.)
+ * Unused arrays may be NULL when writing (their entries are written as 0).
+ * node_* arrays describe GridNodes (grid_nodes.rs:10-15) when has_grid.
+ *
+ * sv_frame_read: with every array pointer NULL it fills time, n, has_grid
+ * and n_nodes only; otherwise n and n_nodes must equal the file's and every
+ * array is filled (the parameter arrays with 0 where the variant or the
+ * Option leaves them unused). */
+#define SV_FRAME_VERSION "0.3.4"
+typedef struct sv_frame {
+    double time;
+    uint64_t n;
+    uint32_t *flags;
+    float *mass, *initial_volume;
+    float *viscosity_dynamic, *viscosity_bulk;
+    float *mu, *lambda, *sand_alpha;
+    int32_t *exponent;
+    float *bulk_modulus;
+    float *elastic_energies;
+    uint32_t *collider_bits;
+    float *positions, *position_gradients, *velocities, *velocity_gradients, *initial_positions;
+    uint32_t has_grid;
+    uint64_t n_nodes;
+    int32_t *node_ids;
+    uint32_t *node_collider_bits;
+    float *node_masses, *node_velocities;
+} sv_frame;
+
+int sv_frame_write(const char *path, const sv_frame *frame, const char *version, uint64_t *bytes_written);
+int sv_frame_read(const char *path, const char *version, sv_frame *frame);
+
+/* The frame cache: frames go to <dir>/frame_%05u.bin, numbered from
+ * first_frame, by a writer thread.  `statics` gives what the substep never
+ * changes and every frame repeats: n, the parameter arrays and
+ * initial_positions, in the original particle order (NULL arrays are
+ * written as 0; the stored flags select the variants as above).
+ *
+ * sv_cache_store queues the copy of the handle's current state (and, when
+ * store_grid, of the grid its last substep gathered, with the collider
+ * variants) on the handle's stream and returns without waiting; the writer
+ * thread waits for the copy, restores the original particle order and
+ * writes the file.  The handle's next kernels wait for the copy (not for the
+ * file).  At most `depth` frames are in flight; a further store waits for
+ * the oldest.  sv_cache_store_frame queues a copy of a host frame.
+ * sv_cache_check returns -1 with the message once the writer has failed
+ * (StoreThread::check); sv_cache_flush waits until every queued frame is
+ * on disk; sv_cache_info reports frames written and their bytes
+ * (total_bytes_on_disk, available_frames).  sv_cache_close flushes and
+ * ends the thread. */
+typedef struct sv_cache sv_cache;
+int sv_cache_open(const char *dir, const char *version, const sv_frame *statics, uint32_t first_frame, uint32_t depth,
+                  sv_cache **out);
+int sv_cache_store(sv_cache *c, sv_handle *h, int store_grid);
+int sv_cache_store_frame(sv_cache *c, const sv_frame *frame);
+int sv_cache_check(sv_cache *c);
+int sv_cache_flush(sv_cache *c);
+int sv_cache_info(sv_cache *c, uint64_t *frames_written, uint64_t *bytes_written);
+int sv_cache_close(sv_cache *c);
+
 #ifdef __cplusplus
 }
 #endif

@@ -123,7 +123,47 @@ class SvFrameInput(ct.Structure):
     ]
 
 
+class SvFrame(ct.Structure):
+    _fields_ = [
+        ("time", ct.c_double),
+        ("n", ct.c_uint64),
+        ("flags", u32p),
+        ("mass", f32p),
+        ("initial_volume", f32p),
+        ("viscosity_dynamic", f32p),
+        ("viscosity_bulk", f32p),
+        ("mu", f32p),
+        ("lambda_", f32p),
+        ("sand_alpha", f32p),
+        ("exponent", i32p),
+        ("bulk_modulus", f32p),
+        ("elastic_energies", f32p),
+        ("collider_bits", u32p),
+        ("positions", f32p),
+        ("position_gradients", f32p),
+        ("velocities", f32p),
+        ("velocity_gradients", f32p),
+        ("initial_positions", f32p),
+        ("has_grid", ct.c_uint32),
+        ("n_nodes", ct.c_uint64),
+        ("node_ids", i32p),
+        ("node_collider_bits", u32p),
+        ("node_masses", f32p),
+        ("node_velocities", f32p),
+    ]
+
+
 _SIGNATURES = {
+    "sv_frame_write": (ct.c_int, [ct.c_char_p, ct.POINTER(SvFrame), ct.c_char_p, ct.POINTER(ct.c_uint64)]),
+    "sv_frame_read": (ct.c_int, [ct.c_char_p, ct.c_char_p, ct.POINTER(SvFrame)]),
+    "sv_cache_open": (ct.c_int, [ct.c_char_p, ct.c_char_p, ct.POINTER(SvFrame), ct.c_uint32, ct.c_uint32,
+                                 ct.POINTER(ct.c_void_p)]),
+    "sv_cache_store": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_int]),
+    "sv_cache_store_frame": (ct.c_int, [ct.c_void_p, ct.POINTER(SvFrame)]),
+    "sv_cache_check": (ct.c_int, [ct.c_void_p]),
+    "sv_cache_flush": (ct.c_int, [ct.c_void_p]),
+    "sv_cache_info": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_uint64), ct.POINTER(ct.c_uint64)]),
+    "sv_cache_close": (ct.c_int, [ct.c_void_p]),
     "sv_create": (ct.c_int, [ct.POINTER(SvConsts), ct.POINTER(SvParticles), ct.POINTER(ct.c_void_p)]),
     "sv_step": (
         ct.c_int,

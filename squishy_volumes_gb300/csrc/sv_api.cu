@@ -343,6 +343,8 @@ void set_last_error(const std::string &msg) { g_last_error = msg; }
 
 void drop_graphs(sv_handle *h) { clear_graphs(h); }
 
+int refresh_counters(sv_handle *h) { return read_counters(h); }
+
 }  // namespace sv
 
 extern "C" {
@@ -895,57 +897,18 @@ int sv_download(sv_handle *h, sv_particles *o) {
     if (o->n != h->n) return fail("sv_download: particle count mismatch");
     const uint64_t n = h->n;
     const ParticleArrays &a = h->side[h->cur];
-    const bool cell = h->layout.position_form == 1;
     std::vector<float4> pos(n), vel(n);
-    std::vector<int4> cellv(cell ? n : 0);
+    std::vector<int4> cellv(h->layout.position_form == 1 ? n : 0);
     std::vector<float> C(9 * n), F(9 * n), en(n);
-    std::vector<uint32_t> orig(n);
+    std::vector<uint32_t> orig(n), cbits(a.cbits_done ? n : 0);
+    HostParticles hp;
+    hp.n = n;
+    hp.pos = pos.data(), hp.vel = vel.data(), hp.cell = cellv.empty() ? nullptr : cellv.data();
+    hp.C = C.data(), hp.F = F.data(), hp.energy = en.data();
+    hp.orig = orig.data(), hp.cbits = cbits.empty() ? nullptr : cbits.data();
+    SV_CUDA(copy_particles_async(h, hp));
     SV_CUDA(cudaStreamSynchronize(h->stream));
-    SV_CUDA(cudaMemcpy(pos.data(), a.pos, n * 16, cudaMemcpyDeviceToHost));
-    if (cell) SV_CUDA(cudaMemcpy(cellv.data(), a.cell, n * 16, cudaMemcpyDeviceToHost));
-    SV_CUDA(cudaMemcpy(vel.data(), a.vel, n * 16, cudaMemcpyDeviceToHost));
-    SV_CUDA(cudaMemcpy(C.data(), a.C, 9 * n * 4, cudaMemcpyDeviceToHost));
-    SV_CUDA(cudaMemcpy(F.data(), a.F, 9 * n * 4, cudaMemcpyDeviceToHost));
-    SV_CUDA(cudaMemcpy(en.data(), a.energy, n * 4, cudaMemcpyDeviceToHost));
-    SV_CUDA(cudaMemcpy(orig.data(), a.orig, n * 4, cudaMemcpyDeviceToHost));
-    std::vector<uint32_t> cbits;
-    if (a.cbits_done) {
-        cbits.resize(n);
-        SV_CUDA(cudaMemcpy(cbits.data(), a.cbits_done, n * 4, cudaMemcpyDeviceToHost));
-    }
-    const double dx = h->layout.dx;
-    for (uint64_t s = 0; s < n; ++s) {
-        const uint64_t i = orig[s];
-        if (i >= n) return fail("sv_download: corrupt original index");
-        uint32_t packed;
-        std::memcpy(&packed, &pos[s].w, 4);
-        if (o->flags) o->flags[i] = packed & FLAG_MASK;
-        if (o->positions) {
-            if (!cell) {
-                o->positions[3 * i] = pos[s].x, o->positions[3 * i + 1] = pos[s].y, o->positions[3 * i + 2] = pos[s].z;
-            } else {
-                // back to the scene's own coordinates
-                const uint32_t mi = packed >> MATERIAL_SHIFT;
-                const SceneInfo &sc = h->host_scenes[mi < h->host_materials.size() ? h->host_materials[mi].scene : 0];
-                o->positions[3 * i] = (float)(((double)(cellv[s].x - sc.off[0]) + pos[s].x) * dx);
-                o->positions[3 * i + 1] = (float)(((double)(cellv[s].y - sc.off[1]) + pos[s].y) * dx);
-                o->positions[3 * i + 2] = (float)(((double)(cellv[s].z - sc.off[2]) + pos[s].z) * dx);
-            }
-        }
-        if (o->velocities) o->velocities[3 * i] = vel[s].x, o->velocities[3 * i + 1] = vel[s].y, o->velocities[3 * i + 2] = vel[s].z;
-        if (o->plastic_j) o->plastic_j[i] = vel[s].w;
-        for (int k = 0; k < 9; ++k) {
-            if (o->position_gradients) o->position_gradients[9 * i + k] = F[(uint64_t)k * n + s];
-            if (o->velocity_gradients) o->velocity_gradients[9 * i + k] = C[(uint64_t)k * n + s];
-        }
-        if (o->elastic_energies) o->elastic_energies[i] = en[s];
-        if (o->collider_bits) {
-            // without colliders every substep's Collide clears a live
-            // particle's bits (collide.rs:53-56)
-            if (!cbits.empty()) o->collider_bits[i] = cbits[s];
-            else o->collider_bits[i] = (h->substeps_total > 0 && !(packed & SV_TOMBSTONED)) ? 0u : h->collider_bits[i];
-        }
-    }
+    if (!unpack_particles(hp, unpack_info(h, false), o)) return fail("sv_download: corrupt original index");
     return 0;
 }
 
@@ -980,39 +943,15 @@ int sv_download_grid(sv_handle *h, int32_t *node_ids, float *masses, float *velo
     g_last_error.clear();
     if (!h) return fail("sv_download_grid: NULL handle");
     if (read_counters(h)) return -1;
-    uint64_t slots = h->vel_side < 0 ? 0 : std::min<uint64_t>(h->host_counters[C_NSLOT0 + h->vel_map], h->capacity);
+    uint64_t slots = 0, var_cap = 0;
+    grid_sizes(h, slots, var_cap);
     std::vector<uint32_t> active(slots);
     std::vector<float4> g(slots * 64);
-    if (slots) {
-        SV_CUDA(cudaMemcpy(active.data(), h->active[h->vel_map], slots * 4, cudaMemcpyDeviceToHost));
-        SV_CUDA(cudaMemcpy(g.data(), h->grid[h->vel_side], slots * 64 * sizeof(float4), cudaMemcpyDeviceToHost));
-    }
-    struct Node {
-        int32_t id[3];
-        float4 v;
-    };
-    std::vector<Node> nodes;
-    const GridLayout &L = h->layout;
-    for (uint64_t s = 0; s < slots; ++s) {
-        uint32_t b = active[s];
-        int bz = (int)(b % (uint32_t)L.nb[2]), r = (int)(b / (uint32_t)L.nb[2]);
-        int by = r % L.nb[1], bx = r / L.nb[1];
-        for (int l = 0; l < 64; ++l) {
-            float4 v = g[s * 64 + l];
-            if (!(v.w > 0.f)) continue;
-            Node nd;
-            nd.id[0] = L.origin[0] + 4 * bx + (l >> 4);
-            nd.id[1] = L.origin[1] + 4 * by + ((l >> 2) & 3);
-            nd.id[2] = L.origin[2] + 4 * bz + (l & 3);
-            nd.v = v;
-            nodes.push_back(nd);
-        }
-    }
-    std::sort(nodes.begin(), nodes.end(), [](const Node &x, const Node &y) {
-        if (x.id[0] != y.id[0]) return x.id[0] < y.id[0];
-        if (x.id[1] != y.id[1]) return x.id[1] < y.id[1];
-        return x.id[2] < y.id[2];
-    });
+    HostGrid hg;
+    hg.slots = slots, hg.active = active.data(), hg.grid = g.data();  // the bits-0 nodes only
+    SV_CUDA(copy_grid_async(h, hg));
+    SV_CUDA(cudaStreamSynchronize(h->stream));
+    const std::vector<GridNode> nodes = grid_nodes(hg, h->layout);
     if (count) *count = nodes.size();
     for (uint64_t i = 0; i < nodes.size() && i < capacity; ++i) {
         if (node_ids) std::memcpy(&node_ids[3 * i], nodes[i].id, 12);

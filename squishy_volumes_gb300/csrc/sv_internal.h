@@ -282,6 +282,61 @@ cudaError_t launch_interpolate(sv_handle *h, double time);
 cudaError_t launch_g2p_advance(sv_handle *h, float dt);
 cudaError_t launch_clear_variants(sv_handle *h, int which);
 
+// Reads the device counters into h->host_counters (waits for the stream);
+// -1 with the last error set on failure.
+int refresh_counters(sv_handle *h);
+
+// ---- host copies of the device state (sv_cache.cu) ----
+// One particle side copied to the host in device (binning) order.
+struct HostParticles {
+    uint64_t n = 0;
+    float4 *pos = nullptr, *vel = nullptr;
+    int4 *cell = nullptr;                                  // cell form only
+    float *C = nullptr, *F = nullptr, *energy = nullptr;   // C and F as [9][n] element planes
+    uint32_t *orig = nullptr, *cbits = nullptr;            // cbits: with a frame input only
+};
+// What turning such a copy back into the reference's layout needs from the
+// handle (copied, so a queued copy outlives changes to the handle).
+struct UnpackInfo {
+    bool cell = false;
+    double dx = 0.0;
+    std::vector<SceneInfo> scenes;
+    std::vector<Material> materials;
+    bool stepped = false;                      // a substep ran: Collide cleared the live particles' bits
+    const uint32_t *initial_bits = nullptr;    // collider bits the particles were created with
+    std::vector<uint32_t> initial_bits_copy;   // owned copy (own_bits)
+};
+// Queues the copies of the current particle side into `dst` (n elements
+// each; cell and cbits only where the handle has them) on h->stream.
+cudaError_t copy_particles_async(sv_handle *h, const HostParticles &dst);
+// own_bits: copy the handle's initial collider bits instead of pointing at them
+UnpackInfo unpack_info(const sv_handle *h, bool own_bits);
+// Original particle order (the reference's reverse_sort_map restore,
+// cpu_state.rs:71-104); false on a corrupt original index.
+bool unpack_particles(const HostParticles &src, const UnpackInfo &u, sv_particles *out);
+
+// Grid nodes with mass > 0, keyed (node, collider bits).
+struct GridNode {
+    int32_t id[3];
+    uint32_t bits;
+    float4 v;  // vx, vy, vz, m
+};
+// The grid gathered by the last substep (and its collider variants).
+struct HostGrid {
+    uint64_t slots = 0;
+    uint32_t *active = nullptr;  // [slots]
+    float4 *grid = nullptr;      // [slots * 64]
+    uint64_t var_cap = 0;        // 0: no variants
+    unsigned long long *var_key = nullptr;
+    uint32_t *var_bits = nullptr;
+    float4 *var_vel = nullptr;
+};
+// sizes of that grid from the last counter read-back (the stream idle)
+void grid_sizes(const sv_handle *h, uint64_t &slots, uint64_t &var_cap);
+cudaError_t copy_grid_async(sv_handle *h, const HostGrid &dst);
+// sorted like the reference's GridKey (node id, then collider bits)
+std::vector<GridNode> grid_nodes(const HostGrid &g, const GridLayout &L);
+
 // Per-kernel timing hooks.
 void timer_begin(sv_handle *h, const char *name, cudaEvent_t *start);
 void timer_end(sv_handle *h, const char *name, cudaEvent_t start);
