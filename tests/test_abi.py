@@ -74,6 +74,24 @@ def test_frame_input_layout_matches_c_and_the_oracle(tmp_path):
     assert vals[-1] == ct.sizeof(SvFrameInput) == ct.sizeof(OFrameInput)
 
 
+def test_frame_layout_matches_c(tmp_path):
+    from squishy_volumes_gb300._abi import SvFrame
+
+    fields = [f[0] for f in SvFrame._fields_]
+    c_names = ["lambda" if f == "lambda_" else f for f in fields]
+    src = tmp_path / "sv_frame.c"
+    lines = "".join(f'  printf("%zu ", offsetof(sv_frame, {f}));\n' for f in c_names)
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "squishy_volumes_cuda.h"\n'
+                   "int main(void) {\n" + lines + '  printf("%zu\\n", sizeof(sv_frame));\n  return 0;\n}\n')
+    exe = tmp_path / "sv_frame"
+    r = subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("gcc unavailable: " + r.stderr)
+    vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    assert vals[:-1] == [getattr(SvFrame, f).offset for f in fields]
+    assert vals[-1] == ct.sizeof(SvFrame)
+
+
 def test_oracle_is_not_linked_by_the_product():
     """The product library must not depend on the CPU oracle."""
     from squishy_volumes_gb300 import build
