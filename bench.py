@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bound on the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--bake", type=int, default=0,
+                    help="also time this many whole frames with a frame-cache store after each, against the same "
+                         "frames without stores")
     ap.add_argument("--error-substeps", type=int, default=0,
                     help="also run this many substeps from the initial state on the GPU and on the fp64 CPU oracle "
                          "and report the relative errors of x, v, C, F")
@@ -185,6 +188,61 @@ def error_vs_fp64(scene, substeps: int):
             else np.linalg.norm(b)
         res[k] = {"rel_l2": float(np.linalg.norm(a - b) / max(scale, 1e-300)), "max_abs": float(d.max()) if d.size else 0.0}
     res["flags_equal"] = bool(np.array_equal(out.flags, exp.flags))
+    return res
+
+
+def bake_frames(scene, make_gpu, frames: int):
+    """Whole frames of the workload, the reference's compute-thread loop
+    (compute_thread.rs:136-169): step to the frame's end, then hand the state
+    (with the grid) to the frame cache, whose writer thread restores the
+    particle order and writes the file while the next frame computes.  The
+    same frames without stores give the compute-only rate."""
+    import shutil
+    import tempfile
+
+    from squishy_volumes_gb300 import CudaState
+    from squishy_volumes_gb300.frames import FrameCache
+
+    fps = scene.consts.frames_per_second
+    frame_substeps = int(math.ceil((1.0 / fps) / scene.dt))
+    res = {"frames": frames, "substeps_per_frame": frame_substeps, "store_grid": True}
+    for store in (False, True):
+        st_ = make_gpu()
+        if not isinstance(st_, CudaState):
+            st_.close()
+            return None
+        st_.step(frame_substeps, scene.dt, scene.gravity)  # warm-up frame: graphs captured
+        directory = tempfile.mkdtemp(prefix="sv_bake_")
+        cache = None
+        if store:
+            # two warm-up stores give both in-flight slots their pinned buffers
+            cache = FrameCache(directory, scene.io_state.particles)
+            cache.store(st_, store_grid=True)
+            cache.store(st_, store_grid=True)
+            cache.flush()
+        calls = []
+        t0 = time.perf_counter()
+        for _ in range(frames):
+            st_.step(frame_substeps, scene.dt, scene.gravity)
+            if cache is not None:
+                c0 = time.perf_counter()
+                cache.store(st_, store_grid=True)
+                calls.append(time.perf_counter() - c0)
+        t_compute = time.perf_counter()
+        if cache is not None:
+            cache.flush()
+        t1 = time.perf_counter()
+        if cache is None:
+            res["frames_per_s_without_store"] = frames / (t1 - t0)
+        else:
+            written, nbytes = cache.info()
+            cache.close()
+            res["frames_per_s"] = frames / (t1 - t0)
+            res["frames_per_s_until_last_store_queued"] = frames / (t_compute - t0)
+            res["store_call_ms_median"] = float(np.median(calls) * 1e3)
+            res["bytes_per_frame"] = nbytes // max(written, 1)
+        st_.close()
+        shutil.rmtree(directory, ignore_errors=True)
     return res
 
 
@@ -399,6 +457,10 @@ def run_ours(args, rank, world, local):
             "step": "sv_create (upload) + one frame of substeps + sv_download",
         }
 
+    bake = None
+    if args.bake > 0 and rank == 0:
+        bake = bake_frames(scene, make_gpu, args.bake)
+
     error = None
     if args.error_substeps > 0 and rank == 0:
         error = error_vs_fp64(scene, args.error_substeps)
@@ -443,6 +505,7 @@ def run_ours(args, rank, world, local):
         "fp64_svd_particles": st["fp64_svd"],
         "error_vs_fp64": error,
         "closure": closure_info,
+        "bake": bake,
     }
     if rank == 0:
         print(json.dumps(line))

@@ -425,13 +425,16 @@ int sv_frame_read(const char *path, const char *version, sv_frame *frame);
  * initial_positions, in the original particle order (NULL arrays are
  * written as 0; the stored flags select the variants as above).
  *
- * sv_cache_store queues the copy of the handle's current state (and, when
- * store_grid, of the grid its last substep gathered, with the collider
- * variants) on the handle's stream and returns without waiting; the writer
- * thread waits for the copy, restores the original particle order and
- * writes the file.  The handle's next kernels wait for the copy (not for the
- * file).  At most `depth` frames are in flight; a further store waits for
- * the oldest.  sv_cache_store_frame queues a copy of a host frame.
+ * sv_cache_store queues a device snapshot of the handle's current state
+ * (and, when store_grid, of the grid its last substep gathered, with the
+ * collider variants) on the handle's stream, and its copy to pinned host
+ * memory on the cache's own stream, and returns without waiting.  The
+ * handle's next kernels wait only for the device snapshot; the host copy
+ * overlaps them.  The writer thread waits for the host copy, restores the
+ * original particle order and writes the file.  At most `depth` frames are
+ * in flight (each holds a device and a pinned copy of the state); a further
+ * store waits for the oldest.  sv_cache_store_frame queues a copy of a host
+ * frame.
  * sv_cache_check returns -1 with the message once the writer has failed
  * (StoreThread::check); sv_cache_flush waits until every queued frame is
  * on disk; sv_cache_info reports frames written and their bytes

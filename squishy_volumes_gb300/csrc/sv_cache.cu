@@ -37,21 +37,69 @@ static_assert(__BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__, "frame files are little
 namespace sv {
 
 // ------------------------------------------------------------------ state copies
-cudaError_t copy_particles_async(sv_handle *h, const HostParticles &d) {
-    const uint64_t n = h->n;
+namespace {
+
+// The current particle side as device pointers in HostParticles' shape.
+HostParticles device_view(const sv_handle *h) {
     const ParticleArrays &a = h->side[h->cur];
+    HostParticles v;
+    v.n = h->n;
+    v.pos = a.pos, v.vel = a.vel, v.cell = h->layout.position_form == 1 ? a.cell : nullptr;
+    v.C = a.C, v.F = a.F, v.energy = a.energy, v.orig = a.orig, v.cbits = a.cbits_done;
+    return v;
+}
+
+// The grid the last substep gathered (and its variant table) likewise.
+HostGrid device_grid_view(const sv_handle *h, uint64_t slots, uint64_t var_cap) {
+    HostGrid v;
+    v.slots = slots, v.var_cap = var_cap;
+    if (slots) v.active = h->active[h->vel_map], v.grid = h->grid[h->vel_side];
+    if (var_cap) {
+        // the variant table the last substep gathered from (melded velocities)
+        const int s = h->vel_side;
+        v.var_key = h->var_key[s], v.var_bits = h->var_bits[s], v.var_vel = h->var_vel[s];
+    }
+    return v;
+}
+
+}  // namespace
+
+// Copies between any two such views (device or host memory) on `s`; the
+// arrays dst lacks (cell, cbits) are skipped.
+cudaError_t copy_particles(const HostParticles &d, const HostParticles &a, cudaStream_t s) {
+    const uint64_t n = a.n;
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(d.pos, a.pos, n * 16, cudaMemcpyDeviceToHost, h->stream)) ||
-        (e = cudaMemcpyAsync(d.vel, a.vel, n * 16, cudaMemcpyDeviceToHost, h->stream)) ||
-        (e = cudaMemcpyAsync(d.C, a.C, 9 * n * 4, cudaMemcpyDeviceToHost, h->stream)) ||
-        (e = cudaMemcpyAsync(d.F, a.F, 9 * n * 4, cudaMemcpyDeviceToHost, h->stream)) ||
-        (e = cudaMemcpyAsync(d.energy, a.energy, n * 4, cudaMemcpyDeviceToHost, h->stream)) ||
-        (e = cudaMemcpyAsync(d.orig, a.orig, n * 4, cudaMemcpyDeviceToHost, h->stream)))
+    if ((e = cudaMemcpyAsync(d.pos, a.pos, n * 16, cudaMemcpyDefault, s)) ||
+        (e = cudaMemcpyAsync(d.vel, a.vel, n * 16, cudaMemcpyDefault, s)) ||
+        (e = cudaMemcpyAsync(d.C, a.C, 9 * n * 4, cudaMemcpyDefault, s)) ||
+        (e = cudaMemcpyAsync(d.F, a.F, 9 * n * 4, cudaMemcpyDefault, s)) ||
+        (e = cudaMemcpyAsync(d.energy, a.energy, n * 4, cudaMemcpyDefault, s)) ||
+        (e = cudaMemcpyAsync(d.orig, a.orig, n * 4, cudaMemcpyDefault, s)))
         return e;
-    if (d.cell && (e = cudaMemcpyAsync(d.cell, a.cell, n * 16, cudaMemcpyDeviceToHost, h->stream))) return e;
-    if (d.cbits && a.cbits_done && (e = cudaMemcpyAsync(d.cbits, a.cbits_done, n * 4, cudaMemcpyDeviceToHost, h->stream)))
-        return e;
+    if (d.cell && a.cell && (e = cudaMemcpyAsync(d.cell, a.cell, n * 16, cudaMemcpyDefault, s))) return e;
+    if (d.cbits && a.cbits && (e = cudaMemcpyAsync(d.cbits, a.cbits, n * 4, cudaMemcpyDefault, s))) return e;
     return cudaSuccess;
+}
+
+cudaError_t copy_grid(const HostGrid &d, const HostGrid &a, cudaStream_t s) {
+    cudaError_t e;
+    if (a.slots) {
+        if ((e = cudaMemcpyAsync(d.active, a.active, a.slots * 4, cudaMemcpyDefault, s)) ||
+            (e = cudaMemcpyAsync(d.grid, a.grid, a.slots * 64 * sizeof(float4), cudaMemcpyDefault, s)))
+            return e;
+    }
+    if (a.var_cap) {
+        const uint64_t c = a.var_cap;
+        if ((e = cudaMemcpyAsync(d.var_key, a.var_key, c * sizeof(unsigned long long), cudaMemcpyDefault, s)) ||
+            (e = cudaMemcpyAsync(d.var_bits, a.var_bits, c * col::VK * 4, cudaMemcpyDefault, s)) ||
+            (e = cudaMemcpyAsync(d.var_vel, a.var_vel, c * col::VK * sizeof(float4), cudaMemcpyDefault, s)))
+            return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t copy_particles_async(sv_handle *h, const HostParticles &d) {
+    return copy_particles(d, device_view(h), h->stream);
 }
 
 UnpackInfo unpack_info(const sv_handle *h, bool own_bits) {
@@ -112,25 +160,7 @@ void grid_sizes(const sv_handle *h, uint64_t &slots, uint64_t &var_cap) {
 }
 
 cudaError_t copy_grid_async(sv_handle *h, const HostGrid &d) {
-    cudaError_t e;
-    if (d.slots) {
-        if ((e = cudaMemcpyAsync(d.active, h->active[h->vel_map], d.slots * 4, cudaMemcpyDeviceToHost, h->stream)) ||
-            (e = cudaMemcpyAsync(d.grid, h->grid[h->vel_side], d.slots * 64 * sizeof(float4), cudaMemcpyDeviceToHost,
-                                 h->stream)))
-            return e;
-    }
-    if (d.var_cap) {
-        // the variant table the last substep gathered from (melded velocities)
-        const int s = h->vel_side;
-        const uint64_t c = d.var_cap;
-        if ((e = cudaMemcpyAsync(d.var_key, h->var_key[s], c * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                                 h->stream)) ||
-            (e = cudaMemcpyAsync(d.var_bits, h->var_bits[s], c * col::VK * 4, cudaMemcpyDeviceToHost, h->stream)) ||
-            (e = cudaMemcpyAsync(d.var_vel, h->var_vel[s], c * col::VK * sizeof(float4), cudaMemcpyDeviceToHost,
-                                 h->stream)))
-            return e;
-    }
-    return cudaSuccess;
+    return copy_grid(d, device_grid_view(h, d.slots, d.var_cap), h->stream);
 }
 
 std::vector<GridNode> grid_nodes(const HostGrid &g, const GridLayout &L) {
@@ -495,59 +525,99 @@ sv_frame view_of(FrameData &d) {
     return f;
 }
 
-// Pinned host buffers of one frame in flight from a handle.
-struct Slot {
-    cudaEvent_t copied = nullptr;
+// One set of state buffers of a frame in flight: pinned host or device memory.
+struct Buffers {
+    bool device = false;
     uint64_t n_cap = 0, slots_cap = 0, var_cap_cap = 0;
     bool has_cell = false, has_cbits = false;
-    HostParticles hp;
-    HostGrid hg;
+    HostParticles p;
+    HostGrid g;
+
+    template <class T> cudaError_t alloc(T **ptr, uint64_t count) {
+        const size_t bytes = std::max<size_t>((size_t)count * sizeof(T), 16);
+        return device ? cudaMalloc((void **)ptr, bytes) : cudaHostAlloc((void **)ptr, bytes, cudaHostAllocDefault);
+    }
+    void drop(void *ptr) {
+        if (!ptr) return;
+        if (device) cudaFree(ptr);
+        else cudaFreeHost(ptr);
+    }
+    void free_particles() {
+        for (void *q : {(void *)p.pos, (void *)p.vel, (void *)p.cell, (void *)p.C, (void *)p.F, (void *)p.energy,
+                        (void *)p.orig, (void *)p.cbits})
+            drop(q);
+        p = HostParticles{};
+        n_cap = 0, has_cell = has_cbits = false;
+    }
     void release() {
-        for (void *p : {(void *)hp.pos, (void *)hp.vel, (void *)hp.cell, (void *)hp.C, (void *)hp.F, (void *)hp.energy,
-                        (void *)hp.orig, (void *)hp.cbits, (void *)hg.active, (void *)hg.grid, (void *)hg.var_key,
-                        (void *)hg.var_bits, (void *)hg.var_vel})
-            if (p) cudaFreeHost(p);
-        hp = HostParticles{}, hg = HostGrid{};
-        n_cap = slots_cap = var_cap_cap = 0;
-        has_cell = has_cbits = false;
+        free_particles();
+        for (void *q : {(void *)g.active, (void *)g.grid, (void *)g.var_key, (void *)g.var_bits, (void *)g.var_vel}) drop(q);
+        g = HostGrid{};
+        slots_cap = var_cap_cap = 0;
+    }
+    cudaError_t ensure(uint64_t n, bool cell, bool cbits, uint64_t slots, uint64_t var_cap) {
+        cudaError_t e = cudaSuccess;
+        if (n > n_cap || (cell && !has_cell) || (cbits && !has_cbits)) {
+            const uint64_t c = std::max(n, n_cap);
+            const bool want_cell = cell || has_cell, want_cbits = cbits || has_cbits;
+            free_particles();
+            if ((e = alloc(&p.pos, c)) || (e = alloc(&p.vel, c)) || (e = alloc(&p.C, 9 * c)) || (e = alloc(&p.F, 9 * c)) ||
+                (e = alloc(&p.energy, c)) || (e = alloc(&p.orig, c)) || (want_cell && (e = alloc(&p.cell, c))) ||
+                (want_cbits && (e = alloc(&p.cbits, c))))
+                return e;
+            n_cap = c, has_cell = want_cell, has_cbits = want_cbits;
+        }
+        if (slots > slots_cap) {
+            drop(g.active), drop(g.grid);
+            g.active = nullptr, g.grid = nullptr;
+            if ((e = alloc(&g.active, slots)) || (e = alloc(&g.grid, slots * 64))) return e;
+            slots_cap = slots;
+        }
+        if (var_cap > var_cap_cap) {
+            drop(g.var_key), drop(g.var_bits), drop(g.var_vel);
+            g.var_key = nullptr, g.var_bits = nullptr, g.var_vel = nullptr;
+            if ((e = alloc(&g.var_key, var_cap)) || (e = alloc(&g.var_bits, var_cap * col::VK)) ||
+                (e = alloc(&g.var_vel, var_cap * col::VK)))
+                return e;
+            var_cap_cap = var_cap;
+        }
+        return cudaSuccess;
+    }
+    // views sized for one frame (cell and cbits only where the state has them)
+    HostParticles particles(uint64_t n, bool cell, bool cbits) const {
+        HostParticles v = p;
+        v.n = n;
+        if (!cell) v.cell = nullptr;
+        if (!cbits) v.cbits = nullptr;
+        return v;
+    }
+    HostGrid grid(uint64_t slots, uint64_t var_cap) const {
+        HostGrid v = g;
+        v.slots = slots, v.var_cap = var_cap;
+        return v;
     }
 };
 
-template <class T> cudaError_t pin(T **p, uint64_t count) {
-    return cudaHostAlloc((void **)p, std::max<size_t>((size_t)count * sizeof(T), 16), cudaHostAllocDefault);
-}
-
-cudaError_t ensure(Slot &s, uint64_t n, bool cell, bool cbits, uint64_t slots, uint64_t var_cap) {
-    cudaError_t e = cudaSuccess;
-    if (!s.copied && (e = cudaEventCreateWithFlags(&s.copied, cudaEventDisableTiming | cudaEventBlockingSync))) return e;
-    if (n > s.n_cap || (cell && !s.has_cell) || (cbits && !s.has_cbits)) {
-        for (void *p : {(void *)s.hp.pos, (void *)s.hp.vel, (void *)s.hp.cell, (void *)s.hp.C, (void *)s.hp.F,
-                        (void *)s.hp.energy, (void *)s.hp.orig, (void *)s.hp.cbits})
-            if (p) cudaFreeHost(p);
-        s.hp = HostParticles{};
-        const uint64_t c = std::max(n, s.n_cap);
-        if ((e = pin(&s.hp.pos, c)) || (e = pin(&s.hp.vel, c)) || (e = pin(&s.hp.C, 9 * c)) || (e = pin(&s.hp.F, 9 * c)) ||
-            (e = pin(&s.hp.energy, c)) || (e = pin(&s.hp.orig, c)) || (cell && (e = pin(&s.hp.cell, c))) ||
-            (cbits && (e = pin(&s.hp.cbits, c))))
-            return e;
-        s.n_cap = c, s.has_cell = cell, s.has_cbits = cbits;
+// A frame in flight from a handle: a device snapshot taken on the handle's
+// stream (`snap`), and its copy to pinned memory on the cache's own stream
+// (`copied`), which overlaps the handle's next substeps.
+struct Slot {
+    cudaEvent_t snap = nullptr, copied = nullptr;
+    Buffers dev{true}, host{false};
+    cudaError_t ensure(uint64_t n, bool cell, bool cbits, uint64_t slots, uint64_t var_cap) {
+        cudaError_t e;
+        if (!snap && (e = cudaEventCreateWithFlags(&snap, cudaEventDisableTiming))) return e;
+        if (!copied && (e = cudaEventCreateWithFlags(&copied, cudaEventDisableTiming | cudaEventBlockingSync))) return e;
+        if ((e = dev.ensure(n, cell, cbits, slots, var_cap))) return e;
+        return host.ensure(n, cell, cbits, slots, var_cap);
     }
-    if (slots > s.slots_cap) {
-        if (s.hg.active) cudaFreeHost(s.hg.active), cudaFreeHost(s.hg.grid);
-        s.hg.active = nullptr, s.hg.grid = nullptr;
-        if ((e = pin(&s.hg.active, slots)) || (e = pin(&s.hg.grid, slots * 64))) return e;
-        s.slots_cap = slots;
+    void release() {
+        if (snap) cudaEventDestroy(snap);
+        if (copied) cudaEventDestroy(copied);
+        snap = copied = nullptr;
+        dev.release(), host.release();
     }
-    if (var_cap > s.var_cap_cap) {
-        if (s.hg.var_key) cudaFreeHost(s.hg.var_key), cudaFreeHost(s.hg.var_bits), cudaFreeHost(s.hg.var_vel);
-        s.hg.var_key = nullptr, s.hg.var_bits = nullptr, s.hg.var_vel = nullptr;
-        if ((e = pin(&s.hg.var_key, var_cap)) || (e = pin(&s.hg.var_bits, var_cap * col::VK)) ||
-            (e = pin(&s.hg.var_vel, var_cap * col::VK)))
-            return e;
-        s.var_cap_cap = var_cap;
-    }
-    return cudaSuccess;
-}
+};
 
 struct Job {
     uint32_t frame = 0;
@@ -581,6 +651,8 @@ struct sv_cache {
     std::string error;  // first failure of the writer
     std::atomic<uint64_t> frames{0}, bytes{0};
     std::thread worker;
+    cudaStream_t copy_stream = nullptr;  // device snapshot -> pinned memory
+    int stream_device = -1;
 
     // One frame: a handle's copies (unpacked here) or a host frame.
     std::string write(Job &j) {
@@ -752,19 +824,32 @@ int sv_cache_store(sv_cache *c, sv_handle *h, int store_grid) {
     }
     Slot &s = c->slots[k];
     const bool cell = h->layout.position_form == 1, cbits = h->side[h->cur].cbits_done != nullptr;
-    cudaError_t e = ensure(s, h->n, cell, cbits, slots, var_cap);
     Job j;
+    cudaGetDevice(&j.device);
+    cudaError_t e = cudaSuccess;
+    if (!c->copy_stream) {
+        e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking);
+        c->stream_device = j.device;
+    }
+    if (e == cudaSuccess && j.device != c->stream_device) e = cudaErrorInvalidDevice;  // one device per cache
+    if (e == cudaSuccess) e = s.ensure(h->n, cell, cbits, slots, var_cap);
     if (e == cudaSuccess) {
         j.slot = k, j.n = h->n, j.time = h->time, j.store_grid = store_grid != 0;
         j.unpack = unpack_info(h, true);
         j.layout = h->layout;
-        j.hp = s.hp, j.hp.n = h->n;
-        if (!cell) j.hp.cell = nullptr;
-        if (!cbits) j.hp.cbits = nullptr;
-        j.hg = s.hg, j.hg.slots = slots, j.hg.var_cap = var_cap;
-        cudaGetDevice(&j.device);
-        if ((e = copy_particles_async(h, j.hp)) == cudaSuccess && (!store_grid || (e = copy_grid_async(h, j.hg)) == cudaSuccess))
-            e = cudaEventRecord(s.copied, h->stream);
+        j.hp = s.host.particles(h->n, cell, cbits);
+        j.hg = s.host.grid(slots, var_cap);
+        const HostParticles dp = s.dev.particles(h->n, cell, cbits);
+        const HostGrid dg = s.dev.grid(slots, var_cap);
+        // device snapshot on the handle's stream, so its next substeps only
+        // wait for a copy at HBM speed; the host copy runs on the cache's stream
+        if ((e = copy_particles(dp, device_view(h), h->stream)) == cudaSuccess &&
+            (!store_grid || (e = copy_grid(dg, device_grid_view(h, slots, var_cap), h->stream)) == cudaSuccess) &&
+            (e = cudaEventRecord(s.snap, h->stream)) == cudaSuccess &&
+            (e = cudaStreamWaitEvent(c->copy_stream, s.snap, 0)) == cudaSuccess &&
+            (e = copy_particles(j.hp, dp, c->copy_stream)) == cudaSuccess &&
+            (!store_grid || (e = copy_grid(j.hg, dg, c->copy_stream)) == cudaSuccess))
+            e = cudaEventRecord(s.copied, c->copy_stream);
     }
     if (e != cudaSuccess) {
         std::lock_guard<std::mutex> lk(c->m);
@@ -824,10 +909,8 @@ int sv_cache_close(sv_cache *c) {
     c->cv.notify_all();
     if (c->worker.joinable()) c->worker.join();
     const int rc = writer_error(c);
-    for (Slot &s : c->slots) {
-        if (s.copied) cudaEventDestroy(s.copied);
-        s.release();
-    }
+    for (Slot &s : c->slots) s.release();
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     delete c;
     return rc;
 }
