@@ -84,7 +84,12 @@ typedef struct sv_consts {
      * memory access"), k = every k substeps.  Results do not depend on it
      * beyond fp32 summation order. */
     uint32_t sort_interval;
-    uint32_t reserved[5];
+    /* How sv_create and sv_download move the particle arrays: 0 = kernels
+     * that read and write the caller's host arrays directly where the
+     * device can access pageable memory (a Grace host over NVLink-C2C), else
+     * staged copies; 1 = staged copies always.  Same results either way. */
+    uint32_t host_transfer;
+    uint32_t reserved[4];
 } sv_consts;
 
 typedef struct sv_particles {
@@ -294,6 +299,9 @@ int sv_get_time(sv_handle *h, double *time);
 /* Whether sv_step runs whole binning periods as CUDA graphs (default on;
  * off, and while profiling, every kernel is launched directly). */
 int sv_set_graphs(sv_handle *h, int enable);
+/* sv_consts::host_transfer for the handle's later downloads; *direct (if
+ * not NULL) tells whether the direct path is now in use. */
+int sv_set_host_transfer(sv_handle *h, uint32_t mode, uint32_t *direct);
 int sv_get_stats(sv_handle *h, sv_stats *out);
 
 /* Addition: picks the substeps between binning sorts and the CTAs per SM of

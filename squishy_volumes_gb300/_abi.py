@@ -46,7 +46,8 @@ class SvConsts(ct.Structure):
         ("svd_fp64_policy", ct.c_uint32),
         ("block_capacity", ct.c_uint64),
         ("sort_interval", ct.c_uint32),
-        ("reserved", ct.c_uint32 * 5),
+        ("host_transfer", ct.c_uint32),
+        ("reserved", ct.c_uint32 * 4),
     ]
 
 
@@ -184,6 +185,7 @@ _SIGNATURES = {
     "sv_get_stats": (ct.c_int, [ct.c_void_p, ct.POINTER(SvStats)]),
     "sv_set_stream": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "sv_set_graphs": (ct.c_int, [ct.c_void_p, ct.c_int]),
+    "sv_set_host_transfer": (ct.c_int, [ct.c_void_p, ct.c_uint32, u32p]),
     "sv_step_adaptive": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_double), ct.c_double, ct.c_float, f32p,
                                     ct.POINTER(ct.c_int32), u32p, u32p]),
     "sv_time_step_limits": (ct.c_int, [ct.c_void_p, f32p]),

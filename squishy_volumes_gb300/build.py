@@ -19,7 +19,8 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB_NAME = "libsquishy_volumes_cuda.so"
-SOURCES = ["sv_api.cu", "sv_substep.cu", "sv_sort.cu", "sv_mlp.cu", "sv_closure.cu", "sv_frame.cu", "sv_cache.cu"]
+SOURCES = ["sv_api.cu", "sv_substep.cu", "sv_sort.cu", "sv_mlp.cu", "sv_closure.cu", "sv_frame.cu", "sv_cache.cu",
+           "sv_transfer.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3",

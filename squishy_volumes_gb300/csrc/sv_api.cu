@@ -3,6 +3,7 @@
 // CpuState::produce_next_state (rust/crates/cpu/src/cpu_state.rs:146-197).
 #include <algorithm>
 #include <array>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -52,7 +53,7 @@ void free_handle(sv_handle *h) {
     cudaFree(h->materials), cudaFree(h->keys), cudaFree(h->sorted_keys), cudaFree(h->perm), cudaFree(h->sort_temp);
     cudaFree(h->seg_start), cudaFree(h->seg_block), cudaFree(h->tile_counts), cudaFree(h->scan_temp);
     for (int s = 0; s < 2; ++s) cudaFree(h->blockmap[s]), cudaFree(h->active[s]), cudaFree(h->grid[s]);
-    cudaFree(h->counters), cudaFree(h->scenes);
+    cudaFree(h->counters), cudaFree(h->scenes), cudaFree(h->inv);
     if (h->host_counters) cudaFreeHost(h->host_counters);
     for (auto &p : h->timer.pending) cudaEventDestroy(p.second.first), cudaEventDestroy(p.second.second);
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -77,6 +78,129 @@ struct MaterialHash {
         return (size_t)h;
     }
 };
+
+int build_material(const sv_particles *p, uint64_t i, Material &m, std::string &err);
+
+// The host pass of sv_create over host threads: per particle its material
+// (deduplicated ParticleParameters, numbered in order of first appearance
+// like a sequential pass) and the bounds of the live particles of each
+// scene.  Errors are those a sequential pass meets first: the lowest
+// particle with an invalid parameter set, else a non-finite position.
+struct Prepass {
+    std::vector<Material> mats;
+    std::vector<uint32_t> mat_index;
+    std::vector<std::array<double, 3>> lo, hi;  // per scene, of live particles
+    std::string err;
+};
+
+void prepass(const sv_particles *ps, uint32_t n_scenes, const std::vector<uint64_t> &first, Prepass &out) {
+    const uint64_t n = first[n_scenes];
+    out.mat_index.assign(n, 0);
+    const uint64_t per = 1u << 16;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned T = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(std::min(hw, 64u), (n + per - 1) / per));
+    struct Part {
+        std::vector<Material> mats;
+        std::vector<uint32_t> remap;
+        std::vector<std::array<double, 3>> lo, hi;
+        uint64_t err_at = UINT64_MAX;
+        std::string err;
+        bool nonfinite = false;
+    };
+    std::vector<Part> parts(T);
+    auto range = [&](unsigned t, uint64_t &g0, uint64_t &g1) { g0 = n * t / T, g1 = n * (t + 1) / T; };
+    auto pass1 = [&](unsigned t) {
+        Part &pt = parts[t];
+        pt.lo.assign(n_scenes, {INFINITY, INFINITY, INFINITY});
+        pt.hi.assign(n_scenes, {-INFINITY, -INFINITY, -INFINITY});
+        std::unordered_map<MaterialKey, uint32_t, MaterialHash> index;
+        Material prev{};
+        uint32_t prev_idx = UINT32_MAX;
+        uint64_t g0, g1;
+        range(t, g0, g1);
+        uint32_t s = (uint32_t)(std::upper_bound(first.begin(), first.end(), g0) - first.begin()) - 1;
+        for (uint64_t g = g0; g < g1; ++g) {
+            while (g >= first[s + 1]) ++s;
+            const sv_particles *p = &ps[s];
+            const uint64_t i = g - first[s];
+            Material m;
+            std::string err;
+            if (build_material(p, i, m, err)) {
+                pt.err_at = g, pt.err = err;
+                return;
+            }
+            m.scene = s;
+            if (!(p->flags[i] & SV_TOMBSTONED)) {
+                for (int a = 0; a < 3; ++a) {
+                    const double x = p->positions[3 * i + a];
+                    if (!std::isfinite(x)) pt.nonfinite = true;
+                    pt.lo[s][a] = std::min(pt.lo[s][a], x), pt.hi[s][a] = std::max(pt.hi[s][a], x);
+                }
+            }
+            if (prev_idx != UINT32_MAX && std::memcmp(&m, &prev, sizeof(m)) == 0) {
+                out.mat_index[g] = prev_idx;
+                continue;
+            }
+            auto it = index.find(MaterialKey{m});
+            uint32_t idx;
+            if (it == index.end()) {
+                idx = (uint32_t)pt.mats.size();
+                index.emplace(MaterialKey{m}, idx);
+                pt.mats.push_back(m);
+            } else {
+                idx = it->second;
+            }
+            out.mat_index[g] = idx;  // local to the part until the merge
+            prev = m, prev_idx = idx;
+        }
+    };
+    auto run = [&](auto &&fn) {
+        std::vector<std::thread> pool;
+        for (unsigned t = 1; t < T; ++t) pool.emplace_back(fn, t);
+        fn(0u);
+        for (auto &th : pool) th.join();
+    };
+    run(pass1);
+    for (const Part &pt : parts)
+        if (pt.err_at != UINT64_MAX) {  // parts in index order: the first one found is the lowest
+            out.err = pt.err;
+            return;
+        }
+    // merge the parts' materials in part order, which keeps first-appearance order
+    std::unordered_map<MaterialKey, uint32_t, MaterialHash> index;
+    for (Part &pt : parts) {
+        pt.remap.resize(pt.mats.size());
+        for (size_t k = 0; k < pt.mats.size(); ++k) {
+            auto it = index.find(MaterialKey{pt.mats[k]});
+            if (it == index.end()) {
+                if (out.mats.size() >= MAX_MATERIALS) {
+                    out.err = "more than 2^24 distinct particle parameter sets";
+                    return;
+                }
+                it = index.emplace(MaterialKey{pt.mats[k]}, (uint32_t)out.mats.size()).first;
+                out.mats.push_back(pt.mats[k]);
+            }
+            pt.remap[k] = it->second;
+        }
+    }
+    run([&](unsigned t) {
+        uint64_t g0, g1;
+        range(t, g0, g1);
+        const std::vector<uint32_t> &r = parts[t].remap;
+        for (uint64_t g = g0; g < g1; ++g) out.mat_index[g] = r[out.mat_index[g]];
+    });
+    if (out.mats.empty()) out.mats.push_back(Material{});
+    out.lo.assign(n_scenes, {INFINITY, INFINITY, INFINITY});
+    out.hi.assign(n_scenes, {-INFINITY, -INFINITY, -INFINITY});
+    bool nonfinite = false;
+    for (const Part &pt : parts) {
+        nonfinite |= pt.nonfinite;
+        for (uint32_t s = 0; s < n_scenes; ++s)
+            for (int a = 0; a < 3; ++a)
+                out.lo[s][a] = std::min(out.lo[s][a], pt.lo[s][a]), out.hi[s][a] = std::max(out.hi[s][a], pt.hi[s][a]);
+    }
+    if (nonfinite) out.err = "non-finite particle position";
+}
 
 int build_material(const sv_particles *p, uint64_t i, Material &m, std::string &err) {
     std::memset(&m, 0, sizeof(m));
@@ -391,41 +515,13 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     n = first[n_scenes];
     if (n >= (1ull << 31)) return fail("sv_create: too many particles (limit 2^31 - 1)");
 
-    // materials (deduplicated ParticleParameters, one set per scene)
-    std::vector<Material> mats;
-    std::vector<uint32_t> mat_index(n);
-    {
-        std::unordered_map<MaterialKey, uint32_t, MaterialHash> index;
-        Material prev{};
-        uint32_t prev_idx = UINT32_MAX;
-        std::string err;
-        for (uint32_t s = 0; s < n_scenes; ++s) {
-            const sv_particles *p = &ps[s];
-            for (uint64_t i = 0; i < p->n; ++i) {
-                Material m;
-                if (build_material(p, i, m, err)) return fail("sv_create: " + err);
-                m.scene = s;
-                const uint64_t gi = first[s] + i;
-                if (prev_idx != UINT32_MAX && std::memcmp(&m, &prev, sizeof(m)) == 0) {
-                    mat_index[gi] = prev_idx;
-                    continue;
-                }
-                auto it = index.find(MaterialKey{m});
-                uint32_t idx;
-                if (it == index.end()) {
-                    idx = (uint32_t)mats.size();
-                    if (idx >= MAX_MATERIALS) return fail("sv_create: more than 2^24 distinct particle parameter sets");
-                    index.emplace(MaterialKey{m}, idx);
-                    mats.push_back(m);
-                } else {
-                    idx = it->second;
-                }
-                mat_index[gi] = idx;
-                prev = m, prev_idx = idx;
-            }
-        }
-        if (mats.empty()) mats.push_back(Material{});
-    }
+    // materials (deduplicated ParticleParameters, one set per scene) and the
+    // bounds of the live particles
+    Prepass pre;
+    prepass(ps, n_scenes, first, pre);
+    if (!pre.err.empty()) return fail("sv_create: " + pre.err);
+    const std::vector<Material> &mats = pre.mats;
+    const std::vector<uint32_t> &mat_index = pre.mat_index;
 
     sv_handle *h = new sv_handle();
     h->n = n;
@@ -453,19 +549,10 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     std::vector<SceneInfo> scenes(n_scenes);
     std::vector<std::array<int64_t, 3>> clo(n_scenes), chi(n_scenes);
     for (uint32_t s = 0; s < n_scenes; ++s) {
-        const sv_particles *p = &ps[s];
         double lo[3], hi[3];
-        for (int a = 0; a < 3; ++a) lo[a] = cs[s].domain_min[a], hi[a] = cs[s].domain_max[a];
-        for (uint64_t i = 0; i < p->n; ++i) {
-            if (p->flags[i] & SV_TOMBSTONED) continue;
-            for (int a = 0; a < 3; ++a) {
-                double x = p->positions[3 * i + a];
-                if (!std::isfinite(x)) {
-                    free_handle(h);
-                    return fail("sv_create: non-finite particle position");
-                }
-                lo[a] = std::min(lo[a], x), hi[a] = std::max(hi[a], x);
-            }
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min<double>(cs[s].domain_min[a], pre.lo[s][a]);
+            hi[a] = std::max<double>(cs[s].domain_max[a], pre.hi[s][a]);
         }
         for (int a = 0; a < 3; ++a) {
             const double cmin = std::floor(lo[a] / L.dx - 0.5), cmax = std::floor(hi[a] / L.dx - 0.5);
@@ -552,8 +639,17 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     if ((e = alloc_grid(h, cap))) return cuda_fail(e, "grid");
     if ((e = cudaMallocHost((void **)&h->host_counters, C_COUNT * sizeof(uint32_t)))) return cuda_fail(e, "pinned");
 
-    // Upload.  Host staging in the device layout, then one copy per array.
-    {
+    if ((e = cudaMemcpy(h->materials, mats.data(), mats.size() * sizeof(Material), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemcpy(h->scenes, scenes.data(), n_scenes * sizeof(SceneInfo), cudaMemcpyHostToDevice)) ||
+        (e = cudaMemset(h->blockmap[0], 0xFF, total * 4)) || (e = cudaMemset(h->blockmap[1], 0xFF, total * 4)) ||
+        (e = cudaMemset(h->counters, 0, C_COUNT * 4)))
+        return cuda_fail(e, "upload");
+    h->direct_host = c.host_transfer == 0 && pageable_access();
+    if (h->direct_host) {
+        // one kernel reads the caller's arrays (sv_transfer.cu)
+        if ((e = upload_direct(h, ps, n_scenes, first.data(), mat_index.data()))) return cuda_fail(e, "upload");
+    } else {
+        // Host staging in the device layout, then one copy per array.
         std::vector<float4> pos(n), vel(n);
         std::vector<int4> cellv(cell ? n : 0);
         std::vector<float> C(9 * n), F(9 * n), en(n);
@@ -597,11 +693,7 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
             (e = cudaMemcpy(a.C, C.data(), 9 * n * 4, cudaMemcpyHostToDevice)) ||
             (e = cudaMemcpy(a.F, F.data(), 9 * n * 4, cudaMemcpyHostToDevice)) ||
             (e = cudaMemcpy(a.energy, en.data(), n * 4, cudaMemcpyHostToDevice)) ||
-            (e = cudaMemcpy(a.orig, orig.data(), n * 4, cudaMemcpyHostToDevice)) ||
-            (e = cudaMemcpy(h->materials, mats.data(), mats.size() * sizeof(Material), cudaMemcpyHostToDevice)) ||
-            (e = cudaMemcpy(h->scenes, scenes.data(), n_scenes * sizeof(SceneInfo), cudaMemcpyHostToDevice)) ||
-            (e = cudaMemset(h->blockmap[0], 0xFF, total * 4)) || (e = cudaMemset(h->blockmap[1], 0xFF, total * 4)) ||
-            (e = cudaMemset(h->counters, 0, C_COUNT * 4)))
+            (e = cudaMemcpy(a.orig, orig.data(), n * 4, cudaMemcpyHostToDevice)))
             return cuda_fail(e, "upload");
     }
     h->collider_bits.assign(n, 0);
@@ -895,6 +987,7 @@ int sv_download(sv_handle *h, sv_particles *o) {
     g_last_error.clear();
     if (!h || !o) return fail("sv_download: NULL argument");
     if (o->n != h->n) return fail("sv_download: particle count mismatch");
+    if (h->direct_host) return download_direct(h, o);  // kernels write the caller's arrays (sv_transfer.cu)
     const uint64_t n = h->n;
     const ParticleArrays &a = h->side[h->cur];
     std::vector<float4> pos(n), vel(n);
@@ -1111,6 +1204,14 @@ int sv_autotune(sv_handle *h, float dt, const float gravity[3], uint32_t substep
 int sv_set_graphs(sv_handle *h, int enable) {
     if (!h) return fail("sv_set_graphs: NULL handle");
     h->use_graphs = enable != 0;
+    return 0;
+}
+
+int sv_set_host_transfer(sv_handle *h, uint32_t mode, uint32_t *direct) {
+    if (!h) return fail("sv_set_host_transfer: NULL handle");
+    if (mode > 1) return fail("sv_set_host_transfer: mode must be 0 or 1");
+    h->direct_host = mode == 0 && pageable_access();
+    if (direct) *direct = h->direct_host ? 1u : 0u;
     return 0;
 }
 

@@ -49,7 +49,8 @@ enum Counter : int {
     C_CLOSURE_FB = 10,   // snow/sand particle-substeps that fell back to the return map
     C_CLOSURE_ERR = 11,  // a tensor-core wait of the learned closure gave up
     C_CTA_DONE = 12,     // CTAs of a self-latching particle pass that have finished
-    C_COUNT = 13,
+    C_TRANSFER_BAD = 13, // a direct download met an original index out of range or repeated
+    C_COUNT = 14,
 };
 
 // One side of the particle state (ping-pong).  Structure of arrays: pos and
@@ -160,6 +161,11 @@ struct sv_handle {
 
     uint32_t *counters = nullptr;       // device [C_COUNT]
     uint32_t *host_counters = nullptr;  // pinned mirror
+
+    // Upload and download by kernels that access the caller's pageable host
+    // arrays (sv_transfer.cu), where the device can; else staged copies.
+    bool direct_host = false;
+    uint32_t *inv = nullptr;  // [n] slot of each original particle (direct download)
     // C_STOP will hold the stop bits of every kernel queued so far (the last
     // status-setting launch was a latch or a self-latching particle pass)
     bool stop_latched = false;
@@ -285,6 +291,16 @@ cudaError_t launch_clear_variants(sv_handle *h, int which);
 // Reads the device counters into h->host_counters (waits for the stream);
 // -1 with the last error set on failure.
 int refresh_counters(sv_handle *h);
+
+// ---- direct host transfers (sv_transfer.cu) ----
+// whether the current device reads and writes pageable host memory
+bool pageable_access();
+// side 0 from the caller's arrays (h->scenes uploaded first); waits for it
+cudaError_t upload_direct(sv_handle *h, const sv_particles *ps, uint32_t n_scenes, const uint64_t *first,
+                          const uint32_t *mat_index);
+// the current side into the caller's arrays in the original order; -1 with
+// the last error set on failure
+int download_direct(sv_handle *h, sv_particles *out);
 
 // ---- host copies of the device state (sv_cache.cu) ----
 // One particle side copied to the host in device (binning) order.

@@ -1,0 +1,266 @@
+// sv_transfer.cu -- particle state to and from the caller's host arrays by
+// kernels that access pageable host memory directly.
+//
+// On a Grace host (NVLink-C2C, address translation through the host page
+// tables: cudaDevAttrPageableMemoryAccess) the GPU reads and writes ordinary
+// malloc'd memory coherently.  The upload then is one kernel that reads the
+// caller's arrays (file_frame's [n][3] / [n][9] layouts) and writes the
+// device layout -- packing flags with the material index, converting to the
+// cell + offset form, transposing the matrices into element planes -- instead
+// of a single-threaded host staging loop and pageable copies.  The download
+// inverts the binning permutation on the device and writes the caller's
+// arrays in the original particle order (the reference's reverse_sort_map
+// restore, cpu_state.rs:71-104) with coalesced stores.  Both give the same
+// bits as the staged path in sv_api.cu / sv_cache.cu, which remains for
+// devices without pageable-memory access.
+#include <sys/mman.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cstring>
+#include <thread>
+#include <utility>
+#include <vector>
+
+#include "sv_internal.h"
+
+namespace sv {
+namespace {
+
+constexpr int TPB = 256;
+
+struct UploadArgs {
+    const sv_particles *ps;      // host: one per scene
+    const uint64_t *first;       // host: first particle of each scene, n_scenes + 1
+    uint32_t n_scenes;
+    const uint32_t *mat_index;   // host: material of each particle
+    const SceneInfo *scenes;     // device
+    ParticleArrays a;            // device, side 0
+    uint64_t n;
+    double dx;
+};
+
+__device__ __forceinline__ uint32_t scene_of(const uint64_t *first, uint32_t n_scenes, uint64_t i) {
+    uint32_t lo = 0, hi = n_scenes;  // first[lo] <= i < first[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (first[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// The staged upload's per-particle conversion (sv_api.cu create_impl),
+// reading the caller's arrays directly.
+template <bool CELL> __global__ void __launch_bounds__(TPB) k_upload(UploadArgs u) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < u.n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t sc = scene_of(u.first, u.n_scenes, i);
+        const sv_particles &p = u.ps[sc];
+        const uint64_t li = i - u.first[sc];
+        const uint32_t packed = (p.flags[li] & FLAG_MASK) | (u.mat_index[i] << MATERIAL_SHIFT);
+        const float x = p.positions[3 * li], y = p.positions[3 * li + 1], z = p.positions[3 * li + 2];
+        float4 pos;
+        if (!CELL) {
+            pos = make_float4(x, y, z, 0.f);
+        } else {
+            const double q[3] = {(double)x / u.dx, (double)y / u.dx, (double)z / u.dx};
+            int ci[3];
+            float o[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const double f = floor(q[a]);
+                ci[a] = (int)f + u.scenes[sc].off[a];
+                o[a] = (float)(q[a] - f);
+                if (o[a] >= 1.f) o[a] = 0.f, ci[a] += 1;
+            }
+            pos = make_float4(o[0], o[1], o[2], 0.f);
+            u.a.cell[i] = make_int4(ci[0], ci[1], ci[2], 0);
+        }
+        pos.w = __uint_as_float(packed);
+        u.a.pos[i] = pos;
+        u.a.vel[i] = make_float4(p.velocities[3 * li], p.velocities[3 * li + 1], p.velocities[3 * li + 2],
+                                 p.plastic_j ? p.plastic_j[li] : 1.f);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            u.a.C[(uint64_t)k * u.n + i] = p.velocity_gradients[9 * li + k];
+            u.a.F[(uint64_t)k * u.n + i] = p.position_gradients[9 * li + k];
+        }
+        u.a.energy[i] = p.elastic_energies ? p.elastic_energies[li] : 0.f;
+        u.a.orig[i] = (uint32_t)i;
+    }
+}
+
+__global__ void __launch_bounds__(TPB) k_invert(const uint32_t *orig, uint32_t *inv, uint64_t n, uint32_t *bad) {
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t i = orig[s];
+        if (i >= n || atomicExch(&inv[i], (uint32_t)s) != 0xFFFFFFFFu) atomicOr(bad, 1u);
+    }
+}
+
+struct DownloadArgs {
+    ParticleArrays a;          // device, the current side
+    const uint32_t *inv;       // device: slot of each original particle
+    const Material *mats;      // device
+    const SceneInfo *scenes;   // device
+    const uint32_t *bits0;     // host: collider bits the particles were created with (no frame input)
+    bool stepped;
+    sv_particles o;            // host arrays (NULL ones are skipped)
+    uint64_t n;
+    uint32_t n_materials;
+    double dx;
+};
+
+// unpack_particles (sv_cache.cu) with the original index as the thread index.
+template <bool CELL> __global__ void __launch_bounds__(TPB) k_download(DownloadArgs d) {
+    const sv_particles &o = d.o;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t s = d.inv[i];
+        if (s >= d.n) continue;  // reported through the flag of k_invert
+        const float4 p = d.a.pos[s], v = d.a.vel[s];
+        const uint32_t packed = __float_as_uint(p.w);
+        if (o.flags) o.flags[i] = packed & FLAG_MASK;
+        if (o.positions) {
+            float x = p.x, y = p.y, z = p.z;
+            if (CELL) {
+                // back to the scene's own coordinates
+                const uint32_t mi = packed >> MATERIAL_SHIFT;
+                const SceneInfo &sc = d.scenes[mi < d.n_materials ? d.mats[mi].scene : 0];
+                const int4 c = d.a.cell[s];
+                x = (float)(((double)(c.x - sc.off[0]) + p.x) * d.dx);
+                y = (float)(((double)(c.y - sc.off[1]) + p.y) * d.dx);
+                z = (float)(((double)(c.z - sc.off[2]) + p.z) * d.dx);
+            }
+            o.positions[3 * i] = x, o.positions[3 * i + 1] = y, o.positions[3 * i + 2] = z;
+        }
+        if (o.velocities) o.velocities[3 * i] = v.x, o.velocities[3 * i + 1] = v.y, o.velocities[3 * i + 2] = v.z;
+        if (o.plastic_j) o.plastic_j[i] = v.w;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            if (o.position_gradients) o.position_gradients[9 * i + k] = d.a.F[(uint64_t)k * d.n + s];
+            if (o.velocity_gradients) o.velocity_gradients[9 * i + k] = d.a.C[(uint64_t)k * d.n + s];
+        }
+        if (o.elastic_energies) o.elastic_energies[i] = d.a.energy[s];
+        if (o.collider_bits) {
+            // without colliders every substep's Collide clears a live
+            // particle's bits (collide.rs:53-56)
+            if (d.a.cbits_done) o.collider_bits[i] = d.a.cbits_done[s];
+            else o.collider_bits[i] = (d.stepped && !(packed & SV_TOMBSTONED)) ? 0u : (d.bits0 ? d.bits0[i] : 0u);
+        }
+    }
+}
+
+// Populates the pages of the caller's output arrays from host threads (one
+// read-and-write of the same byte per page, so the contents stay).  A page
+// the GPU touches first is populated through a device-side fault serviced
+// by the host, tens of microseconds each; freshly allocated arrays (numpy's
+// zeros map pages lazily) would otherwise cost more than the copy itself.
+void populate(const std::vector<std::pair<void *, size_t>> &arrays) {
+    const size_t page = (size_t)std::max(4096L, sysconf(_SC_PAGESIZE));
+    size_t total = 0;
+    for (const auto &a : arrays) total += a.second;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned T = (unsigned)std::max<size_t>(1, std::min<size_t>(std::min(hw, 16u), total / (8u << 20)));
+    auto work = [&](unsigned t) {
+        for (const auto &a : arrays) {
+            const uintptr_t b0 = (uintptr_t)a.first / page * page;
+            const uintptr_t b1 = ((uintptr_t)a.first + a.second + page - 1) / page * page;
+            const size_t pages = (b1 - b0) / page;
+            const uintptr_t c0 = b0 + pages * t / T * page, c1 = b0 + pages * (t + 1) / T * page;
+            if (c1 <= c0) continue;
+            // one call populates the range writable (Linux 5.14+); else touch each page
+            if (madvise((void *)c0, c1 - c0, MADV_POPULATE_WRITE) == 0) continue;
+            for (uintptr_t q = std::max<uintptr_t>(c0, (uintptr_t)a.first); q < c1 && q < (uintptr_t)a.first + a.second;
+                 q = (q / page + 1) * page) {
+                volatile uint8_t *p = reinterpret_cast<volatile uint8_t *>(q);
+                *p = *p;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < T; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (auto &th : pool) th.join();
+}
+
+unsigned blocks_for(uint64_t n) {
+    const uint64_t b = (n + TPB - 1) / TPB;
+    const uint64_t cap = (uint64_t)sm_count() * 8;
+    return (unsigned)std::max<uint64_t>(1, std::min(b, cap));
+}
+
+}  // namespace
+
+bool pageable_access() {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) return false;
+    return v == 1;
+}
+
+cudaError_t upload_direct(sv_handle *h, const sv_particles *ps, uint32_t n_scenes, const uint64_t *first,
+                          const uint32_t *mat_index) {
+    UploadArgs u;
+    u.ps = ps, u.first = first, u.n_scenes = n_scenes, u.mat_index = mat_index;
+    u.scenes = h->scenes, u.a = h->side[0], u.n = h->n, u.dx = h->layout.dx;
+    if (h->n == 0) return cudaSuccess;
+    if (h->layout.position_form == 1) k_upload<true><<<blocks_for(h->n), TPB, 0, h->stream>>>(u);
+    else k_upload<false><<<blocks_for(h->n), TPB, 0, h->stream>>>(u);
+    h->launches += 1;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);  // the caller's arrays may go away
+    return e;
+}
+
+int download_direct(sv_handle *h, sv_particles *o) {
+    const uint64_t n = h->n;
+    if (n == 0) return 0;
+    cudaError_t e;
+    if (!h->inv) {
+        if ((e = cudaMalloc((void **)&h->inv, n * 4)) != cudaSuccess) {
+            h->inv = nullptr;
+            set_last_error(std::string("sv_download: ") + cudaGetErrorString(e));
+            return -1;
+        }
+        h->device_bytes += n * 4;
+    }
+    uint32_t *bad = h->counters + C_TRANSFER_BAD;  // an original index out of range or repeated
+    DownloadArgs d;
+    d.a = h->side[h->cur], d.inv = h->inv, d.mats = h->materials, d.scenes = h->scenes;
+    d.bits0 = h->collider_bits.empty() ? nullptr : h->collider_bits.data();
+    d.stepped = h->substeps_total > 0;
+    d.o = *o, d.n = n, d.n_materials = h->n_materials, d.dx = h->layout.dx;
+    // unset entries (a corrupt state) stay 0xFFFFFFFF and are skipped
+    if ((e = cudaMemsetAsync(bad, 0, 4, h->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(h->inv, 0xFF, n * 4, h->stream)) != cudaSuccess) {
+        set_last_error(std::string("sv_download: ") + cudaGetErrorString(e));
+        return -1;
+    }
+    k_invert<<<blocks_for(n), TPB, 0, h->stream>>>(h->side[h->cur].orig, h->inv, n, bad);
+    {
+        std::vector<std::pair<void *, size_t>> out;
+        auto add = [&](void *p, size_t bytes) {
+            if (p) out.push_back({p, bytes});
+        };
+        add(o->flags, n * 4), add(o->positions, n * 12), add(o->position_gradients, n * 36);
+        add(o->velocities, n * 12), add(o->velocity_gradients, n * 36), add(o->elastic_energies, n * 4);
+        add(o->collider_bits, n * 4), add(o->plastic_j, n * 4);
+        populate(out);  // overlaps k_invert
+    }
+    if (h->layout.position_form == 1) k_download<true><<<blocks_for(n), TPB, 0, h->stream>>>(d);
+    else k_download<false><<<blocks_for(n), TPB, 0, h->stream>>>(d);
+    h->launches += 2;
+    uint32_t flag = 0;
+    if ((e = cudaGetLastError()) != cudaSuccess ||
+        (e = cudaMemcpyAsync(&flag, bad, 4, cudaMemcpyDeviceToHost, h->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(h->stream)) != cudaSuccess) {
+        set_last_error(std::string("sv_download: ") + cudaGetErrorString(e));
+        return -1;
+    }
+    if (flag) {
+        set_last_error("sv_download: corrupt original index");
+        return -1;
+    }
+    return 0;
+}
+
+}  // namespace sv

@@ -245,6 +245,7 @@ class Extras:
     svd_fp64_policy: int = 1
     block_capacity: int = 0
     sort_interval: int = 0  # 0 adaptive, 1 every substep, k every k substeps
+    host_transfer: int = 0  # 0 direct access to host arrays where possible, 1 staged copies
 
 
 @dataclass
@@ -346,6 +347,7 @@ class CudaState:
         c.svd_fp64_policy = extras.svd_fp64_policy
         c.block_capacity = extras.block_capacity
         c.sort_interval = extras.sort_interval
+        c.host_transfer = extras.host_transfer
         return c
 
     @classmethod
@@ -544,6 +546,14 @@ class CudaState:
 
     def set_graphs(self, on: bool):
         check(self._lib.sv_set_graphs(self._h, 1 if on else 0))
+
+    def set_host_transfer(self, mode: int) -> bool:
+        """0: downloads by kernels writing the host arrays where the device
+        can access pageable memory, 1: staged copies; returns whether the
+        direct path is in use."""
+        direct = ct.c_uint32(0)
+        check(self._lib.sv_set_host_transfer(self._h, int(mode), ct.byref(direct)))
+        return bool(direct.value)
 
     def autotune(self, dt: float, gravity, substeps_per_trial: int = 16):
         """Times the binning interval x CTAs-per-SM candidates on a snapshot
