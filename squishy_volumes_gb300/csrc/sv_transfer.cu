@@ -50,43 +50,82 @@ __device__ __forceinline__ uint32_t scene_of(const uint64_t *first, uint32_t n_s
     return lo;
 }
 
+// One particle of the upload, its position, velocity and matrix rows already
+// in shared memory.
+template <bool CELL>
+__device__ __forceinline__ void upload_one(const UploadArgs &u, uint64_t i, const float *rx, const float *rv,
+                                           const float *rF, const float *rC) {
+    const uint32_t sc = scene_of(u.first, u.n_scenes, i);
+    const sv_particles &p = u.ps[sc];
+    const uint64_t li = i - u.first[sc];
+    const uint32_t packed = (p.flags[li] & FLAG_MASK) | (u.mat_index[i] << MATERIAL_SHIFT);
+    const float x = rx[0], y = rx[1], z = rx[2];
+    float4 pos;
+    if (!CELL) {
+        pos = make_float4(x, y, z, 0.f);
+    } else {
+        const double q[3] = {(double)x / u.dx, (double)y / u.dx, (double)z / u.dx};
+        int ci[3];
+        float o[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const double f = floor(q[a]);
+            ci[a] = (int)f + u.scenes[sc].off[a];
+            o[a] = (float)(q[a] - f);
+            if (o[a] >= 1.f) o[a] = 0.f, ci[a] += 1;
+        }
+        pos = make_float4(o[0], o[1], o[2], 0.f);
+        u.a.cell[i] = make_int4(ci[0], ci[1], ci[2], 0);
+    }
+    pos.w = __uint_as_float(packed);
+    u.a.pos[i] = pos;
+    u.a.vel[i] = make_float4(rv[0], rv[1], rv[2], p.plastic_j ? p.plastic_j[li] : 1.f);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        u.a.C[(uint64_t)k * u.n + i] = rC[k];
+        u.a.F[(uint64_t)k * u.n + i] = rF[k];
+    }
+    u.a.energy[i] = p.elastic_energies ? p.elastic_energies[li] : 0.f;
+    u.a.orig[i] = (uint32_t)i;
+}
+
+// Loads a tile's rows of `width` floats (src rows li0 ...) into shared memory
+// with consecutive threads on consecutive words.
+__device__ __forceinline__ void load_rows(float *stage, const float *src, uint64_t li0, int count, int width) {
+    const float *in = src + li0 * width;
+    for (int e = threadIdx.x; e < count * width; e += TPB) stage[e] = in[e];
+}
+
 // The staged upload's per-particle conversion (sv_api.cu create_impl),
-// reading the caller's arrays directly.
+// reading the caller's arrays directly: over tiles of TPB particles, whose
+// [n][3] and [n][9] rows arrive through shared memory with coalesced loads.
 template <bool CELL> __global__ void __launch_bounds__(TPB) k_upload(UploadArgs u) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < u.n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t sc = scene_of(u.first, u.n_scenes, i);
-        const sv_particles &p = u.ps[sc];
-        const uint64_t li = i - u.first[sc];
-        const uint32_t packed = (p.flags[li] & FLAG_MASK) | (u.mat_index[i] << MATERIAL_SHIFT);
-        const float x = p.positions[3 * li], y = p.positions[3 * li + 1], z = p.positions[3 * li + 2];
-        float4 pos;
-        if (!CELL) {
-            pos = make_float4(x, y, z, 0.f);
-        } else {
-            const double q[3] = {(double)x / u.dx, (double)y / u.dx, (double)z / u.dx};
-            int ci[3];
-            float o[3];
+    __shared__ float sx[TPB * 3], sv[TPB * 3], sF[TPB * 9], sC[TPB * 9];
+    for (uint64_t i0 = (uint64_t)blockIdx.x * TPB; i0 < u.n; i0 += (uint64_t)gridDim.x * TPB) {
+        const int count = (int)(u.n - i0 < (uint64_t)TPB ? u.n - i0 : (uint64_t)TPB);
+        const int t = threadIdx.x;
+        const uint32_t s0 = scene_of(u.first, u.n_scenes, i0), s1 = scene_of(u.first, u.n_scenes, i0 + count - 1);
+        if (s0 == s1) {
+            const sv_particles &p = u.ps[s0];
+            const uint64_t li0 = i0 - u.first[s0];
+            load_rows(sx, p.positions, li0, count, 3);
+            load_rows(sv, p.velocities, li0, count, 3);
+            load_rows(sF, p.position_gradients, li0, count, 9);
+            load_rows(sC, p.velocity_gradients, li0, count, 9);
+        } else if (t < count) {
+            // a tile across scenes: each thread its own rows
+            const uint32_t sc = scene_of(u.first, u.n_scenes, i0 + t);
+            const sv_particles &p = u.ps[sc];
+            const uint64_t li = i0 + t - u.first[sc];
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                const double f = floor(q[a]);
-                ci[a] = (int)f + u.scenes[sc].off[a];
-                o[a] = (float)(q[a] - f);
-                if (o[a] >= 1.f) o[a] = 0.f, ci[a] += 1;
-            }
-            pos = make_float4(o[0], o[1], o[2], 0.f);
-            u.a.cell[i] = make_int4(ci[0], ci[1], ci[2], 0);
-        }
-        pos.w = __uint_as_float(packed);
-        u.a.pos[i] = pos;
-        u.a.vel[i] = make_float4(p.velocities[3 * li], p.velocities[3 * li + 1], p.velocities[3 * li + 2],
-                                 p.plastic_j ? p.plastic_j[li] : 1.f);
+            for (int k = 0; k < 3; ++k) sx[3 * t + k] = p.positions[3 * li + k], sv[3 * t + k] = p.velocities[3 * li + k];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            u.a.C[(uint64_t)k * u.n + i] = p.velocity_gradients[9 * li + k];
-            u.a.F[(uint64_t)k * u.n + i] = p.position_gradients[9 * li + k];
+            for (int k = 0; k < 9; ++k)
+                sF[9 * t + k] = p.position_gradients[9 * li + k], sC[9 * t + k] = p.velocity_gradients[9 * li + k];
         }
-        u.a.energy[i] = p.elastic_energies ? p.elastic_energies[li] : 0.f;
-        u.a.orig[i] = (uint32_t)i;
+        __syncthreads();
+        if (t < count) upload_one<CELL>(u, i0 + t, sx + 3 * t, sv + 3 * t, sF + 9 * t, sC + 9 * t);
+        __syncthreads();
     }
 }
 
@@ -110,16 +149,29 @@ struct DownloadArgs {
     double dx;
 };
 
-// unpack_particles (sv_cache.cu) with the original index as the thread index.
+// Writes a tile's rows of `width` floats, staged in shared memory, to
+// dst[i0 * width ...] with consecutive threads on consecutive words, so that
+// every host-memory transaction covers whole cache lines.
+__device__ __forceinline__ void flush_rows(float *dst, const float *stage, uint64_t i0, int count, int width) {
+    float *out = dst + i0 * width;
+    for (int e = threadIdx.x; e < count * width; e += TPB) out[e] = stage[e];
+}
+
+// unpack_particles (sv_cache.cu) over tiles of TPB particles in original
+// order: each thread gathers its particle from the device state, the tile's
+// [n][3] and [n][9] rows are staged in shared memory and leave coalesced.
 template <bool CELL> __global__ void __launch_bounds__(TPB) k_download(DownloadArgs d) {
+    __shared__ float sx[TPB * 3], sv[TPB * 3], sF[TPB * 9], sC[TPB * 9];
     const sv_particles &o = d.o;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t s = d.inv[i];
-        if (s >= d.n) continue;  // reported through the flag of k_invert
-        const float4 p = d.a.pos[s], v = d.a.vel[s];
-        const uint32_t packed = __float_as_uint(p.w);
-        if (o.flags) o.flags[i] = packed & FLAG_MASK;
-        if (o.positions) {
+    for (uint64_t i0 = (uint64_t)blockIdx.x * TPB; i0 < d.n; i0 += (uint64_t)gridDim.x * TPB) {
+        const int count = (int)(d.n - i0 < (uint64_t)TPB ? d.n - i0 : (uint64_t)TPB);
+        const int t = threadIdx.x;
+        const uint64_t i = i0 + t;
+        const uint64_t s = t < count ? d.inv[i] : d.n;
+        if (s < d.n) {  // else unset (reported through the flag of k_invert) or past the end
+            const float4 p = d.a.pos[s], v = d.a.vel[s];
+            const uint32_t packed = __float_as_uint(p.w);
+            if (o.flags) o.flags[i] = packed & FLAG_MASK;
             float x = p.x, y = p.y, z = p.z;
             if (CELL) {
                 // back to the scene's own coordinates
@@ -130,22 +182,40 @@ template <bool CELL> __global__ void __launch_bounds__(TPB) k_download(DownloadA
                 y = (float)(((double)(c.y - sc.off[1]) + p.y) * d.dx);
                 z = (float)(((double)(c.z - sc.off[2]) + p.z) * d.dx);
             }
-            o.positions[3 * i] = x, o.positions[3 * i + 1] = y, o.positions[3 * i + 2] = z;
-        }
-        if (o.velocities) o.velocities[3 * i] = v.x, o.velocities[3 * i + 1] = v.y, o.velocities[3 * i + 2] = v.z;
-        if (o.plastic_j) o.plastic_j[i] = v.w;
+            sx[3 * t] = x, sx[3 * t + 1] = y, sx[3 * t + 2] = z;
+            sv[3 * t] = v.x, sv[3 * t + 1] = v.y, sv[3 * t + 2] = v.z;
+            if (o.plastic_j) o.plastic_j[i] = v.w;
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            if (o.position_gradients) o.position_gradients[9 * i + k] = d.a.F[(uint64_t)k * d.n + s];
-            if (o.velocity_gradients) o.velocity_gradients[9 * i + k] = d.a.C[(uint64_t)k * d.n + s];
+            for (int k = 0; k < 9; ++k) {
+                sF[9 * t + k] = d.a.F[(uint64_t)k * d.n + s];
+                sC[9 * t + k] = d.a.C[(uint64_t)k * d.n + s];
+            }
+            if (o.elastic_energies) o.elastic_energies[i] = d.a.energy[s];
+            if (o.collider_bits) {
+                // without colliders every substep's Collide clears a live
+                // particle's bits (collide.rs:53-56)
+                if (d.a.cbits_done) o.collider_bits[i] = d.a.cbits_done[s];
+                else o.collider_bits[i] = (d.stepped && !(packed & SV_TOMBSTONED)) ? 0u : (d.bits0 ? d.bits0[i] : 0u);
+            }
+        } else if (t < count) {
+            // an unset row keeps what the caller's array held
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                sx[3 * t + k] = o.positions ? o.positions[3 * i + k] : 0.f;
+                sv[3 * t + k] = o.velocities ? o.velocities[3 * i + k] : 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                sF[9 * t + k] = o.position_gradients ? o.position_gradients[9 * i + k] : 0.f;
+                sC[9 * t + k] = o.velocity_gradients ? o.velocity_gradients[9 * i + k] : 0.f;
+            }
         }
-        if (o.elastic_energies) o.elastic_energies[i] = d.a.energy[s];
-        if (o.collider_bits) {
-            // without colliders every substep's Collide clears a live
-            // particle's bits (collide.rs:53-56)
-            if (d.a.cbits_done) o.collider_bits[i] = d.a.cbits_done[s];
-            else o.collider_bits[i] = (d.stepped && !(packed & SV_TOMBSTONED)) ? 0u : (d.bits0 ? d.bits0[i] : 0u);
-        }
+        __syncthreads();
+        if (o.positions) flush_rows(o.positions, sx, i0, count, 3);
+        if (o.velocities) flush_rows(o.velocities, sv, i0, count, 3);
+        if (o.position_gradients) flush_rows(o.position_gradients, sF, i0, count, 9);
+        if (o.velocity_gradients) flush_rows(o.velocity_gradients, sC, i0, count, 9);
+        __syncthreads();
     }
 }
 
