@@ -302,6 +302,12 @@ int sv_set_graphs(sv_handle *h, int enable);
 /* sv_consts::host_transfer for the handle's later downloads; *direct (if
  * not NULL) tells whether the direct path is now in use. */
 int sv_set_host_transfer(sv_handle *h, uint32_t mode, uint32_t *direct);
+/* Maps the pages of `count` host arrays (bytes[k] bytes at arrays[k]) for a
+ * later direct sv_download into them, without changing their contents.  A
+ * page the GPU writes first is mapped through a device-side fault, much
+ * slower; freshly allocated arrays can be prepared from another thread while
+ * sv_step runs.  Touches no handle. */
+int sv_prepare_host(void *const *arrays, const uint64_t *bytes, uint32_t count);
 int sv_get_stats(sv_handle *h, sv_stats *out);
 
 /* Addition: picks the substeps between binning sorts and the CTAs per SM of

@@ -186,6 +186,7 @@ _SIGNATURES = {
     "sv_set_stream": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "sv_set_graphs": (ct.c_int, [ct.c_void_p, ct.c_int]),
     "sv_set_host_transfer": (ct.c_int, [ct.c_void_p, ct.c_uint32, u32p]),
+    "sv_prepare_host": (ct.c_int, [ct.POINTER(ct.c_void_p), ct.POINTER(ct.c_uint64), ct.c_uint32]),
     "sv_step_adaptive": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_double), ct.c_double, ct.c_float, f32p,
                                     ct.POINTER(ct.c_int32), u32p, u32p]),
     "sv_time_step_limits": (ct.c_int, [ct.c_void_p, f32p]),

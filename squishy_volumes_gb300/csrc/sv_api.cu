@@ -90,6 +90,7 @@ struct Prepass {
     std::vector<Material> mats;
     std::vector<uint32_t> mat_index;
     std::vector<std::array<double, 3>> lo, hi;  // per scene, of live particles
+    bool any_bits = false;                      // some particle has collider bits
     std::string err;
 };
 
@@ -105,7 +106,7 @@ void prepass(const sv_particles *ps, uint32_t n_scenes, const std::vector<uint64
         std::vector<std::array<double, 3>> lo, hi;
         uint64_t err_at = UINT64_MAX;
         std::string err;
-        bool nonfinite = false;
+        bool nonfinite = false, any_bits = false;
     };
     std::vector<Part> parts(T);
     auto range = [&](unsigned t, uint64_t &g0, uint64_t &g1) { g0 = n * t / T, g1 = n * (t + 1) / T; };
@@ -130,6 +131,7 @@ void prepass(const sv_particles *ps, uint32_t n_scenes, const std::vector<uint64
                 return;
             }
             m.scene = s;
+            if (p->collider_bits && p->collider_bits[i]) pt.any_bits = true;
             if (!(p->flags[i] & SV_TOMBSTONED)) {
                 for (int a = 0; a < 3; ++a) {
                     const double x = p->positions[3 * i + a];
@@ -195,6 +197,7 @@ void prepass(const sv_particles *ps, uint32_t n_scenes, const std::vector<uint64
     bool nonfinite = false;
     for (const Part &pt : parts) {
         nonfinite |= pt.nonfinite;
+        out.any_bits |= pt.any_bits;
         for (uint32_t s = 0; s < n_scenes; ++s)
             for (int a = 0; a < 3; ++a)
                 out.lo[s][a] = std::min(out.lo[s][a], pt.lo[s][a]), out.hi[s][a] = std::max(out.hi[s][a], pt.hi[s][a]);
@@ -635,7 +638,9 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
         return cuda_fail(e, "sort buffers");
     if ((e = dalloc(h, &h->blockmap[0], total)) || (e = dalloc(h, &h->blockmap[1], total)))
         return cuda_fail(e, "block map");
-    uint64_t cap = c.block_capacity ? c.block_capacity : std::min<uint64_t>(total, std::max<uint64_t>(65536, n / 4));
+    // blocks claimed are about n / 200 for bodies of 8 particles per cell;
+    // n / 16 leaves room for sparse ones, and sv_step doubles it on overflow
+    uint64_t cap = c.block_capacity ? c.block_capacity : std::min<uint64_t>(total, std::max<uint64_t>(65536, n / 16));
     if ((e = alloc_grid(h, cap))) return cuda_fail(e, "grid");
     if ((e = cudaMallocHost((void **)&h->host_counters, C_COUNT * sizeof(uint32_t)))) return cuda_fail(e, "pinned");
 
@@ -696,8 +701,10 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
             (e = cudaMemcpy(a.orig, orig.data(), n * 4, cudaMemcpyHostToDevice)))
             return cuda_fail(e, "upload");
     }
-    h->collider_bits.assign(n, 0);
-    if (!batched && ps[0].collider_bits) h->collider_bits.assign(ps[0].collider_bits, ps[0].collider_bits + n);
+    // kept only when some particle starts with collider bits (empty: all 0)
+    h->collider_bits.clear();
+    if (!batched && ps[0].collider_bits && pre.any_bits)
+        h->collider_bits.assign(ps[0].collider_bits, ps[0].collider_bits + n);
     h->keys_valid = false;
     *out = h;
     return 0;

@@ -242,7 +242,7 @@ extern "C" int sv_set_frame_input(sv_handle *h, const sv_frame_input *in) {
     // input (whose Collide would have cleared them), and the variant tables
     if (!h->side[0].cbits) {
         std::vector<uint32_t> bits(n, 0u);
-        if (h->substeps_total == 0) {
+        if (h->substeps_total == 0 && !h->collider_bits.empty()) {
             std::vector<uint32_t> orig(n);
             FR_CUDA(cudaMemcpy(orig.data(), h->side[h->cur].orig, n * 4, cudaMemcpyDeviceToHost));
             for (uint64_t s = 0; s < n; ++s) bits[s] = h->collider_bits[orig[s]];

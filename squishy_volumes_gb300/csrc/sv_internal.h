@@ -178,7 +178,8 @@ struct sv_handle {
     uint64_t launches = 0;  // kernels launched by this handle
     uint64_t sorts = 0;     // binning sorts run
 
-    // host-side copies of what the substep never changes
+    // host-side copies of what the substep never changes: the collider bits
+    // the particles were created with (empty when all are 0)
     std::vector<uint32_t> collider_bits;
 
     bool profiling = false;

@@ -334,3 +334,15 @@ int download_direct(sv_handle *h, sv_particles *o) {
 }
 
 }  // namespace sv
+
+extern "C" int sv_prepare_host(void *const *arrays, const uint64_t *bytes, uint32_t count) {
+    if (count && (!arrays || !bytes)) {
+        sv::set_last_error("sv_prepare_host: NULL argument");
+        return -1;
+    }
+    std::vector<std::pair<void *, size_t>> list;
+    for (uint32_t k = 0; k < count; ++k)
+        if (arrays[k] && bytes[k]) list.push_back({arrays[k], (size_t)bytes[k]});
+    sv::populate(list);
+    return 0;
+}

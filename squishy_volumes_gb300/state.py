@@ -20,6 +20,7 @@ physics.
 from __future__ import annotations
 
 import ctypes as ct
+import threading
 from dataclasses import dataclass, field, fields
 from typing import Optional
 
@@ -308,6 +309,9 @@ class CudaState:
         self._template = template
         self._frame_keep = None
         self.time = time
+        direct = ct.c_uint32(0)
+        check(self._lib.sv_set_host_transfer(self._h, int(extras.host_transfer), ct.byref(direct)))
+        self._direct = bool(direct.value)  # downloads by kernels writing the host arrays
 
     # the simulation time lives in the handle (sv_step advances it)
     @property
@@ -413,14 +417,19 @@ class CudaState:
         buffered EnergyError (state still valid).  Canceled / ZeroTimeStep
         are raised, like the reference's outer Result."""
         if params.adaptive_time_steps:
-            status, done, t = self.step_adaptive(params.target_time, params.max_time_step, frame_input.gravity,
-                                                 harness)
+            out, helper = self._download_ahead()
+            try:
+                status, done, t = self.step_adaptive(params.target_time, params.max_time_step, frame_input.gravity,
+                                                     harness)
+            finally:
+                if helper is not None:
+                    helper.join()
             error = None
             if status & _abi.SV_STATUS_PARTICLE_INVERTED:
                 error = EnergyError("The position gradient has negative determinant")
             if status & _abi.SV_STATUS_CANCELED:
                 raise Canceled("The computation was canceled")
-            return self.to_io_state(params.store_grid), error
+            return self.to_io_state(params.store_grid, out), error
         dt = np.float32(params.max_time_step)
         if dt == 0:
             raise ZeroTimeStep("The time step ended up being 0")
@@ -431,43 +440,74 @@ class CudaState:
         while t < params.target_time:
             t += float(dt)
             n += 1
-        status, done = self.step(n, float(dt), frame_input.gravity, harness)
+        out, helper = self._download_ahead()
+        try:
+            status, done = self.step(n, float(dt), frame_input.gravity, harness)
+        finally:
+            if helper is not None:
+                helper.join()
         error = None
         if status & _abi.SV_STATUS_PARTICLE_INVERTED:
             error = EnergyError("The position gradient has negative determinant")
         if status & _abi.SV_STATUS_CANCELED:
             raise Canceled("The computation was canceled")
-        return self.to_io_state(params.store_grid), error
+        return self.to_io_state(params.store_grid, out), error
 
     # -- to_io_state (cpu_state.rs:68-135)
-    def download(self, out: Optional[Particles] = None) -> Particles:
+    _DOWNLOADED = ("flags", "positions", "position_gradients", "velocities", "velocity_gradients",
+                   "elastic_energies", "collider_bits", "plastic_j")
+
+    def _new_download(self) -> Particles:
+        """Particles with fresh arrays for what sv_download writes (every
+        element of them) and the template's parameters."""
         t = self._template
         n = self.n
+        return Particles(
+            flags=np.empty(n, np.uint32),
+            positions=np.empty((n, 3), np.float32),
+            position_gradients=np.empty((n, 9), np.float32),
+            velocities=np.empty((n, 3), np.float32),
+            velocity_gradients=np.empty((n, 9), np.float32),
+            mass=t.mass,
+            initial_volume=t.initial_volume,
+            mu=t.mu,
+            lambda_=t.lambda_,
+            sand_alpha=t.sand_alpha,
+            exponent=t.exponent,
+            bulk_modulus=t.bulk_modulus,
+            viscosity_dynamic=t.viscosity_dynamic,
+            viscosity_bulk=t.viscosity_bulk,
+            elastic_energies=np.empty(n, np.float32),
+            collider_bits=np.empty(n, np.uint32),
+            initial_positions=self._initial_positions,
+            model=t.model,
+            hardening=t.hardening,
+            crit_compression=t.crit_compression,
+            crit_stretch=t.crit_stretch,
+            plastic_j=np.empty(n, np.float32),
+        )
+
+    def _prepare(self, out: Particles) -> None:
+        """Maps the pages of out's downloaded arrays (sv_prepare_host)."""
+        arrays = [getattr(out, k) for k in self._DOWNLOADED]
+        ptrs = (ct.c_void_p * len(arrays))(*[a.ctypes.data for a in arrays])
+        sizes = (ct.c_uint64 * len(arrays))(*[a.nbytes for a in arrays])
+        check(self._lib.sv_prepare_host(ptrs, sizes, len(arrays)))
+
+    def _download_ahead(self):
+        """For the direct download: the frame's output arrays, and a thread
+        that maps their pages while the substeps run (the calling thread
+        only waits on the GPU then)."""
+        if not self._direct:
+            return None, None
+        out = self._new_download()
+        helper = threading.Thread(target=self._prepare, args=(out,), daemon=True)
+        helper.start()
+        return out, helper
+
+    def download(self, out: Optional[Particles] = None) -> Particles:
         if out is None:
-            out = Particles(
-                flags=np.zeros(n, np.uint32),
-                positions=np.zeros((n, 3), np.float32),
-                position_gradients=np.zeros((n, 9), np.float32),
-                velocities=np.zeros((n, 3), np.float32),
-                velocity_gradients=np.zeros((n, 9), np.float32),
-                mass=t.mass,
-                initial_volume=t.initial_volume,
-                mu=t.mu,
-                lambda_=t.lambda_,
-                sand_alpha=t.sand_alpha,
-                exponent=t.exponent,
-                bulk_modulus=t.bulk_modulus,
-                viscosity_dynamic=t.viscosity_dynamic,
-                viscosity_bulk=t.viscosity_bulk,
-                elastic_energies=np.zeros(n, np.float32),
-                collider_bits=np.zeros(n, np.uint32),
-                initial_positions=self._initial_positions,
-                model=t.model,
-                hardening=t.hardening,
-                crit_compression=t.crit_compression,
-                crit_stretch=t.crit_stretch,
-                plastic_j=np.ones(n, np.float32),
-            )
+            out = self._new_download()
         s = out.to_struct()
         check(self._lib.sv_download(self._h, ct.byref(s)))
         return out
@@ -483,8 +523,8 @@ class CudaState:
                                          ct.byref(cnt)))
         return GridNodes(ids, np.zeros(m, np.uint32), masses, vel)
 
-    def to_io_state(self, store_grid: bool = False) -> IoState:
-        return IoState(self.time, self.download(), self.grid() if store_grid else None)
+    def to_io_state(self, store_grid: bool = False, out: Optional[Particles] = None) -> IoState:
+        return IoState(self.time, self.download(out), self.grid() if store_grid else None)
 
     # -- inspection
     def p2g_only(self, dt: float, gravity) -> GridNodes:
