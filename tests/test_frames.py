@@ -182,3 +182,22 @@ def test_cache_reports_a_failed_writer(cuda_lib, tmp_path):
         cache.store_io_state(io)
     with pytest.raises(SvError):
         cache.close()
+
+
+def test_prepare_host_keeps_contents(cuda_lib):
+    """sv_prepare_host maps the pages of host arrays without changing them
+    (no device involved)."""
+    import ctypes as ct
+
+    rng = np.random.default_rng(9)
+    arrays = [rng.standard_normal(n).astype(np.float32) for n in (1, 1000, 3_000_000)]
+    arrays.append(np.empty(2_000_000, np.uint32))  # fresh pages
+    arrays[-1][:] = 7
+    copies = [a.copy() for a in arrays]
+    ptrs = (ct.c_void_p * 5)(*[a.ctypes.data for a in arrays], None)
+    sizes = (ct.c_uint64 * 5)(*[a.nbytes for a in arrays], 64)
+    assert cuda_lib.sv_prepare_host(ptrs, sizes, 5) == 0  # NULL entries are skipped
+    for a, c in zip(arrays, copies):
+        np.testing.assert_array_equal(a, c)
+    assert cuda_lib.sv_prepare_host(None, None, 0) == 0
+    assert cuda_lib.sv_prepare_host(None, sizes, 1) == -1
