@@ -61,7 +61,7 @@ void free_handle(sv_handle *h) {
         if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     free_closure(h);
     free_frame(h);
-    cudaFree(h->adt);
+    cudaFree(h->adt), cudaFree(h->adt_backup);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
 }
@@ -839,21 +839,30 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
 namespace {
 
 int adaptive_substep(sv_handle *h, float3 g) {
-    if (!h->keys_valid) SV_CUDA(launch_keys(h));
-    SV_CUDA(launch_sort_and_segments(h));
-    const int which = h->map_cur ^ 1;
-    SV_CUDA(launch_activate(h, which));
-    h->map_cur = h->map_next = which;
+    SV_CUDA(launch_adaptive_begin(h));
+    // The binning is redone every sort_interval substeps, as in the fused
+    // path: particles that left their segment's tile scatter and gather
+    // through global memory, and one that left the claimed blocks stops the
+    // substep (ST_MOVED_FAR), which sv_step_adaptive then redoes.
+    if (h->since_sort >= h->sort_interval) {
+        if (!h->keys_valid) SV_CUDA(launch_keys(h));
+        SV_CUDA(launch_sort_and_segments(h));
+        const int which = h->map_cur ^ 1;
+        SV_CUDA(launch_activate(h, which));
+        h->map_cur = h->map_next = which;
+        h->since_sort = 0;
+    }
     if (h->fin_active) {
         SV_CUDA(launch_interpolate(h, 0.0));  // at the device time of the substep
         SV_CUDA(launch_clear_variants(h, h->gcur));
     }
     SV_CUDA(launch_limits_force(h));
-    SV_CUDA(launch_clear(h, h->gcur, which));
+    SV_CUDA(launch_clear(h, h->gcur, h->map_cur));
     SV_CUDA(launch_p2g(h, 0.f, g));
     SV_CUDA(launch_grid_update(h, false));
     SV_CUDA(launch_g2p_only(h));
     SV_CUDA(launch_advance(h));
+    h->since_sort += 1;
     return 0;
 }
 
@@ -871,6 +880,7 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
     adaptive::State st;
     if (!h->adt) {
         SV_CUDA(cudaMalloc(&h->adt, sizeof(adaptive::State)));
+        SV_CUDA(cudaMalloc(&h->adt_backup, sizeof(adaptive::State)));
         std::memset(&st, 0, sizeof(st));
         st.vel = st.def = st.sound = st.iso = adaptive::NONE;
         st.hist_len = 0;
@@ -892,6 +902,7 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
     h->since_sort = h->sort_interval;
     if (!(st.time < target_time)) return 0;
     const uint32_t base = h->host_counters[C_SUBSTEPS];
+    uint32_t fallback_before = h->host_counters[C_FALLBACK], substeps_before = base;
     uint32_t status = 0;
     h->adaptive_active = true;
     int rc = 0;
@@ -923,22 +934,39 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
             break;
         }
         if (stw & (STOP_MASK & ~ST_TIME_REACHED)) h->keys_valid = false;  // stopped advances copied in place
-        if (stw & ST_CAPACITY) {
-            const uint64_t cap = std::min<uint64_t>(h->layout.total_blocks, h->capacity * 2);
-            if (cap <= h->capacity) {
-                rc = fail("sv_step_adaptive: grid block capacity exhausted");
-                break;
+        if (stw & (ST_CAPACITY | ST_MOVED_FAR)) {
+            if (stw & ST_CAPACITY) {
+                const uint64_t cap = std::min<uint64_t>(h->layout.total_blocks, h->capacity * 2);
+                if (cap <= h->capacity) {
+                    rc = fail("sv_step_adaptive: grid block capacity exhausted");
+                    break;
+                }
+                if (alloc_grid(h, cap) != cudaSuccess) {
+                    rc = fail("sv_step_adaptive: grid allocation failed");
+                    break;
+                }
+                clear_graphs(h);
             }
-            if (alloc_grid(h, cap) != cudaSuccess) {
-                rc = fail("sv_step_adaptive: grid allocation failed");
-                break;
-            }
-            clear_graphs(h);
-            h->host_counters[C_STATUS] &= ~ST_CAPACITY;
+            if (stw & ST_MOVED_FAR) h->sort_interval = std::max<uint32_t>(1, h->sort_interval / 2);
+            // Redo the stopped substep from its start, binned afresh, with the
+            // adaptive state it began with (its limits not yet in the history).
+            SV_CUDA(cudaMemcpyAsync(h->adt, h->adt_backup, sizeof(adaptive::State), cudaMemcpyDeviceToDevice,
+                                    h->stream));
+            h->since_sort = h->sort_interval;
+            h->host_counters[C_STATUS] &= ~(ST_CAPACITY | ST_MOVED_FAR);
             SV_CUDA(cudaMemcpyAsync(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice,
                                     h->stream));
             if (!(stw & ST_INVERTED)) continue;
         }
+        if (h->adaptive_interval) {
+            // as in sv_step: bin more often when many gathers miss their tile
+            const double miss = (double)(h->host_counters[C_FALLBACK] - fallback_before) /
+                                ((double)h->n * (h->host_counters[C_SUBSTEPS] - substeps_before) + 1.0);
+            if (miss > 0.02 && h->sort_interval > 1) h->sort_interval /= 2;
+            else if (miss < 0.002 && h->sort_interval < h->max_interval) h->sort_interval *= 2;
+        }
+        fallback_before = h->host_counters[C_FALLBACK];
+        substeps_before = h->host_counters[C_SUBSTEPS];
         if (stw & ST_INVERTED) {
             status |= SV_STATUS_PARTICLE_INVERTED;
             break;

@@ -215,6 +215,7 @@ struct sv_handle {
     // Adaptive time steps (adaptive::State in device memory, sv_adaptive.cuh);
     // adaptive_active while sv_step_adaptive runs.
     void *adt = nullptr;
+    void *adt_backup = nullptr;  // the state at the start of the running substep
     bool adaptive_active = false;
 
     // Simulation time of the completed state (the reference's CpuState::time),
@@ -282,6 +283,8 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 gravity, bool write_keys
 cudaError_t launch_limits_force(sv_handle *h);
 cudaError_t launch_g2p_only(sv_handle *h);
 cudaError_t launch_advance(sv_handle *h);
+// latches the stop bits and keeps the adaptive state for a redo
+cudaError_t launch_adaptive_begin(sv_handle *h);
 // frame input: interpolation at `time` (adaptive: the device time), the
 // gather + advance without the scatter of the next substep, clearing the
 // variant table the next scatter fills

@@ -1302,7 +1302,7 @@ StepArgs make_args(sv_handle *h, float dt, float3 g) {
     A.mats = h->materials;
     A.scenes = h->scenes;
     A.counters = h->counters;
-    A.perm = h->perm;
+    A.perm = h->need_perm ? h->perm : nullptr;  // the state is not yet in the last binning's order
     A.seg_start = h->seg_start;
     A.seg_block = h->seg_block;
     A.map_cur = h->blockmap[h->map_cur];
@@ -1406,6 +1406,7 @@ cudaError_t launch_sort_and_segments(sv_handle *h) {
         if (err != cudaSuccess) return err;
         h->launches += radix_sort_launches(h->n, h->layout.key_bits);
         h->sorts += 1;
+        h->need_perm = true;  // until a pass writes the state in the new order
     }
     Scoped s(h, "segments");
     uint32_t tiles = (uint32_t)((h->n + SEG_TILE - 1) / SEG_TILE);
@@ -1477,6 +1478,25 @@ cudaError_t launch_advance(sv_handle *h) {
     h->launches += 2;
     h->cur ^= 1;
     h->keys_valid = true;
+    h->need_perm = false;  // written in the binning's order
+    return cudaGetLastError();
+}
+
+// Start of an adaptive substep: latches the stop bits of the substeps before
+// it, then (unless stopped) keeps the adaptive state as it is now, to return
+// to if this substep is redone after a particle left its claimed blocks -- so
+// that the redo does not push its limits into the history twice.
+__global__ void k_adaptive_begin(const adaptive::State *st, adaptive::State *backup, uint32_t *counters) {
+    const uint32_t stop = counters[C_STATUS] & STOP_MASK;
+    counters[C_STOP] = stop;
+    if (!stop) *backup = *st;
+}
+
+cudaError_t launch_adaptive_begin(sv_handle *h) {
+    k_adaptive_begin<<<1, 1, 0, h->stream>>>(reinterpret_cast<const adaptive::State *>(h->adt),
+                                             reinterpret_cast<adaptive::State *>(h->adt_backup), h->counters);
+    h->launches += 1;
+    h->stop_latched = true;
     return cudaGetLastError();
 }
 
