@@ -526,11 +526,14 @@ def run_reference(args, rank, world):
 
     threads = os.cpu_count() or 1
     o = oracle.OracleState(scene.io_state.particles, scene.consts, scene.extras, fp64=False, threads=threads)
-    # each step is one substep of the full scene; the step count is bounded
-    # so the run stays within a few minutes
-    warm = min(args.warmup, 2)
-    steps = max(1, min(args.steps, 5))
+    # each step is one substep of the full scene: the requested warm-up and
+    # timed steps, unless they would take longer than about 150 s, in which
+    # case fewer timed steps are run (and reported)
+    warm = max(1, args.warmup)
+    t0 = time.perf_counter()
     o.step(warm, scene.dt, scene.gravity)
+    per_step = (time.perf_counter() - t0) / warm
+    steps = max(1, min(args.steps, int(150.0 / max(per_step, 1e-6))))
     t0 = time.perf_counter()
     o.step(steps, scene.dt, scene.gravity)
     el = time.perf_counter() - t0
