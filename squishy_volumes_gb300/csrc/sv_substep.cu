@@ -555,6 +555,7 @@ struct Shared {
     int4 gbase[PT];             // global base cell of REC_GLOBAL records
     int32_t slot_cur[27];
     int32_t slot_next[27];
+    int raised;                 // a thread of the CTA set a status bit (see cta_done)
 };
 
 // Tile node (tx, ty, tz) in [0, 8)^3 of block (bx, by, bz): global node
@@ -628,7 +629,7 @@ __device__ __forceinline__ void scatter_records(Shared &sh, int count, const Ste
                 atomicAdd(&A.grid_next[(uint64_t)slot * 64 + local],
                           make_float4(w * (p0.x + p1.x + p2.x), w * (p0.y + p1.y + p2.y), w * (p0.z + p1.z + p2.z), w * m));
             else
-                atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR);
+                atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR), sh.raised = 1;
         }
     }
     // records of particles with collider bits: their (node, bits) variants
@@ -645,7 +646,7 @@ __device__ __forceinline__ void scatter_records(Shared &sh, int count, const Ste
                 atomicAdd(&A.vnext.acc[s],
                           make_float4(w * (p0.x + p1.x + p2.x), w * (p0.y + p1.y + p2.y), w * (p0.z + p1.z + p2.z), w * m));
             else
-                atomicOr(&A.counters[C_STATUS], ST_VARIANT_FULL);
+                atomicOr(&A.counters[C_STATUS], ST_VARIANT_FULL), sh.raised = 1;
         }
     }
 }
@@ -750,11 +751,13 @@ static_assert(sizeof(Rec) * PT >= tc::NIN * PT * 2 + tc::NH * PT * 2, "closure o
 // End of a self-latching pass (one call per CTA, by all its threads): the
 // last CTA to finish latches the stop bits for the kernels that follow and
 // counts the substep unless the pass started stopped -- the work of k_latch
-// and k_finish without their launches.  Every status bit of the CTA is set
-// before the barrier; thread 0's fence then orders them before its ticket.
-__device__ __forceinline__ void cta_done(const StepArgs &A, uint32_t stop_at_start) {
+// and k_finish without their launches.  Threads that set a status bit fence
+// it (only when one did: `raised`), then thread 0's fence orders everything
+// before its ticket.
+__device__ __forceinline__ void cta_done(const StepArgs &A, uint32_t stop_at_start, const volatile int *raised) {
     if (!A.self_latch) return;
-    __threadfence();
+    __syncthreads();
+    if (raised && *raised) __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -792,9 +795,10 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
             for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x)
                 copy_particle(A.in, A.out, A.n, i, i, CELL);
         }
-        cta_done(A, stop_at_start);
+        cta_done(A, stop_at_start, nullptr);
         return;
     }
+    if (threadIdx.x == 0) sh.raised = 0;
     mlp::Phase ph;
     uint32_t n_learned = 0, n_closure_fb = 0;
     if constexpr (LEARNED) {
@@ -1044,7 +1048,7 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
                     } else if (!(J > 0.f)) {
                         // try_elastic_energy_neo_hookean: J <= 0 -> FAILED (advance_particles.rs:73-74)
                         packed |= SV_FAILED;
-                        atomicOr(&A.counters[C_STATUS], ST_INVERTED);
+                        atomicOr(&A.counters[C_STATUS], ST_INVERTED), sh.raised = 1;
                     } else if (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW) {
                         // mu |F - R|^2 + lambda/2 (J - 1)^2 = mu sum (s - 1)^2 + ...
                         const float d2 = (S[0] - 1.f) * (S[0] - 1.f) + (S[1] - 1.f) * (S[1] - 1.f) + (S[2] - 1.f) * (S[2] - 1.f);
@@ -1096,7 +1100,7 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
                     if (!(packed & SV_TOMBSTONED)) {
                         bool ok;
                         key = cell_key(nbase[0], nbase[1], nbase[2], A.L, ok);
-                        if (!ok) atomicOr(&A.counters[C_STATUS], ST_OUT_OF_GRID);
+                        if (!ok) atomicOr(&A.counters[C_STATUS], ST_OUT_OF_GRID), sh.raised = 1;
                     }
                     A.keys_out[i] = key;
                 }
@@ -1161,7 +1165,7 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
                     if (slot >= 0)
                         atomicAdd(&A.grid_next[(uint64_t)slot * 64 + tile_local(tx, ty, tz)], make_float4(px, py, pz, m));
                     else
-                        atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR);
+                        atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR), sh.raised = 1;
                 }
             }
         __syncthreads();
@@ -1195,7 +1199,7 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
         if (n_closure_fb) atomicAdd(&A.counters[C_CLOSURE_FB], n_closure_fb);
     }
     if constexpr (LEARNED) mlp::ctl_finish(shl.ctl, mlp::TMEM_COLS_INFER, &A.counters[C_CLOSURE_ERR]);
-    cta_done(A, 0u);
+    cta_done(A, 0u, &sh.raised);
 }
 
 __global__ void k_finish(uint32_t *counters) {

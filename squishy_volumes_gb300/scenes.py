@@ -270,10 +270,20 @@ def snow_sand_2m(seed: int = 6, box_dims=(100, 100, 100), dx: float = 1.0 / 512)
     return Scene("snow_sand_2m", IoState(0.0, p), consts, extras, dt=5e-5, substeps=1000)
 
 
+def dam_break_1m(seed: int = 3) -> Scene:
+    """dam_break_8m at one eighth of the particles (half the extent per axis
+    of the fluid column and the boxes; same dx, materials and time step): a
+    case of the same kernels small enough for a full profiler capture."""
+    s = dam_break_8m(seed, fluid_dims=(205, 183, 20), box_dims=(40, 40, 39))
+    s.name = "dam_break_1m"
+    return s
+
+
 SCENES = {
     "cube_64k": cube_64k,
     "three_boxes_1m": three_boxes_1m,
     "dam_break_8m": dam_break_8m,
+    "dam_break_1m": dam_break_1m,
     "small_mixed": small_mixed,
     "batched_64": batched_64,
     "snow_sand_2m": snow_sand_2m,
