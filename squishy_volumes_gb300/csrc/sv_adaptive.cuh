@@ -29,6 +29,9 @@ struct State {
     uint32_t red_max_v, red_max_c, red_live;
     uint32_t red_sound, red_iso;
     uint32_t substeps;
+    // red_sound / red_iso already hold the force limits of the current
+    // particle state: the last adaptive substep's advance reduced them
+    uint32_t force_ready;
 };
 
 // adaptive_time_step_state.rs:35-47

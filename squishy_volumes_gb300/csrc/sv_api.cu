@@ -731,6 +731,7 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
     if (!(dt > 0.f)) return fail("sv_step: dt must be positive");  // cpu_state.rs:170-172 ZeroTimeStep
     float3 g = gravity ? make_float3(gravity[0], gravity[1], gravity[2]) : make_float3(0.f, 0.f, 0.f);
     if (read_counters(h)) return -1;
+    h->force_limits_valid = false;  // fixed substeps (graph replays included) move the particles
     // A previous energy error does not carry over: the reference checks each
     // substep afresh (cpu_state.rs:178-183).
     if (h->host_counters[C_STATUS] & ST_INVERTED) {
@@ -856,7 +857,10 @@ int adaptive_substep(sv_handle *h, float3 g) {
         SV_CUDA(launch_interpolate(h, 0.0));  // at the device time of the substep
         SV_CUDA(launch_clear_variants(h, h->gcur));
     }
-    SV_CUDA(launch_limits_force(h));
+    // Later substeps of a call take the force limits that the advance before
+    // them reduced (a stopped substep stops all that follow it).
+    SV_CUDA(launch_limits_force(h, h->limits_pass_pending));
+    h->limits_pass_pending = false;
     SV_CUDA(launch_clear(h, h->gcur, h->map_cur));
     SV_CUDA(launch_p2g(h, 0.f, g));
     SV_CUDA(launch_grid_update(h, false));
@@ -891,7 +895,13 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
     st.max_dt = max_time_step;  // cpu_state.rs:162
     st.time = *time_inout;
     st.target = target_time;
-    st.red_sound = st.red_iso = 0x7f7fffffu;  // FLT_MAX bits
+    if (!h->force_limits_valid) {
+        // the particles changed since the last advance reduced the force
+        // limits: the first substep's k_limits_force reduces them
+        st.force_ready = 0;
+        st.red_sound = st.red_iso = 0x7f7fffffu;  // FLT_MAX bits
+    }
+    h->limits_pass_pending = true;
     SV_CUDA(cudaMemcpyAsync(h->adt, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
     if (read_counters(h)) return -1;
     h->host_counters[C_STATUS] &= ~(ST_INVERTED | ST_TIME_REACHED | ST_ZERO_DT);
@@ -952,6 +962,7 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
             // adaptive state it began with (its limits not yet in the history).
             SV_CUDA(cudaMemcpyAsync(h->adt, h->adt_backup, sizeof(adaptive::State), cudaMemcpyDeviceToDevice,
                                     h->stream));
+            h->limits_pass_pending = true;
             h->since_sort = h->sort_interval;
             h->host_counters[C_STATUS] &= ~(ST_CAPACITY | ST_MOVED_FAR);
             SV_CUDA(cudaMemcpyAsync(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice,
@@ -975,6 +986,7 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
     }
     h->adaptive_active = false;
     h->keys_valid = false;
+    h->force_limits_valid = rc == 0;
     if (rc) return -1;
     SV_CUDA(cudaMemcpyAsync(&st, h->adt, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
     SV_CUDA(cudaStreamSynchronize(h->stream));
@@ -1121,10 +1133,15 @@ int sv_sort_pairs(const uint32_t *keys, uint32_t *perm, uint64_t n) {
     uint32_t *dk = nullptr, *dko = nullptr, *dv = nullptr;
     void *temp = nullptr;
     size_t tb = radix_sort_temp_bytes(n);
+    // sort on the significant bits only: the passes follow the largest key
+    uint32_t any = 0;
+    for (uint64_t i = 0; i < n; ++i) any |= keys[i];
+    int key_bits = 1;  // all-zero keys still take one pass, which writes the identity
+    while (key_bits < 32 && (any >> key_bits) != 0) ++key_bits;
     cudaError_t e;
     if ((e = cudaMalloc(&dk, n * 4)) || (e = cudaMalloc(&dko, n * 4)) || (e = cudaMalloc(&dv, n * 4)) ||
         (e = cudaMalloc(&temp, tb)) || (e = cudaMemcpy(dk, keys, n * 4, cudaMemcpyHostToDevice)) ||
-        (e = radix_sort_pairs(dk, nullptr, dko, dv, n, 32, temp, 0)) ||
+        (e = radix_sort_pairs(dk, nullptr, dko, dv, n, key_bits, temp, 0)) ||
         (e = cudaMemcpy(perm, dv, n * 4, cudaMemcpyDeviceToHost))) {
         cudaFree(dk), cudaFree(dko), cudaFree(dv), cudaFree(temp);
         return fail(std::string("sv_sort_pairs: ") + cudaGetErrorString(e));

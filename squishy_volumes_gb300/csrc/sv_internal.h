@@ -217,6 +217,13 @@ struct sv_handle {
     void *adt = nullptr;
     void *adt_backup = nullptr;  // the state at the start of the running substep
     bool adaptive_active = false;
+    // the particle state is still the one the last sv_step_adaptive left, so
+    // the force limits its last advance reduced (adaptive::State::force_ready)
+    // still apply; any other pass that writes particles clears it
+    bool force_limits_valid = false;
+    // the next adaptive substep queues k_limits_force: the first of a call and
+    // the redo of a stopped one, whose state may predate any advance
+    bool limits_pass_pending = false;
 
     // Simulation time of the completed state (the reference's CpuState::time),
     // used to interpolate the frame input.
@@ -280,7 +287,9 @@ cudaError_t launch_grid_update(sv_handle *h, bool clear_next, bool latch = true)
 // substep itself (its last CTA), so no k_latch / k_finish launches follow.
 cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 gravity, bool write_keys, bool use_perm);
 // adaptive time steps (the unfused substep)
-cudaError_t launch_limits_force(sv_handle *h);
+// k_dt_force, after k_limits_force when `reduce` (the pass returns at once
+// when the last advance reduced the force limits already)
+cudaError_t launch_limits_force(sv_handle *h, bool reduce);
 cudaError_t launch_g2p_only(sv_handle *h);
 cudaError_t launch_advance(sv_handle *h);
 // latches the stop bits and keeps the adaptive state for a redo

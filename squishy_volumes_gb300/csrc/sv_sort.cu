@@ -1,7 +1,9 @@
 // sv_sort.cu -- stable LSD radix sort and exclusive scan, written for
-// sm_103a: 8-bit digits, per-tile histograms scanned digit-major, and a
-// stable scatter whose in-tile ranks come from __match_any_sync peer groups
-// processed row by row (so equal digits keep input order).
+// sm_103a: digits of up to 10 bits, split evenly over the fewest passes
+// (25-bit binning keys take three passes of 9, 8 and 8 bits, not four),
+// per-tile histograms scanned digit-major, and a stable scatter whose
+// in-tile ranks come from __match_any_sync peer groups processed row by row
+// (so equal digits keep input order).
 #include "sv_sort.cuh"
 
 #include <cstring>
@@ -19,7 +21,16 @@ constexpr int SORT_WARPS = 8;
 constexpr int SORT_THREADS = SORT_WARPS * 32;
 constexpr int SORT_ITEMS = 8;
 constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;
-constexpr int RADIX = 256;
+constexpr int MAX_DIGIT_BITS = 10;
+constexpr int MAX_RADIX = 1 << MAX_DIGIT_BITS;
+
+// Digit width of each pass for a key of `key_bits` bits: the fewest passes
+// of at most MAX_DIGIT_BITS bits, as even as possible.
+inline int sort_passes(int key_bits) { return (key_bits + MAX_DIGIT_BITS - 1) / MAX_DIGIT_BITS; }
+inline int pass_bits(int key_bits, int pass) {
+    const int passes = sort_passes(key_bits);
+    return key_bits / passes + (pass < key_bits % passes ? 1 : 0);
+}
 
 inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -98,6 +109,8 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 }
 
 // Per-tile digit histogram, stored digit-major: hist[d * tiles + tile].
+// RADIX is the shared table size, a power of two above `mask`.
+template <int RADIX>
 __global__ void __launch_bounds__(SORT_THREADS)
     k_radix_hist(const uint32_t *keys, uint64_t n, int shift, uint32_t mask, uint32_t *hist, uint32_t tiles) {
     __shared__ uint32_t h[RADIX];
@@ -116,6 +129,7 @@ __global__ void __launch_bounds__(SORT_THREADS)
 // Stable scatter (vals_in == nullptr means "value = element index").  Warp w owns elements [w*32*ITEMS, (w+1)*32*ITEMS) of the
 // tile; row j of lane l is element w*32*ITEMS + j*32 + l, so walking rows in
 // order and lanes in order visits the warp's elements in input order.
+template <int RADIX>
 __global__ void __launch_bounds__(SORT_THREADS)
     k_radix_scatter(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out, uint32_t *vals_out,
                     uint64_t n, int shift, uint32_t mask, const uint32_t *scanned, uint32_t tiles) {
@@ -208,16 +222,13 @@ int radix_sort_launches(uint64_t n, int key_bits) {
     if (key_bits > 32) key_bits = 32;
     uint64_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
     int total = 0;
-    for (int shift = 0; shift < key_bits; shift += 8) {
-        int bits = key_bits - shift < 8 ? key_bits - shift : 8;
-        total += 2 + scan_launches(((uint64_t)1 << bits) * tiles);
-    }
+    for (int p = 0; p < sort_passes(key_bits); ++p) total += 2 + scan_launches(((uint64_t)1 << pass_bits(key_bits, p)) * tiles);
     return total;
 }
 
 size_t radix_sort_temp_bytes(uint64_t n) {
     uint64_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
-    uint64_t hist = tiles * RADIX;
+    uint64_t hist = tiles * MAX_RADIX;
     return 2 * align_up(n * sizeof(uint32_t)) + 2 * align_up(hist * sizeof(uint32_t)) + scan_temp_bytes(hist);
 }
 
@@ -232,7 +243,7 @@ cudaError_t radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, u
     }
     if (key_bits > 32) key_bits = 32;
     uint32_t tiles = (uint32_t)((n + SORT_TILE - 1) / SORT_TILE);
-    uint64_t hist_n = (uint64_t)tiles * RADIX;
+    uint64_t hist_n = (uint64_t)tiles * MAX_RADIX;
     char *t = static_cast<char *>(temp);
     uint32_t *alt_keys = reinterpret_cast<uint32_t *>(t);
     t += align_up(n * 4);
@@ -244,22 +255,30 @@ cudaError_t radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, u
     t += align_up(hist_n * 4);
     void *scan_temp = t;
 
-    const int passes = (key_bits + 7) / 8;
+    const int passes = sort_passes(key_bits);
     const uint32_t *src_k = keys_in, *src_v = vals_in;
+    int shift = 0;
     for (int p = 0; p < passes; ++p) {
-        int shift = p * 8;
-        int bits = key_bits - shift < 8 ? key_bits - shift : 8;
+        const int bits = pass_bits(key_bits, p);
         uint32_t mask = (1u << bits) - 1u;
         bool to_out = ((passes - 1 - p) % 2) == 0;
         uint32_t *dk = to_out ? keys_out : alt_keys, *dv = to_out ? vals_out : alt_vals;
         uint64_t used = (uint64_t)(mask + 1) * tiles;
-        k_radix_hist<<<tiles, SORT_THREADS, 0, stream>>>(src_k, n, shift, mask, hist, tiles);
+        if (bits <= 8) k_radix_hist<256><<<tiles, SORT_THREADS, 0, stream>>>(src_k, n, shift, mask, hist, tiles);
+        else if (bits == 9) k_radix_hist<512><<<tiles, SORT_THREADS, 0, stream>>>(src_k, n, shift, mask, hist, tiles);
+        else k_radix_hist<MAX_RADIX><<<tiles, SORT_THREADS, 0, stream>>>(src_k, n, shift, mask, hist, tiles);
         cudaError_t err = exclusive_scan_u32(hist, scanned, used, scan_temp, stream);
         if (err != cudaSuccess) return err;
-        k_radix_scatter<<<tiles, SORT_THREADS, 0, stream>>>(src_k, src_v, dk, dv, n, shift, mask, scanned, tiles);
+        if (bits <= 8)
+            k_radix_scatter<256><<<tiles, SORT_THREADS, 0, stream>>>(src_k, src_v, dk, dv, n, shift, mask, scanned, tiles);
+        else if (bits == 9)
+            k_radix_scatter<512><<<tiles, SORT_THREADS, 0, stream>>>(src_k, src_v, dk, dv, n, shift, mask, scanned, tiles);
+        else
+            k_radix_scatter<MAX_RADIX><<<tiles, SORT_THREADS, 0, stream>>>(src_k, src_v, dk, dv, n, shift, mask, scanned, tiles);
         err = cudaGetLastError();
         if (err != cudaSuccess) return err;
         src_k = dk, src_v = dv;
+        shift += bits;
     }
     return cudaSuccess;
 }
@@ -288,8 +307,8 @@ constexpr size_t ce_scan_temp(uint64_t n) {
                                    : 256;
 }
 constexpr size_t ce_sort_temp(uint64_t n) {
-    return 2 * ce_align(n * 4) + 2 * ce_align(((n + SORT_TILE - 1) / SORT_TILE) * RADIX * 4) +
-           ce_scan_temp(((n + SORT_TILE - 1) / SORT_TILE) * RADIX);
+    return 2 * ce_align(n * 4) + 2 * ce_align(((n + SORT_TILE - 1) / SORT_TILE) * MAX_RADIX * 4) +
+           ce_scan_temp(((n + SORT_TILE - 1) / SORT_TILE) * MAX_RADIX);
 }
 // sorted keys, then the radix sort's temporary storage
 constexpr size_t NOALLOC_KEYS_BYTES = ce_align(NOALLOC_MAX_KEYS * 4);

@@ -817,6 +817,8 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
     if (A.adt) dt_force = A.adt->dt_a, dt_scatter = A.adt->dt_b, dt_adv = A.adt->dt_c;
     float red_v = 0.f, red_c = 0.f;  // G2P_ONLY: max |v| and max |C_ij| of live particles
     bool red_live = false;
+    // ADVANCE: the next substep's sound and isolated limits of the advanced state
+    float lim_sound = adaptive::NONE, lim_iso = adaptive::NONE;
     if (G2P) {
         // particles that were tombstoned at binning time are carried over
         for (uint64_t i = nlive + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -1076,6 +1078,30 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
                     }
                     if (!inside) packed |= SV_TOMBSTONED;
                     alive = !(packed & (SV_TOMBSTONED | SV_FAILED));
+                    if constexpr (MODE == MODE_ADVANCE) {
+                        // LimitTimeStepBeforeForce of the next substep
+                        // (limit_time_step.rs:25-178) over the state just
+                        // written: the singular values come from this pass's
+                        // SVD (after the plastic projection, which sets them);
+                        // Neo-Hookean solids took none and take one here.
+                        if (A.adt && !(packed & SV_TOMBSTONED)) {
+                            float s[3] = {S[0], S[1], S[2]};
+                            if (kind == KIND_NEO_HOOKEAN) {
+                                uint32_t none = 0;
+                                particle_svd(F, U, s, V, 0, none);
+                            }
+                            if (s[0] < s[1]) { const float t = s[0]; s[0] = s[1], s[1] = t; }
+                            if (s[1] < s[2]) { const float t = s[1]; s[1] = s[2], s[2] = t; }
+                            if (s[0] < s[1]) { const float t = s[0]; s[0] = s[1], s[1] = t; }
+                            const bool fluid = kind == KIND_FLUID;
+                            const float a = adaptive::sound_limit<float>(fluid, mat.mu, mat.lambda, mat.bulk_modulus,
+                                                                         mat.exponent, mat.mass, mat.initial_volume, s, dx);
+                            const float b = adaptive::isolated_limit<float>(fluid, mat.mu, mat.lambda, mat.bulk_modulus,
+                                                                            mat.exponent, mat.mass, mat.initial_volume, J, dx);
+                            if (a > 0.f && a < adaptive::NONE) lim_sound = fminf(lim_sound, a);
+                            if (b > 0.f && b < adaptive::NONE) lim_iso = fminf(lim_iso, b);
+                        }
+                    }
                     // write the advanced state in sorted order
                     pos.w = __uint_as_float(packed);
                     A.out.pos[i] = pos;
@@ -1183,6 +1209,19 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
             atomicOr(&A.adt->red_live, 1u);
         }
     }
+    if constexpr (MODE == MODE_ADVANCE) {
+        if (A.adt) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lim_sound = fminf(lim_sound, __shfl_xor_sync(0xffffffffu, lim_sound, o));
+                lim_iso = fminf(lim_iso, __shfl_xor_sync(0xffffffffu, lim_iso, o));
+            }
+            if ((threadIdx.x & 31) == 0) {
+                if (lim_sound < adaptive::NONE) atomicMin(&A.adt->red_sound, __float_as_uint(lim_sound));
+                if (lim_iso < adaptive::NONE) atomicMin(&A.adt->red_iso, __float_as_uint(lim_iso));
+            }
+        }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         fp64_count += __shfl_xor_sync(0xffffffffu, fp64_count, o);
@@ -1213,7 +1252,8 @@ __global__ void k_finish(uint32_t *counters) {
 __global__ void __launch_bounds__(ELEM_THREADS)
     k_limits_force(ParticleArrays s, const Material *mats, uint64_t n, float dx, adaptive::State *st,
                    const uint32_t *counters) {
-    if (stopped(counters)) return;
+    // the last substep's advance reduced them over the same state already
+    if (stopped(counters) || st->force_ready) return;
     float ls = adaptive::NONE, li = adaptive::NONE;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t packed = __float_as_uint(s.pos[i].w);
@@ -1271,6 +1311,7 @@ __global__ void k_dt_integrate(adaptive::State *st, uint32_t *counters, float dx
     adaptive::push(*st);
     st->dt_c = adaptive::allowed(*st);
     st->red_sound = __float_as_uint(adaptive::NONE), st->red_iso = __float_as_uint(adaptive::NONE);
+    st->force_ready = 0;  // the advance that follows reduces them afresh
     if (!(st->dt_c > 0.f)) counters[C_STATUS] |= ST_ZERO_DT;
 }
 
@@ -1278,6 +1319,7 @@ __global__ void k_dt_integrate(adaptive::State *st, uint32_t *counters, float dx
 // run stops (ST_TIME_REACHED latches) once the target time is reached.
 __global__ void k_adaptive_finish(adaptive::State *st, uint32_t *counters) {
     if (counters[C_STOP] || (counters[C_STATUS] & STOP_MASK)) return;
+    st->force_ready = 1;  // the advance completed its reduction of the next force limits
     st->time += (double)st->dt_c;
     st->substeps += 1;
     counters[C_SUBSTEPS] += 1;
@@ -1359,6 +1401,7 @@ unsigned particle_blocks(const sv_handle *h) { return (unsigned)sm_count() * (h-
 template <int MODE> void launch_particles(sv_handle *h, const StepArgs &A) {
     const unsigned blocks = particle_blocks(h);
     h->stop_latched = A.self_latch;
+    if (MODE != MODE_ADVANCE && MODE != MODE_P2G && MODE != MODE_G2P_ONLY) h->force_limits_valid = false;
     if constexpr (MODE != MODE_G2P2G_LEARNED) {
         if (h->fin_active) {
             if (h->layout.position_form) k_particles<true, MODE, true><<<blocks, PT, 0, h->stream>>>(A);
@@ -1450,13 +1493,16 @@ cudaError_t launch_clear(sv_handle *h, int grid_side, int which) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_limits_force(sv_handle *h) {
+cudaError_t launch_limits_force(sv_handle *h, bool reduce) {
     Scoped s(h, "limits_force");
     auto *st = reinterpret_cast<adaptive::State *>(h->adt);
-    k_limits_force<<<elem_blocks(h->n), ELEM_THREADS, 0, h->stream>>>(h->side[h->cur], h->materials, h->n,
-                                                                       h->layout.dx, st, h->counters);
+    if (reduce) {
+        k_limits_force<<<elem_blocks(h->n), ELEM_THREADS, 0, h->stream>>>(h->side[h->cur], h->materials, h->n,
+                                                                           h->layout.dx, st, h->counters);
+        h->launches += 1;
+    }
     k_dt_force<<<1, 1, 0, h->stream>>>(st, h->counters);
-    h->launches += 2;
+    h->launches += 1;
     return cudaGetLastError();
 }
 
@@ -1490,14 +1536,18 @@ cudaError_t launch_advance(sv_handle *h) {
 // it, then (unless stopped) keeps the adaptive state as it is now, to return
 // to if this substep is redone after a particle left its claimed blocks -- so
 // that the redo does not push its limits into the history twice.
-__global__ void k_adaptive_begin(const adaptive::State *st, adaptive::State *backup, uint32_t *counters) {
+__global__ void k_adaptive_begin(adaptive::State *st, adaptive::State *backup, uint32_t *counters) {
     const uint32_t stop = counters[C_STATUS] & STOP_MASK;
     counters[C_STOP] = stop;
-    if (!stop) *backup = *st;
+    if (stop) return;
+    *backup = *st;
+    // k_limits_force reduces this substep's force limits unless the last
+    // advance did
+    if (!st->force_ready) st->red_sound = st->red_iso = __float_as_uint(adaptive::NONE);
 }
 
 cudaError_t launch_adaptive_begin(sv_handle *h) {
-    k_adaptive_begin<<<1, 1, 0, h->stream>>>(reinterpret_cast<const adaptive::State *>(h->adt),
+    k_adaptive_begin<<<1, 1, 0, h->stream>>>(reinterpret_cast<adaptive::State *>(h->adt),
                                              reinterpret_cast<adaptive::State *>(h->adt_backup), h->counters);
     h->launches += 1;
     h->stop_latched = true;

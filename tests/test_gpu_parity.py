@@ -70,6 +70,23 @@ def test_sort_pairs_is_stable_sort(cuda_lib, n):
     np.testing.assert_array_equal(perm, np.argsort(keys, kind="stable").astype(np.uint32))
 
 
+@pytest.mark.parametrize("key_bits", [1, 9, 10, 17, 20, 25, 28, 30])
+def test_sort_pairs_digit_widths(cuda_lib, key_bits):
+    # the passes split the significant bits evenly into digits of at most
+    # 10 bits: 25 bits sort as 9 + 8 + 8, 28 as 10 + 9 + 9, 17 as 9 + 8
+    rng = np.random.default_rng(key_bits)
+    keys = rng.integers(0, 2**key_bits, 150_000, dtype=np.uint64).astype(np.uint32)
+    keys[::5] = keys[::5] >> (key_bits // 2)  # duplicates and short keys
+    keys[3] = 2**key_bits - 1
+    perm = sort_pairs(keys)
+    np.testing.assert_array_equal(perm, np.argsort(keys, kind="stable").astype(np.uint32))
+
+
+def test_sort_pairs_all_zero_keys(cuda_lib):
+    perm = sort_pairs(np.zeros(5000, np.uint32))
+    np.testing.assert_array_equal(perm, np.arange(5000, dtype=np.uint32))
+
+
 def test_sort_pairs_full_32_bit_keys(cuda_lib):
     rng = np.random.default_rng(42)
     keys = rng.integers(0, 2**32, 300_000, dtype=np.uint64).astype(np.uint32)
