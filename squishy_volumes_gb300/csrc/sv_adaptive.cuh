@@ -32,6 +32,10 @@ struct State {
     // red_sound / red_iso already hold the force limits of the current
     // particle state: the last adaptive substep's advance reduced them
     uint32_t force_ready;
+    // the advance's step when the G2P's velocity and deformation limits do
+    // not bind, and whether they did (the speculative advance is redone)
+    float dt_spec;
+    uint32_t redo;
 };
 
 // adaptive_time_step_state.rs:35-47
@@ -44,6 +48,16 @@ __host__ __device__ inline float allowed(const State &s) {
     for (int k = 0; k < s.hist_len; ++k) a = fminf(a, s.hist[k]);
     return a;
 }
+// allowed() right after the push of LimitTimeStepBeforeIntegrate, less the
+// two limits that push brings (velocity and deformation): the push drops the
+// oldest prior once the history is full, and the minimum over the rest does
+// not depend on the new limits.  So that step is min(this, vel, def).
+__host__ __device__ inline float step_without_g2p_limits(const State &s) {
+    float d = fminf(fminf(s.max_dt, s.sound), s.iso);
+    for (int k = s.hist_len > HISTORY - 1 ? 1 : 0; k < s.hist_len; ++k) d = fminf(d, s.hist[k]);
+    return d;
+}
+
 // adaptive_time_step_state.rs:56-63
 __host__ __device__ inline void push(State &s) {
     const float cur = without_prior(s);

@@ -864,8 +864,15 @@ int adaptive_substep(sv_handle *h, float3 g) {
     SV_CUDA(launch_clear(h, h->gcur, h->map_cur));
     SV_CUDA(launch_p2g(h, 0.f, g));
     SV_CUDA(launch_grid_update(h, false));
-    SV_CUDA(launch_g2p_only(h));
-    SV_CUDA(launch_advance(h));
+    if (h->fin_active) {
+        SV_CUDA(launch_g2p_only(h));
+        SV_CUDA(launch_advance(h));
+    } else {
+        // The velocity and deformation limits of the G2P rarely bind: the
+        // advance goes ahead at the step that holds unless they do and is
+        // redone from the same input, at the step they allow, when they do.
+        SV_CUDA(launch_g2p_advance_adaptive(h));
+    }
     h->since_sort += 1;
     return 0;
 }

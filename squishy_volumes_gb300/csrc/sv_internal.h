@@ -292,6 +292,9 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 gravity, bool write_keys
 cudaError_t launch_limits_force(sv_handle *h, bool reduce);
 cudaError_t launch_g2p_only(sv_handle *h);
 cudaError_t launch_advance(sv_handle *h);
+// G2P and the advance of an adaptive substep in one pass at the step the
+// advance takes unless the G2P's own limits bind, redone when they do
+cudaError_t launch_g2p_advance_adaptive(sv_handle *h);
 // latches the stop bits and keeps the adaptive state for a redo
 cudaError_t launch_adaptive_begin(sv_handle *h);
 // frame input: interpolation at `time` (adaptive: the device time), the

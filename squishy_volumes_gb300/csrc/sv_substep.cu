@@ -90,6 +90,9 @@ struct StepArgs {
     col::FrameArgs fa;                   // frame input (kernels instantiated with FIN only)
     col::VariantTable vcur, vnext;       // collider variants gathered from / scattered into
     bool self_latch;                     // the last CTA latches the stop bits and counts the substep
+    // adaptive G2P_ADVANCE: 1 = the pass at the speculative step dt_spec,
+    // reducing the G2P's limits; 2 = its redo at dt_c, only when flagged
+    uint32_t adt_pass;
     uint64_t n;
     GridLayout L;
     float dt;
@@ -788,6 +791,7 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
     constexpr bool LOAD_VC = MODE == MODE_P2G || MODE == MODE_ADVANCE;  // v and C from the state
     __shared__ Shared sh;
     __shared__ typename std::conditional<LEARNED, SharedLearned, int>::type shl;
+    if (MODE == MODE_G2P_ADVANCE && A.adt_pass == 2 && !*(volatile const uint32_t *)&A.adt->redo) return;
     const uint32_t stop_at_start = stopped(A.counters);
     if (stop_at_start) {
         if (G2P) {
@@ -814,10 +818,15 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
     // time steps of the external force, the scatter and the advance: one dt,
     // or the three of the adaptive state's phases
     float dt_force = A.dt, dt_scatter = A.dt, dt_adv = A.dt;
-    if (A.adt) dt_force = A.adt->dt_a, dt_scatter = A.adt->dt_b, dt_adv = A.adt->dt_c;
-    float red_v = 0.f, red_c = 0.f;  // G2P_ONLY: max |v| and max |C_ij| of live particles
+    if (A.adt) dt_force = A.adt->dt_a, dt_scatter = A.adt->dt_b, dt_adv = A.adt_pass == 1 ? A.adt->dt_spec : A.adt->dt_c;
+    // G2P_ONLY and the speculative G2P_ADVANCE: max |v| and max |C_ij| of live particles
+    constexpr bool G2P_LIMITS_MODE = MODE == MODE_G2P_ONLY || MODE == MODE_G2P_ADVANCE;
+    const bool g2p_limits = MODE == MODE_G2P_ONLY || (MODE == MODE_G2P_ADVANCE && A.adt_pass == 1);
+    float red_v = 0.f, red_c = 0.f;
     bool red_live = false;
-    // ADVANCE: the next substep's sound and isolated limits of the advanced state
+    // ADVANCE, adaptive G2P_ADVANCE: the next substep's sound and isolated
+    // limits of the advanced state
+    constexpr bool FORCE_LIMITS_MODE = MODE == MODE_ADVANCE || MODE == MODE_G2P_ADVANCE;
     float lim_sound = adaptive::NONE, lim_iso = adaptive::NONE;
     if (G2P) {
         // particles that were tombstoned at binning time are carried over
@@ -916,14 +925,18 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
                         for (int k = 0; k < 9; ++k) C.a[k] *= cscale;
                     }
                     if constexpr (MODE == MODE_G2P_ONLY) {
-                        // v and C back into the state, in place; the limits of
-                        // limit_time_step.rs:189-222 reduce over them
+                        // v and C back into the state, in place
                         A.in.vel[p] = make_float4(v[0], v[1], v[2], plastic_j);
                         store_mat9(A.in.C, A.n, p, C);
-                        red_v = fmaxf(red_v, sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+                    }
+                    if constexpr (G2P_LIMITS_MODE) {
+                        // the limits of limit_time_step.rs:189-222 reduce over v and C
+                        if (g2p_limits) {
+                            red_v = fmaxf(red_v, sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
 #pragma unroll
-                        for (int k = 0; k < 9; ++k) red_c = fmaxf(red_c, fabsf(C.a[k]));
-                        red_live = true;
+                            for (int k = 0; k < 9; ++k) red_c = fmaxf(red_c, fabsf(C.a[k]));
+                            red_live = true;
+                        }
                     }
                     if (G2P) {
                         // ---- advance (advance_particles.rs:39-41): x += v dt, F += C F dt
@@ -1078,7 +1091,7 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
                     }
                     if (!inside) packed |= SV_TOMBSTONED;
                     alive = !(packed & (SV_TOMBSTONED | SV_FAILED));
-                    if constexpr (MODE == MODE_ADVANCE) {
+                    if constexpr (FORCE_LIMITS_MODE) {
                         // LimitTimeStepBeforeForce of the next substep
                         // (limit_time_step.rs:25-178) over the state just
                         // written: the singular values come from this pass's
@@ -1196,7 +1209,7 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
             }
         __syncthreads();
     }
-    if constexpr (MODE == MODE_G2P_ONLY) {
+    if (G2P_LIMITS_MODE && g2p_limits) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             red_v = fmaxf(red_v, __shfl_xor_sync(0xffffffffu, red_v, o));
@@ -1209,7 +1222,7 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
             atomicOr(&A.adt->red_live, 1u);
         }
     }
-    if constexpr (MODE == MODE_ADVANCE) {
+    if constexpr (FORCE_LIMITS_MODE) {
         if (A.adt) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -1298,6 +1311,11 @@ __global__ void k_dt_force(adaptive::State *st, uint32_t *counters) {
     adaptive::push(*st);
     st->dt_b = adaptive::allowed(*st);
     st->red_max_v = 0u, st->red_max_c = 0u, st->red_live = 0u;
+    // consumed: the advance of this substep reduces the next ones
+    st->red_sound = __float_as_uint(adaptive::NONE), st->red_iso = __float_as_uint(adaptive::NONE);
+    st->force_ready = 0;
+    st->dt_spec = adaptive::step_without_g2p_limits(*st);
+    st->redo = 0;
     if (!(st->dt_a > 0.f) || !(st->dt_b > 0.f)) counters[C_STATUS] |= ST_ZERO_DT;
 }
 
@@ -1310,8 +1328,10 @@ __global__ void k_dt_integrate(adaptive::State *st, uint32_t *counters, float dx
     st->def = st->red_live ? 0.2f / fmaxf(mc, 1e-8f) : adaptive::NONE;
     adaptive::push(*st);
     st->dt_c = adaptive::allowed(*st);
-    st->red_sound = __float_as_uint(adaptive::NONE), st->red_iso = __float_as_uint(adaptive::NONE);
-    st->force_ready = 0;  // the advance that follows reduces them afresh
+    // a speculative advance at dt_spec (adaptive G2P_ADVANCE) is redone when
+    // the G2P's limits bind; the redo reduces the force limits again
+    st->redo = st->dt_c != st->dt_spec;
+    if (st->redo) st->red_sound = st->red_iso = __float_as_uint(adaptive::NONE);
     if (!(st->dt_c > 0.f)) counters[C_STATUS] |= ST_ZERO_DT;
 }
 
@@ -1356,6 +1376,7 @@ StepArgs make_args(sv_handle *h, float dt, float3 g) {
     A.grid_cur = h->grid[h->gcur];
     A.grid_next = h->grid[h->gcur ^ 1];
     A.self_latch = false;
+    A.adt_pass = 0;
     A.keys_out = h->keys;
     A.closure_img = nullptr;
     A.closure_hull = nullptr;
@@ -1398,8 +1419,8 @@ unsigned particle_blocks(const sv_handle *h) { return (unsigned)sm_count() * (h-
 
 // Launches the particle kernel of MODE in the handle's position form, with
 // the frame-input variant when one is loaded.
-template <int MODE> void launch_particles(sv_handle *h, const StepArgs &A) {
-    const unsigned blocks = particle_blocks(h);
+template <int MODE> void launch_particles(sv_handle *h, const StepArgs &A, unsigned grid = 0) {
+    const unsigned blocks = grid ? grid : particle_blocks(h);
     h->stop_latched = A.self_latch;
     if (MODE != MODE_ADVANCE && MODE != MODE_P2G && MODE != MODE_G2P_ONLY) h->force_limits_valid = false;
     if constexpr (MODE != MODE_G2P2G_LEARNED) {
@@ -1409,10 +1430,8 @@ template <int MODE> void launch_particles(sv_handle *h, const StepArgs &A) {
             return;
         }
     }
-    if constexpr (MODE != MODE_G2P_ADVANCE) {
-        if (h->layout.position_form) k_particles<true, MODE><<<blocks, PT, 0, h->stream>>>(A);
-        else k_particles<false, MODE><<<blocks, PT, 0, h->stream>>>(A);
-    }
+    if (h->layout.position_form) k_particles<true, MODE><<<blocks, PT, 0, h->stream>>>(A);
+    else k_particles<false, MODE><<<blocks, PT, 0, h->stream>>>(A);
 }
 
 }  // namespace
@@ -1519,6 +1538,31 @@ cudaError_t launch_g2p_only(sv_handle *h) {
     return cudaGetLastError();
 }
 
+cudaError_t launch_g2p_advance_adaptive(sv_handle *h) {
+    StepArgs A = make_args(h, 0.f, make_float3(0.f, 0.f, 0.f));
+    A.adt = reinterpret_cast<adaptive::State *>(h->adt);
+    {
+        Scoped s(h, "g2p_advance");
+        A.adt_pass = 1;
+        launch_particles<MODE_G2P_ADVANCE>(h, A);
+        k_dt_integrate<<<1, 1, 0, h->stream>>>(A.adt, h->counters, h->layout.dx);
+    }
+    {
+        // one resident wave: it returns at once unless the step was wrong
+        Scoped s(h, "advance_redo");
+        A.adt_pass = 2;
+        launch_particles<MODE_G2P_ADVANCE>(h, A, (unsigned)sm_count() * 5);
+        k_adaptive_finish<<<1, 1, 0, h->stream>>>(A.adt, h->counters);
+    }
+    h->launches += 4;
+    h->vel_side = h->gcur;
+    h->vel_map = h->map_cur;
+    h->cur ^= 1;
+    h->keys_valid = true;
+    h->need_perm = false;  // written in the binning's order
+    return cudaGetLastError();
+}
+
 cudaError_t launch_advance(sv_handle *h) {
     StepArgs A = make_args(h, 0.f, make_float3(0.f, 0.f, 0.f));
     A.adt = reinterpret_cast<adaptive::State *>(h->adt);
@@ -1539,6 +1583,7 @@ cudaError_t launch_advance(sv_handle *h) {
 __global__ void k_adaptive_begin(adaptive::State *st, adaptive::State *backup, uint32_t *counters) {
     const uint32_t stop = counters[C_STATUS] & STOP_MASK;
     counters[C_STOP] = stop;
+    st->redo = 0;
     if (stop) return;
     *backup = *st;
     // k_limits_force reduces this substep's force limits unless the last
