@@ -166,6 +166,7 @@ struct sv_handle {
     // arrays (sv_transfer.cu), where the device can; else staged copies.
     bool direct_host = false;
     uint32_t *inv = nullptr;  // [n] slot of each original particle (direct download)
+    void *arena = nullptr;    // the one allocation the fixed-size device buffers are carved from
     // C_STOP will hold the stop bits of every kernel queued so far (the last
     // status-setting launch was a latch or a self-latching particle pass)
     bool stop_latched = false;

@@ -285,14 +285,6 @@ int download_direct(sv_handle *h, sv_particles *o) {
     const uint64_t n = h->n;
     if (n == 0) return 0;
     cudaError_t e;
-    if (!h->inv) {
-        if ((e = cudaMalloc((void **)&h->inv, n * 4)) != cudaSuccess) {
-            h->inv = nullptr;
-            set_last_error(std::string("sv_download: ") + cudaGetErrorString(e));
-            return -1;
-        }
-        h->device_bytes += n * 4;
-    }
     uint32_t *bad = h->counters + C_TRANSFER_BAD;  // an original index out of range or repeated
     DownloadArgs d;
     d.a = h->side[h->cur], d.inv = h->inv, d.mats = h->materials, d.scenes = h->scenes;
