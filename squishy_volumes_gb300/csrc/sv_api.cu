@@ -96,6 +96,22 @@ struct MaterialHash {
 
 int build_material(const sv_particles *p, uint64_t i, Material &m, std::string &err);
 
+// Particle i > 0 of a scene has the same flags and parameter words as
+// particle i - 1, so it has the same material and passes the same checks.
+// Bodies are made of runs of identical parameters, and this comparison
+// costs a fraction of build_material.
+bool same_as_previous(const sv_particles *p, uint64_t i) {
+    auto eq = [i](const void *a) {
+        if (!a) return true;
+        const uint32_t *w = static_cast<const uint32_t *>(a);
+        return w[i] == w[i - 1];
+    };
+    return p->flags[i] == p->flags[i - 1] && eq(p->mass) && eq(p->initial_volume) && eq(p->model) &&
+           eq(p->mu) && eq(p->lambda) && eq(p->sand_alpha) && eq(p->exponent) && eq(p->bulk_modulus) &&
+           eq(p->viscosity_dynamic) && eq(p->viscosity_bulk) && eq(p->hardening) && eq(p->crit_compression) &&
+           eq(p->crit_stretch);
+}
+
 // The host pass of sv_create over host threads: per particle its material
 // (deduplicated ParticleParameters, numbered in order of first appearance
 // like a sequential pass) and the bounds of the live particles of each
@@ -139,13 +155,6 @@ void prepass(const sv_particles *ps, uint32_t n_scenes, const std::vector<uint64
             while (g >= first[s + 1]) ++s;
             const sv_particles *p = &ps[s];
             const uint64_t i = g - first[s];
-            Material m;
-            std::string err;
-            if (build_material(p, i, m, err)) {
-                pt.err_at = g, pt.err = err;
-                return;
-            }
-            m.scene = s;
             if (p->collider_bits && p->collider_bits[i]) pt.any_bits = true;
             if (!(p->flags[i] & SV_TOMBSTONED)) {
                 for (int a = 0; a < 3; ++a) {
@@ -154,6 +163,18 @@ void prepass(const sv_particles *ps, uint32_t n_scenes, const std::vector<uint64
                     pt.lo[s][a] = std::min(pt.lo[s][a], x), pt.hi[s][a] = std::max(pt.hi[s][a], x);
                 }
             }
+            // the previous particle (same scene, this part) had the material prev_idx
+            if (prev_idx != UINT32_MAX && i > 0 && g > g0 && g - 1 >= first[s] && same_as_previous(p, i)) {
+                out.mat_index[g] = prev_idx;
+                continue;
+            }
+            Material m;
+            std::string err;
+            if (build_material(p, i, m, err)) {
+                pt.err_at = g, pt.err = err;
+                return;
+            }
+            m.scene = s;
             if (prev_idx != UINT32_MAX && std::memcmp(&m, &prev, sizeof(m)) == 0) {
                 out.mat_index[g] = prev_idx;
                 continue;
@@ -200,12 +221,19 @@ void prepass(const sv_particles *ps, uint32_t n_scenes, const std::vector<uint64
             pt.remap[k] = it->second;
         }
     }
-    run([&](unsigned t) {
-        uint64_t g0, g1;
-        range(t, g0, g1);
-        const std::vector<uint32_t> &r = parts[t].remap;
-        for (uint64_t g = g0; g < g1; ++g) out.mat_index[g] = r[out.mat_index[g]];
-    });
+    bool identity = true;  // every part found its materials in the global order
+    for (const Part &pt : parts)
+        for (size_t k = 0; k < pt.remap.size(); ++k) identity &= pt.remap[k] == k;
+    if (!identity)
+        run([&](unsigned t) {
+            uint64_t g0, g1;
+            range(t, g0, g1);
+            const std::vector<uint32_t> &r = parts[t].remap;
+            bool same = true;
+            for (size_t k = 0; k < r.size(); ++k) same &= r[k] == k;
+            if (same) return;
+            for (uint64_t g = g0; g < g1; ++g) out.mat_index[g] = r[out.mat_index[g]];
+        });
     if (out.mats.empty()) out.mats.push_back(Material{});
     out.lo.assign(n_scenes, {INFINITY, INFINITY, INFINITY});
     out.hi.assign(n_scenes, {-INFINITY, -INFINITY, -INFINITY});

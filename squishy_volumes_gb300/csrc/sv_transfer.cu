@@ -29,9 +29,17 @@ namespace {
 
 constexpr int TPB = 256;
 
+// The caller's arrays of one scene, copied to device memory once per
+// upload so that no thread chases pointers through host memory.
+struct UploadScene {
+    const uint32_t *flags;
+    const float *positions, *velocities, *position_gradients, *velocity_gradients;
+    const float *elastic_energies, *plastic_j;  // may be NULL
+    uint64_t first;                              // first particle of the scene
+};
+
 struct UploadArgs {
-    const sv_particles *ps;      // host: one per scene
-    const uint64_t *first;       // host: first particle of each scene, n_scenes + 1
+    const UploadScene *sc;       // device: one per scene, plus a sentinel whose first is n
     uint32_t n_scenes;
     const uint32_t *mat_index;   // host: material of each particle
     const SceneInfo *scenes;     // device
@@ -40,25 +48,23 @@ struct UploadArgs {
     double dx;
 };
 
-__device__ __forceinline__ uint32_t scene_of(const uint64_t *first, uint32_t n_scenes, uint64_t i) {
-    uint32_t lo = 0, hi = n_scenes;  // first[lo] <= i < first[hi]
+__device__ __forceinline__ uint32_t scene_of(const UploadScene *sc, uint32_t n_scenes, uint64_t i) {
+    uint32_t lo = 0, hi = n_scenes;  // sc[lo].first <= i < sc[hi].first
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) / 2;
-        if (first[mid] <= i) lo = mid;
+        if (sc[mid].first <= i) lo = mid;
         else hi = mid;
     }
     return lo;
 }
 
-// One particle of the upload, its position, velocity and matrix rows already
-// in shared memory.
+// One particle of the upload: its position, velocity and matrix rows already
+// in shared memory, its per-particle scalars in registers.
 template <bool CELL>
-__device__ __forceinline__ void upload_one(const UploadArgs &u, uint64_t i, const float *rx, const float *rv,
+__device__ __forceinline__ void upload_one(const UploadArgs &u, uint64_t i, uint32_t sc, uint32_t flags, uint32_t mi,
+                                           float plastic_j, float energy, const float *rx, const float *rv,
                                            const float *rF, const float *rC) {
-    const uint32_t sc = scene_of(u.first, u.n_scenes, i);
-    const sv_particles &p = u.ps[sc];
-    const uint64_t li = i - u.first[sc];
-    const uint32_t packed = (p.flags[li] & FLAG_MASK) | (u.mat_index[i] << MATERIAL_SHIFT);
+    const uint32_t packed = (flags & FLAG_MASK) | (mi << MATERIAL_SHIFT);
     const float x = rx[0], y = rx[1], z = rx[2];
     float4 pos;
     if (!CELL) {
@@ -79,22 +85,38 @@ __device__ __forceinline__ void upload_one(const UploadArgs &u, uint64_t i, cons
     }
     pos.w = __uint_as_float(packed);
     u.a.pos[i] = pos;
-    u.a.vel[i] = make_float4(rv[0], rv[1], rv[2], p.plastic_j ? p.plastic_j[li] : 1.f);
+    u.a.vel[i] = make_float4(rv[0], rv[1], rv[2], plastic_j);
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         u.a.C[(uint64_t)k * u.n + i] = rC[k];
         u.a.F[(uint64_t)k * u.n + i] = rF[k];
     }
-    u.a.energy[i] = p.elastic_energies ? p.elastic_energies[li] : 0.f;
+    u.a.energy[i] = energy;
     u.a.orig[i] = (uint32_t)i;
 }
 
-// Loads a tile's rows of `width` floats (src rows li0 ...) into shared memory
-// with consecutive threads on consecutive words.
-__device__ __forceinline__ void load_rows(float *stage, const float *src, uint64_t li0, int count, int width) {
-    const float *in = src + li0 * width;
-    for (int e = threadIdx.x; e < count * width; e += TPB) stage[e] = in[e];
-}
+// Rows of W floats of a tile (src rows li0 ...): element e = threadIdx.x +
+// k * TPB of the tile's count * W words, consecutive threads on consecutive
+// words.  All loads of a tile are issued before any store to shared memory,
+// so each thread has them in flight together across the host link.
+template <int W> struct Rows {
+    float r[W];
+    __device__ __forceinline__ void load(const float *src, uint64_t li0, int count) {
+        const float *in = src + li0 * W;
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+            const int e = threadIdx.x + k * TPB;
+            r[k] = e < count * W ? in[e] : 0.f;
+        }
+    }
+    __device__ __forceinline__ void store(float *stage, int count) const {
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+            const int e = threadIdx.x + k * TPB;
+            if (e < count * W) stage[e] = r[k];
+        }
+    }
+};
 
 // The staged upload's per-particle conversion (sv_api.cu create_impl),
 // reading the caller's arrays directly: over tiles of TPB particles, whose
@@ -104,19 +126,28 @@ template <bool CELL> __global__ void __launch_bounds__(TPB) k_upload(UploadArgs 
     for (uint64_t i0 = (uint64_t)blockIdx.x * TPB; i0 < u.n; i0 += (uint64_t)gridDim.x * TPB) {
         const int count = (int)(u.n - i0 < (uint64_t)TPB ? u.n - i0 : (uint64_t)TPB);
         const int t = threadIdx.x;
-        const uint32_t s0 = scene_of(u.first, u.n_scenes, i0), s1 = scene_of(u.first, u.n_scenes, i0 + count - 1);
+        const uint64_t i = i0 + t;
+        const uint32_t s0 = scene_of(u.sc, u.n_scenes, i0), s1 = scene_of(u.sc, u.n_scenes, i0 + count - 1);
+        // this thread's particle: its scene and scalars
+        const uint32_t sc = s0 == s1 ? s0 : (t < count ? scene_of(u.sc, u.n_scenes, i) : s0);
+        const UploadScene p = u.sc[sc];
+        const uint64_t li = i - p.first;
+        uint32_t flags = 0, mi = 0;
+        float pj = 1.f, en = 0.f;
+        if (t < count) {
+            flags = p.flags[li], mi = u.mat_index[i];
+            if (p.plastic_j) pj = p.plastic_j[li];
+            if (p.elastic_energies) en = p.elastic_energies[li];
+        }
         if (s0 == s1) {
-            const sv_particles &p = u.ps[s0];
-            const uint64_t li0 = i0 - u.first[s0];
-            load_rows(sx, p.positions, li0, count, 3);
-            load_rows(sv, p.velocities, li0, count, 3);
-            load_rows(sF, p.position_gradients, li0, count, 9);
-            load_rows(sC, p.velocity_gradients, li0, count, 9);
+            const uint64_t li0 = i0 - p.first;
+            Rows<3> x, v;
+            Rows<9> F, C;
+            x.load(p.positions, li0, count), v.load(p.velocities, li0, count);
+            F.load(p.position_gradients, li0, count), C.load(p.velocity_gradients, li0, count);
+            x.store(sx, count), v.store(sv, count), F.store(sF, count), C.store(sC, count);
         } else if (t < count) {
             // a tile across scenes: each thread its own rows
-            const uint32_t sc = scene_of(u.first, u.n_scenes, i0 + t);
-            const sv_particles &p = u.ps[sc];
-            const uint64_t li = i0 + t - u.first[sc];
 #pragma unroll
             for (int k = 0; k < 3; ++k) sx[3 * t + k] = p.positions[3 * li + k], sv[3 * t + k] = p.velocities[3 * li + k];
 #pragma unroll
@@ -124,7 +155,7 @@ template <bool CELL> __global__ void __launch_bounds__(TPB) k_upload(UploadArgs 
                 sF[9 * t + k] = p.position_gradients[9 * li + k], sC[9 * t + k] = p.velocity_gradients[9 * li + k];
         }
         __syncthreads();
-        if (t < count) upload_one<CELL>(u, i0 + t, sx + 3 * t, sv + 3 * t, sF + 9 * t, sC + 9 * t);
+        if (t < count) upload_one<CELL>(u, i, sc, flags, mi, pj, en, sx + 3 * t, sv + 3 * t, sF + 9 * t, sC + 9 * t);
         __syncthreads();
     }
 }
@@ -269,14 +300,32 @@ bool pageable_access() {
 
 cudaError_t upload_direct(sv_handle *h, const sv_particles *ps, uint32_t n_scenes, const uint64_t *first,
                           const uint32_t *mat_index) {
-    UploadArgs u;
-    u.ps = ps, u.first = first, u.n_scenes = n_scenes, u.mat_index = mat_index;
-    u.scenes = h->scenes, u.a = h->side[0], u.n = h->n, u.dx = h->layout.dx;
     if (h->n == 0) return cudaSuccess;
-    if (h->layout.position_form == 1) k_upload<true><<<blocks_for(h->n), TPB, 0, h->stream>>>(u);
-    else k_upload<false><<<blocks_for(h->n), TPB, 0, h->stream>>>(u);
-    h->launches += 1;
-    cudaError_t e = cudaGetLastError();
+    std::vector<UploadScene> table(n_scenes + 1);
+    for (uint32_t s = 0; s <= n_scenes; ++s) {
+        UploadScene &t = table[s];
+        t = UploadScene{};
+        t.first = first[s];
+        if (s == n_scenes) break;
+        t.flags = ps[s].flags, t.positions = ps[s].positions, t.velocities = ps[s].velocities;
+        t.position_gradients = ps[s].position_gradients, t.velocity_gradients = ps[s].velocity_gradients;
+        t.elastic_energies = ps[s].elastic_energies, t.plastic_j = ps[s].plastic_j;
+    }
+    UploadScene *dtable = nullptr;
+    const size_t bytes = table.size() * sizeof(UploadScene);
+    cudaError_t e = cudaMallocAsync((void **)&dtable, bytes, h->stream);
+    if (e != cudaSuccess) return e;
+    UploadArgs u;
+    u.sc = dtable, u.n_scenes = n_scenes, u.mat_index = mat_index;
+    u.scenes = h->scenes, u.a = h->side[0], u.n = h->n, u.dx = h->layout.dx;
+    if ((e = cudaMemcpyAsync(dtable, table.data(), bytes, cudaMemcpyHostToDevice, h->stream)) == cudaSuccess) {
+        if (h->layout.position_form == 1) k_upload<true><<<blocks_for(h->n), TPB, 0, h->stream>>>(u);
+        else k_upload<false><<<blocks_for(h->n), TPB, 0, h->stream>>>(u);
+        h->launches += 1;
+        e = cudaGetLastError();
+    }
+    const cudaError_t ef = cudaFreeAsync(dtable, h->stream);
+    if (e == cudaSuccess) e = ef;
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);  // the caller's arrays may go away
     return e;
 }
