@@ -255,8 +255,27 @@ template <bool CELL> __global__ void __launch_bounds__(TPB) k_download(DownloadA
 // the GPU touches first is populated through a device-side fault serviced
 // by the host, tens of microseconds each; freshly allocated arrays (numpy's
 // zeros map pages lazily) would otherwise cost more than the copy itself.
-void populate(const std::vector<std::pair<void *, size_t>> &arrays) {
+// True when every page of the range is mapped (mincore); arrays the caller
+// reuses, or that produce_next_state prepared while the substeps ran, need
+// no second pass, whose thread start-up alone is about 0.3 ms.  A page that
+// is mapped but still read-only (never written) only costs the GPU a fault.
+bool all_resident(const std::pair<void *, size_t> &a, size_t page) {
+    const uintptr_t b0 = (uintptr_t)a.first / page * page;
+    const uintptr_t b1 = ((uintptr_t)a.first + a.second + page - 1) / page * page;
+    std::vector<unsigned char> v((b1 - b0) / page);
+    if (v.empty()) return true;
+    if (mincore((void *)b0, b1 - b0, v.data()) != 0) return false;
+    for (unsigned char c : v)
+        if (!(c & 1)) return false;
+    return true;
+}
+
+void populate(const std::vector<std::pair<void *, size_t>> &all) {
     const size_t page = (size_t)std::max(4096L, sysconf(_SC_PAGESIZE));
+    std::vector<std::pair<void *, size_t>> arrays;
+    for (const auto &a : all)
+        if (!all_resident(a, page)) arrays.push_back(a);
+    if (arrays.empty()) return;
     size_t total = 0;
     for (const auto &a : arrays) total += a.second;
     const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
