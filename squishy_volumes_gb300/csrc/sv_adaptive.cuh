@@ -36,6 +36,11 @@ struct State {
     // not bind, and whether they did (the speculative advance is redone)
     float dt_spec;
     uint32_t redo;
+    // the fused form: the next substep's scatter step assumed by this
+    // substep's pass, the one that holds once its limits are known, and
+    // whether that scatter is redone
+    float dt_spec_b, dt_b_next;
+    uint32_t p2g_redo;
 };
 
 // adaptive_time_step_state.rs:35-47
@@ -59,6 +64,21 @@ __host__ __device__ inline float step_without_g2p_limits(const State &s) {
 }
 
 // adaptive_time_step_state.rs:56-63
+__host__ __device__ inline void push(State &s);
+
+// The scatter step of the next substep (allowed() after its force push) if
+// none of the four limits still to come binds: this substep's velocity and
+// deformation limits and the next one's sound and isolated limits.  The
+// pushes are played on a copy with those limits absent.
+__host__ __device__ inline float next_scatter_step_without_new_limits(const State &s) {
+    State c = s;
+    c.vel = c.def = NONE;
+    push(c);  // LimitTimeStepBeforeIntegrate of this substep
+    c.sound = c.iso = NONE;
+    push(c);  // LimitTimeStepBeforeForce of the next
+    return allowed(c);
+}
+
 __host__ __device__ inline void push(State &s) {
     const float cur = without_prior(s);
     if (s.hist_len > HISTORY - 1) {

@@ -414,6 +414,85 @@ int fused_substep(sv_handle *h, float dt, float3 g, double t_next = 0.0) {
     return 0;
 }
 
+// One adaptive substep in the split form: the limits need reductions over
+// all particles between the gather and the advance, so binning, limits
+// before force, P2G, grid update, G2P, limits before integrate and advance
+// each take their own pass.  Used with a frame input loaded, and where the
+// fused form's speculative steps keep failing.
+int adaptive_substep(sv_handle *h, float3 g) {
+    SV_CUDA(launch_adaptive_begin(h));
+    // The binning is redone every sort_interval substeps, as in the fused
+    // path: particles that left their segment's tile scatter and gather
+    // through global memory, and one that left the claimed blocks stops the
+    // substep (ST_MOVED_FAR), which sv_step_adaptive then redoes.
+    if (h->since_sort >= h->sort_interval) {
+        if (!h->keys_valid) SV_CUDA(launch_keys(h));
+        SV_CUDA(launch_sort_and_segments(h));
+        const int which = h->map_cur ^ 1;
+        SV_CUDA(launch_activate(h, which));
+        h->map_cur = h->map_next = which;
+        h->since_sort = 0;
+    }
+    if (h->fin_active) {
+        SV_CUDA(launch_interpolate(h, 0.0));  // at the device time of the substep
+        SV_CUDA(launch_clear_variants(h, h->gcur));
+    }
+    // Later substeps of a call take the force limits that the advance before
+    // them reduced (a stopped substep stops all that follow it).
+    SV_CUDA(launch_limits_force(h, h->limits_pass_pending));
+    h->limits_pass_pending = false;
+    SV_CUDA(launch_clear(h, h->gcur, h->map_cur));
+    SV_CUDA(launch_p2g(h, 0.f, g));
+    SV_CUDA(launch_grid_update(h, false));
+    SV_CUDA(launch_g2p_only(h));
+    SV_CUDA(launch_advance(h));
+    h->since_sort += 1;
+    return 0;
+}
+
+// One adaptive substep in the fused form (no frame input loaded), shaped
+// like fused_substep: the pass that advances this substep also scatters the
+// next one, at the steps the adaptive state will allow unless one of the
+// limits still to come binds (launch_g2p2g_adaptive checks and redoes).  The
+// first substep of a call, and the one after a recovery, scatter their own
+// momentum first, binned afresh.
+int adaptive_substep_fused(sv_handle *h, float3 g) {
+    SV_CUDA(launch_adaptive_begin(h));
+    if (!h->pending_valid) {
+        SV_CUDA(launch_limits_force(h, h->limits_pass_pending));
+        h->limits_pass_pending = false;
+        if (!h->keys_valid) SV_CUDA(launch_keys(h));
+        SV_CUDA(launch_sort_and_segments(h));
+        const int which = h->map_cur ^ 1;
+        SV_CUDA(launch_activate(h, which));
+        h->map_cur = h->map_next = which;
+        SV_CUDA(launch_clear(h, h->gcur, which));
+        SV_CUDA(launch_p2g(h, 0.f, g));
+        SV_CUDA(launch_latch(h));  // a failed scatter stops the substep before its gather
+        h->pending_valid = true;
+        h->need_perm = true;
+        h->since_sort = 0;
+    } else {
+        SV_CUDA(launch_limits_force(h, false));  // the force step's push
+        if (h->since_sort >= h->sort_interval) {
+            if (!h->keys_valid) SV_CUDA(launch_keys(h));
+            SV_CUDA(launch_sort_and_segments(h));
+            const int which = h->map_cur ^ 1;
+            SV_CUDA(launch_activate(h, which));
+            h->map_next = which;
+            h->need_perm = true;
+            h->since_sort = 0;
+        } else {
+            h->map_next = h->map_cur;
+        }
+    }
+    SV_CUDA(launch_grid_update(h, true, !h->stop_latched));
+    const bool write_keys = h->since_sort + 1 >= h->sort_interval;
+    SV_CUDA(launch_g2p2g_adaptive(h, g, write_keys, h->need_perm));
+    h->since_sort += 1;
+    return 0;
+}
+
 void clear_graphs(sv_handle *h) {
     for (auto &kv : h->graphs)
         if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
@@ -425,9 +504,11 @@ void clear_graphs(sv_handle *h) {
 // configuration occurs, replayed afterwards.  Every launch of a period reads
 // its counts from device memory, so the captured launches stay valid; only
 // the pointers and the host-side bookkeeping differ between configurations,
-// and those are in the key and the saved state.
-int run_period_graph(sv_handle *h, float dt, float3 g) {
-    sv_handle::GraphKey key{h->cur, h->gcur, h->map_cur, h->sort_interval, dt, {g.x, g.y, g.z}};
+// and those are in the key and the saved state.  `adaptive`: substeps of the
+// fused adaptive form, whose steps all come from the device (key dt -1).
+int run_period_graph(sv_handle *h, float dt, float3 g, bool adaptive = false) {
+    auto substep = [&]() { return adaptive ? adaptive_substep_fused(h, g) : fused_substep(h, dt, g); };
+    sv_handle::GraphKey key{h->cur, h->gcur, h->map_cur, h->sort_interval, adaptive ? -1.f : dt, {g.x, g.y, g.z}};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
         // host bookkeeping before the period, put back if the capture fails
@@ -441,7 +522,7 @@ int run_period_graph(sv_handle *h, float dt, float3 g) {
         cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
             int rc = 0;
-            for (uint32_t s = 0; s < key.period && rc == 0; ++s) rc = fused_substep(h, dt, g);
+            for (uint32_t s = 0; s < key.period && rc == 0; ++s) rc = substep();
             e = cudaStreamEndCapture(h->stream, &graph);
             if (rc && e == cudaSuccess) e = cudaErrorStreamCaptureInvalidated;
             if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
@@ -459,7 +540,7 @@ int run_period_graph(sv_handle *h, float dt, float3 g) {
             h->launches = l0, h->sorts = sorts0;
             h->use_graphs = false;
             for (uint32_t s = 0; s < key.period; ++s)
-                if (fused_substep(h, dt, g)) return -1;
+                if (substep()) return -1;
             return 0;
         }
         sv_handle::GraphState st;
@@ -872,52 +953,10 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
 // ------------------------------------------------------------------ adaptive time steps
 // CpuState::produce_next_state with adaptive_time_steps = true
 // (cpu_state.rs:146-197): substeps run while time < target_time, each with
-// the phase order of phase/mod.rs:27-41.  The limits need reductions over
-// all particles between the gather and the advance, so the substep is not
-// fused: binning, limits before force, P2G, grid update, G2P, limits before
-// integrate, advance.  The time steps live on the device; a substep that
-// starts at or after the target time is a no-op (stop latch).
-namespace {
-
-int adaptive_substep(sv_handle *h, float3 g) {
-    SV_CUDA(launch_adaptive_begin(h));
-    // The binning is redone every sort_interval substeps, as in the fused
-    // path: particles that left their segment's tile scatter and gather
-    // through global memory, and one that left the claimed blocks stops the
-    // substep (ST_MOVED_FAR), which sv_step_adaptive then redoes.
-    if (h->since_sort >= h->sort_interval) {
-        if (!h->keys_valid) SV_CUDA(launch_keys(h));
-        SV_CUDA(launch_sort_and_segments(h));
-        const int which = h->map_cur ^ 1;
-        SV_CUDA(launch_activate(h, which));
-        h->map_cur = h->map_next = which;
-        h->since_sort = 0;
-    }
-    if (h->fin_active) {
-        SV_CUDA(launch_interpolate(h, 0.0));  // at the device time of the substep
-        SV_CUDA(launch_clear_variants(h, h->gcur));
-    }
-    // Later substeps of a call take the force limits that the advance before
-    // them reduced (a stopped substep stops all that follow it).
-    SV_CUDA(launch_limits_force(h, h->limits_pass_pending));
-    h->limits_pass_pending = false;
-    SV_CUDA(launch_clear(h, h->gcur, h->map_cur));
-    SV_CUDA(launch_p2g(h, 0.f, g));
-    SV_CUDA(launch_grid_update(h, false));
-    if (h->fin_active) {
-        SV_CUDA(launch_g2p_only(h));
-        SV_CUDA(launch_advance(h));
-    } else {
-        // The velocity and deformation limits of the G2P rarely bind: the
-        // advance goes ahead at the step that holds unless they do and is
-        // redone from the same input, at the step they allow, when they do.
-        SV_CUDA(launch_g2p_advance_adaptive(h));
-    }
-    h->since_sort += 1;
-    return 0;
-}
-
-}  // namespace
+// the phase order of phase/mod.rs:27-41.  The time steps live on the device;
+// a substep that starts at or after the target time is a no-op (stop latch).
+// A substep runs in the fused form (adaptive_substep_fused) or the split
+// one (adaptive_substep), see there.
 
 int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float max_time_step,
                      const float gravity[3], const volatile int32_t *cancel, uint32_t *status_out,
@@ -962,18 +1001,42 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
     uint32_t fallback_before = h->host_counters[C_FALLBACK], substeps_before = base;
     uint32_t status = 0;
     h->adaptive_active = true;
+    const bool fused = !h->fin_active;  // with a frame input the substep runs split
     int rc = 0;
     while (true) {
         if (cancel && *cancel) {
             status |= SV_STATUS_CANCELED;
             break;
         }
-        for (int s = 0; s < 16 && rc == 0; ++s) rc = adaptive_substep(h, g);
+        // The fused form pays for a speculation that failed with a second
+        // pass (and a second scatter): where limits keep binding (a run
+        // governed by its velocity limit) the split form is cheaper.  Batches
+        // whose speculations failed in more than a fifth of their substeps
+        // switch to it for the next eight batches, then the fused form is
+        // tried again.
+        const bool use_fused = fused && h->adt_split_batches == 0;
+        if (!use_fused && h->adt_split_batches > 0) h->adt_split_batches -= 1;
+        if (!use_fused) h->pending_valid = false;  // the split form scatters each substep itself
+        const uint32_t miss0 = h->host_counters[C_ADT_MISS], done0 = h->host_counters[C_SUBSTEPS];
+        for (uint32_t s = 0; s < 16 && rc == 0;) {
+            // whole binning periods of the fused form replay CUDA graphs, as
+            // in sv_step
+            if (use_fused && h->use_graphs && !h->profiling && h->pending_valid && h->keys_valid &&
+                h->since_sort >= h->sort_interval && 16 - s >= h->sort_interval) {
+                rc = run_period_graph(h, 0.f, g, true);
+                s += h->sort_interval;
+            } else {
+                rc = use_fused ? adaptive_substep_fused(h, g) : adaptive_substep(h, g);
+                s += 1;
+            }
+        }
         if (rc || read_counters(h)) {
             rc = -1;
             break;
         }
         const uint32_t stw = h->host_counters[C_STATUS];
+        if (use_fused && 5 * (h->host_counters[C_ADT_MISS] - miss0) > h->host_counters[C_SUBSTEPS] - done0 + 1)
+            h->adt_split_batches = 8;
         if (stw & ST_OUT_OF_GRID) {
             rc = fail("sv_step_adaptive: a live particle left the grid block index");
             break;
@@ -1006,9 +1069,21 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
             }
             if (stw & ST_MOVED_FAR) h->sort_interval = std::max<uint32_t>(1, h->sort_interval / 2);
             // Redo the stopped substep from its start, binned afresh, with the
-            // adaptive state it began with (its limits not yet in the history).
-            SV_CUDA(cudaMemcpyAsync(h->adt, h->adt_backup, sizeof(adaptive::State), cudaMemcpyDeviceToDevice,
-                                    h->stream));
+            // adaptive state it began with (its limits not yet in the history)
+            // -- unless it completed and only its scatter of the next substep
+            // failed (the fused form), which the next substep redoes.
+            bool completed = false;
+            if (fused) {
+                adaptive::State now, back;
+                SV_CUDA(cudaMemcpyAsync(&now, h->adt, sizeof(now), cudaMemcpyDeviceToHost, h->stream));
+                SV_CUDA(cudaMemcpyAsync(&back, h->adt_backup, sizeof(back), cudaMemcpyDeviceToHost, h->stream));
+                SV_CUDA(cudaStreamSynchronize(h->stream));
+                completed = now.substeps != back.substeps;
+            }
+            if (!completed)
+                SV_CUDA(cudaMemcpyAsync(h->adt, h->adt_backup, sizeof(adaptive::State), cudaMemcpyDeviceToDevice,
+                                        h->stream));
+            h->pending_valid = false;
             h->limits_pass_pending = true;
             h->since_sort = h->sort_interval;
             h->host_counters[C_STATUS] &= ~(ST_CAPACITY | ST_MOVED_FAR);
@@ -1033,6 +1108,7 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
     }
     h->adaptive_active = false;
     h->keys_valid = false;
+    h->pending_valid = false;  // a scatter made at adaptive steps
     h->force_limits_valid = rc == 0;
     if (rc) return -1;
     SV_CUDA(cudaMemcpyAsync(&st, h->adt, sizeof(st), cudaMemcpyDeviceToHost, h->stream));

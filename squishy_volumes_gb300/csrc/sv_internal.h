@@ -50,7 +50,8 @@ enum Counter : int {
     C_CLOSURE_ERR = 11,  // a tensor-core wait of the learned closure gave up
     C_CTA_DONE = 12,     // CTAs of a self-latching particle pass that have finished
     C_TRANSFER_BAD = 13, // a direct download met an original index out of range or repeated
-    C_COUNT = 14,
+    C_ADT_MISS = 14,     // adaptive substeps whose speculative steps failed (fused form)
+    C_COUNT = 15,
 };
 
 // One side of the particle state (ping-pong).  Structure of arrays: pos and
@@ -225,6 +226,9 @@ struct sv_handle {
     // the next adaptive substep queues k_limits_force: the first of a call and
     // the redo of a stopped one, whose state may predate any advance
     bool limits_pass_pending = false;
+    // batches of adaptive substeps still to run in the split form, after a
+    // batch whose speculative steps failed too often
+    uint32_t adt_split_batches = 0;
 
     // Simulation time of the completed state (the reference's CpuState::time),
     // used to interpolate the frame input.
@@ -293,9 +297,10 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 gravity, bool write_keys
 cudaError_t launch_limits_force(sv_handle *h, bool reduce);
 cudaError_t launch_g2p_only(sv_handle *h);
 cudaError_t launch_advance(sv_handle *h);
-// G2P and the advance of an adaptive substep in one pass at the step the
-// advance takes unless the G2P's own limits bind, redone when they do
-cudaError_t launch_g2p_advance_adaptive(sv_handle *h);
+// The fused pass of an adaptive substep (no frame input): advance at the
+// speculative step, scatter of the next substep at its speculative steps,
+// the checks, the redo of either when a limit bound, and k_adaptive_finish
+cudaError_t launch_g2p2g_adaptive(sv_handle *h, float3 g, bool write_keys, bool use_perm);
 // latches the stop bits and keeps the adaptive state for a redo
 cudaError_t launch_adaptive_begin(sv_handle *h);
 // frame input: interpolation at `time` (adaptive: the device time), the

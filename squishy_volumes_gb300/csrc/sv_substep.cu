@@ -60,8 +60,11 @@ struct Rec {
 };
 
 // MODE_G2P2G_LEARNED is MODE_G2P2G with the learned closure for snow and
-// sand.  Adaptive time steps split the fused pass: MODE_G2P_ONLY gathers v
-// and C (written back in place), MODE_ADVANCE advances from them.
+// sand.  Adaptive time steps: MODE_G2P2G_ADAPTIVE is the fused pass at the
+// speculative steps of the adaptive state, reducing the G2P's limits and the
+// next substep's force limits as it goes; with a frame input loaded the
+// substep is split instead (MODE_G2P_ONLY gathers v and C, written back in
+// place, MODE_ADVANCE advances from them).
 enum Mode {
     MODE_P2G = 0,
     MODE_G2P2G = 1,
@@ -69,6 +72,7 @@ enum Mode {
     MODE_G2P_ONLY = 3,
     MODE_ADVANCE = 4,
     MODE_G2P_ADVANCE = 5,  // the fused pass without the next scatter (the next substep's input is not loaded)
+    MODE_G2P2G_ADAPTIVE = 6,
 };
 
 struct StepArgs {
@@ -90,8 +94,13 @@ struct StepArgs {
     col::FrameArgs fa;                   // frame input (kernels instantiated with FIN only)
     col::VariantTable vcur, vnext;       // collider variants gathered from / scattered into
     bool self_latch;                     // the last CTA latches the stop bits and counts the substep
-    // adaptive G2P_ADVANCE: 1 = the pass at the speculative step dt_spec,
-    // reducing the G2P's limits; 2 = its redo at dt_c, only when flagged
+    // Adaptive passes (their steps come from the adaptive state):
+    //   2  G2P_ADVANCE redoing a G2P2G_ADAPTIVE pass's advance at dt_c, only
+    //      when the G2P's limits bound (redo)
+    //   3  G2P2G_ADAPTIVE: advance at dt_spec, the next substep's scatter at
+    //      dt_spec (its external force) and dt_spec_b (its stress)
+    //   4  P2G of the next substep redone at its exact steps, only when a
+    //      speculation failed (p2g_redo)
     uint32_t adt_pass;
     uint64_t n;
     GridLayout L;
@@ -389,7 +398,9 @@ __global__ void __launch_bounds__(ELEM_THREADS)
     }
 }
 
-__global__ void __launch_bounds__(ELEM_THREADS) k_clear_grid(float4 *grid, uint64_t capacity, uint32_t *counters, int which) {
+__global__ void __launch_bounds__(ELEM_THREADS)
+    k_clear_grid(float4 *grid, uint64_t capacity, uint32_t *counters, int which, const uint32_t *only_if = nullptr) {
+    if (only_if && !*only_if) return;
     uint64_t slots = counters[C_NSLOT0 + which];
     if (slots > capacity) slots = capacity;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < slots * 64; i += (uint64_t)gridDim.x * blockDim.x)
@@ -785,13 +796,15 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
     constexpr bool LEARNED = MODE == MODE_G2P2G_LEARNED;
     // what the pass does: gather from the grid, advance the particles (and
     // write them out in sorted order), scatter into the next grid
-    constexpr bool GATHER = MODE == MODE_G2P2G || LEARNED || MODE == MODE_G2P_ONLY || MODE == MODE_G2P_ADVANCE;
-    constexpr bool G2P = MODE == MODE_G2P2G || LEARNED || MODE == MODE_ADVANCE || MODE == MODE_G2P_ADVANCE;  // advances
-    constexpr bool SCATTER = MODE == MODE_P2G || MODE == MODE_G2P2G || LEARNED;
+    constexpr bool ADT_FUSED = MODE == MODE_G2P2G_ADAPTIVE;
+    constexpr bool GATHER = MODE == MODE_G2P2G || LEARNED || ADT_FUSED || MODE == MODE_G2P_ONLY || MODE == MODE_G2P_ADVANCE;
+    constexpr bool G2P = MODE == MODE_G2P2G || LEARNED || ADT_FUSED || MODE == MODE_ADVANCE || MODE == MODE_G2P_ADVANCE;  // advances
+    constexpr bool SCATTER = MODE == MODE_P2G || MODE == MODE_G2P2G || LEARNED || ADT_FUSED;
     constexpr bool LOAD_VC = MODE == MODE_P2G || MODE == MODE_ADVANCE;  // v and C from the state
     __shared__ Shared sh;
     __shared__ typename std::conditional<LEARNED, SharedLearned, int>::type shl;
     if (MODE == MODE_G2P_ADVANCE && A.adt_pass == 2 && !*(volatile const uint32_t *)&A.adt->redo) return;
+    if (MODE == MODE_P2G && A.adt_pass == 4 && !*(volatile const uint32_t *)&A.adt->p2g_redo) return;
     const uint32_t stop_at_start = stopped(A.counters);
     if (stop_at_start) {
         if (G2P) {
@@ -818,15 +831,19 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
     // time steps of the external force, the scatter and the advance: one dt,
     // or the three of the adaptive state's phases
     float dt_force = A.dt, dt_scatter = A.dt, dt_adv = A.dt;
-    if (A.adt) dt_force = A.adt->dt_a, dt_scatter = A.adt->dt_b, dt_adv = A.adt_pass == 1 ? A.adt->dt_spec : A.adt->dt_c;
+    if (A.adt) {
+        dt_force = A.adt->dt_a, dt_scatter = A.adt->dt_b, dt_adv = A.adt->dt_c;
+        if (A.adt_pass == 3) dt_adv = dt_force = A.adt->dt_spec, dt_scatter = A.adt->dt_spec_b;
+        if (A.adt_pass == 4) dt_force = A.adt->dt_c, dt_scatter = A.adt->dt_b_next;
+    }
     // G2P_ONLY and the speculative G2P_ADVANCE: max |v| and max |C_ij| of live particles
-    constexpr bool G2P_LIMITS_MODE = MODE == MODE_G2P_ONLY || MODE == MODE_G2P_ADVANCE;
-    const bool g2p_limits = MODE == MODE_G2P_ONLY || (MODE == MODE_G2P_ADVANCE && A.adt_pass == 1);
+    constexpr bool G2P_LIMITS_MODE = MODE == MODE_G2P_ONLY || MODE == MODE_G2P_ADVANCE || ADT_FUSED;
+    const bool g2p_limits = MODE == MODE_G2P_ONLY || ADT_FUSED;
     float red_v = 0.f, red_c = 0.f;
     bool red_live = false;
     // ADVANCE, adaptive G2P_ADVANCE: the next substep's sound and isolated
     // limits of the advanced state
-    constexpr bool FORCE_LIMITS_MODE = MODE == MODE_ADVANCE || MODE == MODE_G2P_ADVANCE;
+    constexpr bool FORCE_LIMITS_MODE = MODE == MODE_ADVANCE || MODE == MODE_G2P_ADVANCE || ADT_FUSED;
     float lim_sound = adaptive::NONE, lim_iso = adaptive::NONE;
     if (G2P) {
         // particles that were tombstoned at binning time are carried over
@@ -1315,7 +1332,8 @@ __global__ void k_dt_force(adaptive::State *st, uint32_t *counters) {
     st->red_sound = __float_as_uint(adaptive::NONE), st->red_iso = __float_as_uint(adaptive::NONE);
     st->force_ready = 0;
     st->dt_spec = adaptive::step_without_g2p_limits(*st);
-    st->redo = 0;
+    st->dt_spec_b = adaptive::next_scatter_step_without_new_limits(*st);
+    st->redo = 0, st->p2g_redo = 0;
     if (!(st->dt_a > 0.f) || !(st->dt_b > 0.f)) counters[C_STATUS] |= ST_ZERO_DT;
 }
 
@@ -1337,8 +1355,12 @@ __global__ void k_dt_integrate(adaptive::State *st, uint32_t *counters, float dx
 
 // cpu_state.rs:186-189: the substep's time step is added to the time; the
 // run stops (ST_TIME_REACHED latches) once the target time is reached.
-__global__ void k_adaptive_finish(adaptive::State *st, uint32_t *counters) {
-    if (counters[C_STOP] || (counters[C_STATUS] & STOP_MASK)) return;
+// `next_scatter`: the substep's pass also scattered the next substep, whose
+// failure (a particle outside the claimed blocks, the block capacity) is
+// redone by the host without undoing this one.
+__global__ void k_adaptive_finish(adaptive::State *st, uint32_t *counters, bool next_scatter = false) {
+    const uint32_t mask = next_scatter ? STOP_MASK & ~(ST_MOVED_FAR | ST_CAPACITY) : STOP_MASK;
+    if (counters[C_STOP] || (counters[C_STATUS] & mask)) return;
     st->force_ready = 1;  // the advance completed its reduction of the next force limits
     st->time += (double)st->dt_c;
     st->substeps += 1;
@@ -1423,7 +1445,7 @@ template <int MODE> void launch_particles(sv_handle *h, const StepArgs &A, unsig
     const unsigned blocks = grid ? grid : particle_blocks(h);
     h->stop_latched = A.self_latch;
     if (MODE != MODE_ADVANCE && MODE != MODE_P2G && MODE != MODE_G2P_ONLY) h->force_limits_valid = false;
-    if constexpr (MODE != MODE_G2P2G_LEARNED) {
+    if constexpr (MODE != MODE_G2P2G_LEARNED && MODE != MODE_G2P2G_ADAPTIVE) {
         if (h->fin_active) {
             if (h->layout.position_form) k_particles<true, MODE, true><<<blocks, PT, 0, h->stream>>>(A);
             else k_particles<false, MODE, true><<<blocks, PT, 0, h->stream>>>(A);
@@ -1538,28 +1560,62 @@ cudaError_t launch_g2p_only(sv_handle *h) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_g2p_advance_adaptive(sv_handle *h) {
-    StepArgs A = make_args(h, 0.f, make_float3(0.f, 0.f, 0.f));
-    A.adt = reinterpret_cast<adaptive::State *>(h->adt);
+// The next substep's steps as its k_dt_force will take them, from this
+// substep's advance and the force limits its pass reduced (the push on a
+// copy): when they differ from the ones its scatter assumed, that scatter is
+// redone (p2g_redo).
+__global__ void k_dt_next(adaptive::State *st, uint32_t *counters) {
+    if (counters[C_STOP]) return;
+    adaptive::State nx = *st;
+    nx.sound = __uint_as_float(st->red_sound);
+    nx.iso = __uint_as_float(st->red_iso);
+    adaptive::push(nx);
+    st->dt_b_next = adaptive::allowed(nx);
+    st->p2g_redo = st->redo || st->dt_b_next != st->dt_spec_b;
+    if (st->p2g_redo) counters[C_ADT_MISS] += 1;
+}
+
+cudaError_t launch_g2p2g_adaptive(sv_handle *h, float3 g, bool write_keys, bool use_perm) {
+    auto *st = reinterpret_cast<adaptive::State *>(h->adt);
+    StepArgs A = make_args(h, 0.f, g);
+    A.adt = st;
+    if (!write_keys) A.keys_out = nullptr;
+    if (!use_perm) A.perm = nullptr;
     {
-        Scoped s(h, "g2p_advance");
-        A.adt_pass = 1;
-        launch_particles<MODE_G2P_ADVANCE>(h, A);
-        k_dt_integrate<<<1, 1, 0, h->stream>>>(A.adt, h->counters, h->layout.dx);
+        Scoped s(h, "g2p2g_adaptive");
+        A.adt_pass = 3;
+        launch_particles<MODE_G2P2G_ADAPTIVE>(h, A);
+        k_dt_integrate<<<1, 1, 0, h->stream>>>(st, h->counters, h->layout.dx);
     }
     {
-        // one resident wave: it returns at once unless the step was wrong
-        Scoped s(h, "advance_redo");
-        A.adt_pass = 2;
-        launch_particles<MODE_G2P_ADVANCE>(h, A, (unsigned)sm_count() * 5);
-        k_adaptive_finish<<<1, 1, 0, h->stream>>>(A.adt, h->counters);
+        // the advance again at dt_c when the G2P's limits bound; then the
+        // next substep's scatter again when any of its assumed steps was off
+        Scoped s(h, "adaptive_redo");
+        StepArgs R = A;
+        R.adt_pass = 2;
+        launch_particles<MODE_G2P_ADVANCE>(h, R, (unsigned)sm_count() * 5);
+        k_dt_next<<<1, 1, 0, h->stream>>>(st, h->counters);
+        k_clear_grid<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(h->grid[h->gcur ^ 1], h->capacity,
+                                                                                      h->counters, h->map_next, &st->p2g_redo);
+        StepArgs P = make_args(h, 0.f, g);
+        P.adt = st;
+        P.adt_pass = 4;
+        P.in = h->side[h->cur ^ 1];  // the advanced state, in the binning's order
+        P.perm = nullptr;
+        P.keys_out = nullptr;
+        P.map_next = h->blockmap[h->map_next];
+        P.grid_next = h->grid[h->gcur ^ 1];
+        launch_particles<MODE_P2G>(h, P, (unsigned)sm_count() * 5);
+        k_adaptive_finish<<<1, 1, 0, h->stream>>>(st, h->counters, true);
     }
-    h->launches += 4;
+    h->launches += 7;
     h->vel_side = h->gcur;
     h->vel_map = h->map_cur;
     h->cur ^= 1;
-    h->keys_valid = true;
-    h->need_perm = false;  // written in the binning's order
+    h->gcur ^= 1;
+    h->map_cur = h->map_next;
+    h->keys_valid = write_keys;
+    h->need_perm = false;
     return cudaGetLastError();
 }
 
@@ -1583,7 +1639,7 @@ cudaError_t launch_advance(sv_handle *h) {
 __global__ void k_adaptive_begin(adaptive::State *st, adaptive::State *backup, uint32_t *counters) {
     const uint32_t stop = counters[C_STATUS] & STOP_MASK;
     counters[C_STOP] = stop;
-    st->redo = 0;
+    st->redo = 0, st->p2g_redo = 0;
     if (stop) return;
     *backup = *st;
     // k_limits_force reduces this substep's force limits unless the last
