@@ -232,6 +232,8 @@ typedef struct sv_stats {
     uint64_t closure_learned;   /* snow/sand particle-substeps through the learned closure (low 32 bits) */
     uint64_t closure_fallbacks; /* of the learned mode's snow/sand particle-substeps: return-map fallbacks */
     uint64_t closure_mode;      /* 0 return maps, 1 learned closure */
+    uint64_t adaptive_misses;   /* adaptive substeps whose speculative steps failed and were redone */
+    uint64_t adaptive_split;    /* adaptive substeps queued in the split form */
 } sv_stats;
 
 /* Adaptive time steps: CpuState::produce_next_state with

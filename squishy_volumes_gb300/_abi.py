@@ -96,6 +96,8 @@ class SvStats(ct.Structure):
         ("closure_learned", ct.c_uint64),
         ("closure_fallbacks", ct.c_uint64),
         ("closure_mode", ct.c_uint64),
+        ("adaptive_misses", ct.c_uint64),
+        ("adaptive_split", ct.c_uint64),
     ]
 
 

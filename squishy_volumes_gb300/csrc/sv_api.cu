@@ -1027,6 +1027,7 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
                 s += h->sort_interval;
             } else {
                 rc = use_fused ? adaptive_substep_fused(h, g) : adaptive_substep(h, g);
+                if (!use_fused) h->adt_split_substeps += 1;
                 s += 1;
             }
         }
@@ -1292,6 +1293,8 @@ int sv_get_stats(sv_handle *h, sv_stats *out) {
     out->closure_learned = h->host_counters[C_CLOSURE];
     out->closure_fallbacks = h->host_counters[C_CLOSURE_FB];
     out->closure_mode = (uint64_t)h->closure_mode;
+    out->adaptive_misses = h->host_counters[C_ADT_MISS];
+    out->adaptive_split = h->adt_split_substeps;
     return 0;
 }
 

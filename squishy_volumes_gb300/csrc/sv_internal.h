@@ -229,6 +229,7 @@ struct sv_handle {
     // batches of adaptive substeps still to run in the split form, after a
     // batch whose speculative steps failed too often
     uint32_t adt_split_batches = 0;
+    uint64_t adt_split_substeps = 0;  // adaptive substeps queued in the split form
 
     // Simulation time of the completed state (the reference's CpuState::time),
     // used to interpolate the frame input.

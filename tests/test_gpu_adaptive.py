@@ -145,3 +145,64 @@ def test_stale_binning_recovers_like_the_reference(cuda_lib, oracle_mod, sort_in
     if sort_interval == 8:
         assert gpu.stats()["sorts"] < done  # not every substep
     gpu.close()
+
+
+def test_long_adaptive_run_replays_period_graphs(cuda_lib, oracle_mod):
+    """Forty-odd adaptive substeps in the fused form: after the first batch
+    the binning periods replay CUDA graphs (every step and redo flag lives on
+    the device), and the run still matches the oracle substep for substep."""
+    s = scenes.small_mixed()
+    target, max_dt = 0.01, 2.5e-4
+    gpu = CudaState.from_io_state(s.io_state, s.consts, Extras(sort_interval=4))
+    status, done, t = gpu.step_adaptive(target, max_dt, s.gravity, time=0.0)
+    ref = oracle_mod.OracleState(s.io_state.particles, s.consts, None, fp64=False)
+    rc, n_ref, t_ref, lim_ref = ref.step_adaptive(0.0, target, max_dt, s.gravity)
+    assert (status, rc) == (0, 0)
+    assert done == n_ref and done >= 40
+    assert abs(t - t_ref) <= 1e-5 * t_ref
+    assert gpu.stats()["graph_replays"] > 0 and gpu.stats()["adaptive_split"] == 0
+    # after forty substeps max |v| and max |C| carry the state's rounding
+    # differences (velocities agree to the 1e-3 of TOL), so the velocity and
+    # deformation limits are compared at that level
+    _limits_close(gpu.time_step_limits(), lim_ref, rel=1e-3)
+    out, exp = gpu.download(), ref.download()
+    np.testing.assert_array_equal(out.flags, exp.flags)
+    live = (exp.flags & SV_TOMBSTONED) == 0
+    compare_states(out, exp, live, tol=TOL, dx=s.consts.grid_node_size)
+    gpu.close()
+
+
+def test_velocity_governed_run_falls_back_to_the_split_form(cuda_lib, oracle_mod):
+    """Particles speeding up under strong gravity: the velocity limit shrinks
+    every substep, so the fused form's speculative steps keep failing and
+    the run moves to the split form after its first batch.  Both forms'
+    substeps together match the oracle's."""
+    s = scenes.small_mixed()
+    p = s.io_state.particles.copy()
+    p.velocities[:] = np.array([20.0, 0.0, 0.0], np.float32)
+    p.velocity_gradients[:] = 0
+    g = (2000.0, 0.0, 0.0)
+    target, max_dt = 0.02, 1e-2
+    gpu = CudaState.from_io_state(IoState(0.0, p), s.consts)
+    status, done, t = gpu.step_adaptive(target, max_dt, g, time=0.0)
+    ref = oracle_mod.OracleState(p, s.consts, None, fp64=False)
+    rc, n_ref, t_ref, lim_ref = ref.step_adaptive(0.0, target, max_dt, g)
+    assert (status, rc) == (0, 0)
+    assert done == n_ref and done > 16
+    assert abs(t - t_ref) <= 1e-5 * t_ref
+    lim = gpu.time_step_limits()
+    assert lim["velocity"] < min(lim["sound"], lim["isolated"], lim["deformation"])
+    # the governing velocity limit and the steps as tightly as everywhere;
+    # max |C| of a body moving at 60 m/s is a small difference of large
+    # terms, so the (non-governing) deformation limit only to 1e-2
+    deformation = lim["deformation"]
+    lim["deformation"] = float(lim_ref[4])
+    _limits_close(lim, lim_ref)
+    assert abs(deformation - lim_ref[4]) <= 1e-2 * lim_ref[4]
+    st = gpu.stats()
+    assert st["adaptive_misses"] > 0 and st["adaptive_split"] > 0
+    out, exp = gpu.download(), ref.download()
+    np.testing.assert_array_equal(out.flags, exp.flags)
+    live = (exp.flags & SV_TOMBSTONED) == 0
+    compare_states(out, exp, live, tol=TOL, dx=s.consts.grid_node_size)
+    gpu.close()
