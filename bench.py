@@ -13,6 +13,8 @@ dt = 5e-5), synthetic and seeded.  A "step" is one substep over all particles.
                CUDA-event duration, against the measured HBM copy bandwidth
   cpu_baseline the CPU oracle (the reference substep restated in C++, fp32,
                all host threads) on a bounded sample of the same scene
+  adaptive     (--adaptive) sv_step_adaptive over the simulated time of K
+               substeps, the scene's dt as the largest step
 
 --impl reference runs only the CPU restatement of the reference substep (the
 reference itself is Rust and cannot be built here) on the same scene.
@@ -55,6 +57,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bound on the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--adaptive", action="store_true",
+                    help="also time sv_step_adaptive over the same span of simulated time (max step = the scene's dt)")
     ap.add_argument("--bake", type=int, default=0,
                     help="also time this many whole frames with a frame-cache store after each, against the same "
                          "frames without stores")
@@ -429,6 +433,31 @@ def run_ours(args, rank, world, local):
         "frac": round(sub_achieved / hbm, 4),
     }
 
+    # adaptive time steps (sv_step_adaptive) over the time K fixed substeps
+    # span, from the state reached, the scene's dt as the largest step
+    adaptive = None
+    if args.adaptive and batch is None:
+        gpu.step_adaptive(gpu.time + args.warmup * scene.dt * (1 - 1e-6), scene.dt, scene.gravity)
+        sa0 = gpu.stats()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        status_a, done_a, _ = gpu.step_adaptive(gpu.time + args.steps * scene.dt * (1 - 1e-6), scene.dt, scene.gravity)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        sa1 = gpu.stats()
+        el_a = ev0.elapsed_time(ev1) * 1e-3
+        adaptive = {
+            "value": sa1["live_particles"] * done_a / el_a,
+            "unit": METRIC,
+            "substeps": done_a,
+            "status": status_a,
+            "ms_per_substep": el_a * 1e3 / max(done_a, 1),
+            "speculation_misses": sa1["adaptive_misses"] - sa0["adaptive_misses"],
+            "split_substeps": sa1["adaptive_split"] - sa0["adaptive_split"],
+            "graph_replays": sa1["graph_replays"] - sa0["graph_replays"],
+            "max_time_step": scene.dt,
+        }
+
     # end to end through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
@@ -500,6 +529,7 @@ def run_ours(args, rank, world, local):
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "adaptive": adaptive,
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "fp64_svd_particles": st["fp64_svd"],
