@@ -100,10 +100,12 @@ __host__ __device__ inline T sound_limit(bool fluid, T mu, T lambda, T bulk, int
     const T g[3] = {y * z, x * z, x * y};
     const T H[3][3] = {{0, z, y}, {z, 0, x}, {y, x, 0}};
     T first[3], second[3][3];
+    const T iJ = T(1) / J;
     if (!fluid) {
         // elastic.rs:314-339 with the invariant derivatives of elastic.rs:97-141, 276-295
-        const T d1 = (lambda * log(J) - mu) / J;
-        const T d2 = (lambda * (T(1) - log(J)) + mu) / (J * J);
+        const T lj = log(J);
+        const T d1 = (lambda * lj - mu) * iJ;
+        const T d2 = (lambda * (T(1) - lj) + mu) * (iJ * iJ);
         for (int i = 0; i < 3; ++i) {
             first[i] = mu * s[i] + d1 * g[i];
             for (int j = 0; j < 3; ++j) second[i][j] = (i == j ? mu : T(0)) + d2 * g[i] * g[j] + d1 * H[i][j];
@@ -112,8 +114,9 @@ __host__ __device__ inline T sound_limit(bool fluid, T mu, T lambda, T bulk, int
         // elastic.rs:555-570, 630-654
         T Jg = T(1);
         for (int k = 0; k < gamma; ++k) Jg *= J;
-        const T d1 = bulk * (T(1) - T(1) / Jg);
-        const T d2 = (T)gamma * bulk / (Jg * J);
+        const T iJg = T(1) / Jg;
+        const T d1 = bulk * (T(1) - iJg);
+        const T d2 = (T)gamma * bulk * iJg * iJ;
         for (int i = 0; i < 3; ++i) {
             first[i] = d1 * g[i];
             for (int j = 0; j < 3; ++j) second[i][j] = d2 * g[i] * g[j] + d1 * H[i][j];
@@ -131,9 +134,8 @@ __host__ __device__ inline T sound_limit(bool fluid, T mu, T lambda, T bulk, int
     kappa = fmax(kappa, y * y * second[1][1]);
     kappa = fmax(kappa, z * z * second[2][2]);
     kappa = fmax(fmax(kappa, k3), fmax(k4, k5));
-    kappa /= J;
-    const T rho = mass / volume / J;
-    return dx / sqrt(kappa / rho);
+    // c^2 = (kappa / J) / rho with rho = mass / (volume J): the J cancels
+    return dx / sqrt(kappa * volume / mass);
 }
 
 // limit_time_step.rs:126-178

@@ -647,7 +647,7 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     Prepass pre;
     prepass(ps, n_scenes, first, pre);
     if (!pre.err.empty()) return fail("sv_create: " + pre.err);
-    const std::vector<Material> &mats = pre.mats;
+    std::vector<Material> &mats = pre.mats;
     const std::vector<uint32_t> &mat_index = pre.mat_index;
 
     sv_handle *h = new sv_handle();
@@ -757,6 +757,12 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     arena.add(&h->blockmap[0], total), arena.add(&h->blockmap[1], total);
     if ((e = arena.commit(h))) return cuda_fail(e, "particle and work buffers");
     h->n_materials = (uint32_t)mats.size();
+    // the isolated-particle limit of a solid depends on its parameters and
+    // dx only (limit_time_step.rs:137-151): once per material, not per particle
+    for (Material &m : mats)
+        m.iso_limit = m.kind == KIND_FLUID ? adaptive::NONE
+                                           : adaptive::isolated_limit<float>(false, m.mu, m.lambda, 0.f, 0, m.mass,
+                                                                             m.initial_volume, 1.f, L.dx);
     h->host_materials = mats;
     h->host_scenes = scenes;
     // blocks claimed are about n / 200 for bodies of 8 particles per cell;

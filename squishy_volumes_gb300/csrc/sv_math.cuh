@@ -283,7 +283,7 @@ struct Material {
     float xi, theta_c, theta_s;     // snow
     uint32_t use_viscosity;
     uint32_t scene;  // index into the handle's scene table
-    uint32_t pad;
+    float iso_limit; // solids: the isolated-particle time step limit (set once dx is known)
 };
 
 // One independent scene of a handle: its particles are translated by `off`

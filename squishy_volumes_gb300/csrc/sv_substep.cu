@@ -1126,8 +1126,9 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
                             const bool fluid = kind == KIND_FLUID;
                             const float a = adaptive::sound_limit<float>(fluid, mat.mu, mat.lambda, mat.bulk_modulus,
                                                                          mat.exponent, mat.mass, mat.initial_volume, s, dx);
-                            const float b = adaptive::isolated_limit<float>(fluid, mat.mu, mat.lambda, mat.bulk_modulus,
-                                                                            mat.exponent, mat.mass, mat.initial_volume, J, dx);
+                            const float b = fluid ? adaptive::isolated_limit<float>(true, mat.mu, mat.lambda, mat.bulk_modulus,
+                                                                                    mat.exponent, mat.mass, mat.initial_volume, J, dx)
+                                                  : mat.iso_limit;
                             if (a > 0.f && a < adaptive::NONE) lim_sound = fminf(lim_sound, a);
                             if (b > 0.f && b < adaptive::NONE) lim_iso = fminf(lim_iso, b);
                         }
@@ -1301,7 +1302,7 @@ __global__ void __launch_bounds__(ELEM_THREADS)
         const bool fluid = m.kind == KIND_FLUID;
         const float a = adaptive::sound_limit<float>(fluid, m.mu, m.lambda, m.bulk_modulus, m.exponent, m.mass,
                                                      m.initial_volume, S, dx);
-        const float b = adaptive::isolated_limit<float>(fluid, m.mu, m.lambda, m.bulk_modulus, m.exponent, m.mass,
+        const float b = !fluid ? m.iso_limit : adaptive::isolated_limit<float>(true, m.mu, m.lambda, m.bulk_modulus, m.exponent, m.mass,
                                                         m.initial_volume, det3(F), dx);
         if (a > 0.f && a < adaptive::NONE) ls = fminf(ls, a);
         if (b > 0.f && b < adaptive::NONE) li = fminf(li, b);
