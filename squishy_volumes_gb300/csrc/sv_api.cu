@@ -1164,7 +1164,7 @@ int sv_download(sv_handle *h, sv_particles *o) {
     g_last_error.clear();
     if (!h || !o) return fail("sv_download: NULL argument");
     if (o->n != h->n) return fail("sv_download: particle count mismatch");
-    if (h->direct_host) return download_direct(h, o);  // kernels write the caller's arrays (sv_transfer.cu)
+    if (h->direct_host) return download_direct(h, o, 0, h->n);  // kernels write the caller's arrays (sv_transfer.cu)
     const uint64_t n = h->n;
     const ParticleArrays &a = h->side[h->cur];
     std::vector<float4> pos(n), vel(n);
@@ -1188,6 +1188,10 @@ int sv_download_scene(sv_handle *h, uint32_t scene, sv_particles *o) {
     if (scene >= h->host_scenes.size()) return fail("sv_download_scene: no such scene");
     const uint64_t b = h->scene_first[scene], m = h->scene_first[scene + 1] - b;
     if (o->n != m) return fail("sv_download_scene: particle count mismatch");
+    if (h->direct_host) {
+        // the scene's range only, straight into the caller's arrays
+        return download_direct(h, o, b, m);
+    }
     const uint64_t n = h->n;
     std::vector<uint32_t> flags(n), bits(n);
     std::vector<float> x(3 * n), F(9 * n), v(3 * n), C(9 * n), en(n), pj(n);

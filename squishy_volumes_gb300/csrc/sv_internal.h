@@ -323,7 +323,8 @@ cudaError_t upload_direct(sv_handle *h, const sv_particles *ps, uint32_t n_scene
                           const uint32_t *mat_index);
 // the current side into the caller's arrays in the original order; -1 with
 // the last error set on failure
-int download_direct(sv_handle *h, sv_particles *out);
+// particles first .. first + count (original order) into the caller's arrays
+int download_direct(sv_handle *h, sv_particles *out, uint64_t first, uint64_t count);
 
 // ---- host copies of the device state (sv_cache.cu) ----
 // One particle side copied to the host in device (binning) order.

@@ -174,7 +174,8 @@ struct DownloadArgs {
     const SceneInfo *scenes;   // device
     const uint32_t *bits0;     // host: collider bits the particles were created with (no frame input)
     bool stepped;
-    sv_particles o;            // host arrays (NULL ones are skipped)
+    sv_particles o;            // host arrays (NULL ones are skipped) of particles first .. first + count
+    uint64_t first, count;
     uint64_t n;
     uint32_t n_materials;
     double dx;
@@ -194,11 +195,11 @@ __device__ __forceinline__ void flush_rows(float *dst, const float *stage, uint6
 template <bool CELL> __global__ void __launch_bounds__(TPB) k_download(DownloadArgs d) {
     __shared__ float sx[TPB * 3], sv[TPB * 3], sF[TPB * 9], sC[TPB * 9];
     const sv_particles &o = d.o;
-    for (uint64_t i0 = (uint64_t)blockIdx.x * TPB; i0 < d.n; i0 += (uint64_t)gridDim.x * TPB) {
-        const int count = (int)(d.n - i0 < (uint64_t)TPB ? d.n - i0 : (uint64_t)TPB);
+    for (uint64_t i0 = (uint64_t)blockIdx.x * TPB; i0 < d.count; i0 += (uint64_t)gridDim.x * TPB) {
+        const int count = (int)(d.count - i0 < (uint64_t)TPB ? d.count - i0 : (uint64_t)TPB);
         const int t = threadIdx.x;
-        const uint64_t i = i0 + t;
-        const uint64_t s = t < count ? d.inv[i] : d.n;
+        const uint64_t i = i0 + t;  // in the caller's arrays; original particle d.first + i
+        const uint64_t s = t < count ? d.inv[d.first + i] : d.n;
         if (s < d.n) {  // else unset (reported through the flag of k_invert) or past the end
             const float4 p = d.a.pos[s], v = d.a.vel[s];
             const uint32_t packed = __float_as_uint(p.w);
@@ -226,7 +227,7 @@ template <bool CELL> __global__ void __launch_bounds__(TPB) k_download(DownloadA
                 // without colliders every substep's Collide clears a live
                 // particle's bits (collide.rs:53-56)
                 if (d.a.cbits_done) o.collider_bits[i] = d.a.cbits_done[s];
-                else o.collider_bits[i] = (d.stepped && !(packed & SV_TOMBSTONED)) ? 0u : (d.bits0 ? d.bits0[i] : 0u);
+                else o.collider_bits[i] = (d.stepped && !(packed & SV_TOMBSTONED)) ? 0u : (d.bits0 ? d.bits0[d.first + i] : 0u);
             }
         } else if (t < count) {
             // an unset row keeps what the caller's array held
@@ -349,16 +350,16 @@ cudaError_t upload_direct(sv_handle *h, const sv_particles *ps, uint32_t n_scene
     return e;
 }
 
-int download_direct(sv_handle *h, sv_particles *o) {
+int download_direct(sv_handle *h, sv_particles *o, uint64_t first, uint64_t count) {
     const uint64_t n = h->n;
-    if (n == 0) return 0;
+    if (n == 0 || count == 0) return 0;
     cudaError_t e;
     uint32_t *bad = h->counters + C_TRANSFER_BAD;  // an original index out of range or repeated
     DownloadArgs d;
     d.a = h->side[h->cur], d.inv = h->inv, d.mats = h->materials, d.scenes = h->scenes;
     d.bits0 = h->collider_bits.empty() ? nullptr : h->collider_bits.data();
     d.stepped = h->substeps_total > 0;
-    d.o = *o, d.n = n, d.n_materials = h->n_materials, d.dx = h->layout.dx;
+    d.o = *o, d.first = first, d.count = count, d.n = n, d.n_materials = h->n_materials, d.dx = h->layout.dx;
     // unset entries (a corrupt state) stay 0xFFFFFFFF and are skipped
     if ((e = cudaMemsetAsync(bad, 0, 4, h->stream)) != cudaSuccess ||
         (e = cudaMemsetAsync(h->inv, 0xFF, n * 4, h->stream)) != cudaSuccess) {
@@ -371,13 +372,13 @@ int download_direct(sv_handle *h, sv_particles *o) {
         auto add = [&](void *p, size_t bytes) {
             if (p) out.push_back({p, bytes});
         };
-        add(o->flags, n * 4), add(o->positions, n * 12), add(o->position_gradients, n * 36);
-        add(o->velocities, n * 12), add(o->velocity_gradients, n * 36), add(o->elastic_energies, n * 4);
-        add(o->collider_bits, n * 4), add(o->plastic_j, n * 4);
+        add(o->flags, count * 4), add(o->positions, count * 12), add(o->position_gradients, count * 36);
+        add(o->velocities, count * 12), add(o->velocity_gradients, count * 36), add(o->elastic_energies, count * 4);
+        add(o->collider_bits, count * 4), add(o->plastic_j, count * 4);
         populate(out);  // overlaps k_invert
     }
-    if (h->layout.position_form == 1) k_download<true><<<blocks_for(n), TPB, 0, h->stream>>>(d);
-    else k_download<false><<<blocks_for(n), TPB, 0, h->stream>>>(d);
+    if (h->layout.position_form == 1) k_download<true><<<blocks_for(count), TPB, 0, h->stream>>>(d);
+    else k_download<false><<<blocks_for(count), TPB, 0, h->stream>>>(d);
     h->launches += 2;
     uint32_t flag = 0;
     if ((e = cudaGetLastError()) != cudaSuccess ||
