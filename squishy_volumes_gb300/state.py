@@ -626,9 +626,17 @@ class BatchedCudaState(CudaState):
     launches advances them all.  Not in the reference, whose backend holds
     one scene; each scene keeps its own domain and cull bounds."""
 
+    # what downloads take from the creating particles (the rest comes from
+    # the device)
+    _TEMPLATE_FIELDS = ("mass", "initial_volume", "mu", "lambda_", "sand_alpha", "exponent", "bulk_modulus",
+                        "viscosity_dynamic", "viscosity_bulk", "model", "hardening", "crit_compression",
+                        "crit_stretch", "initial_positions")
+
     def __init__(self, handle, counts, consts_list, extras, particles_list):
         total = sum(counts)
-        merged = _concat([p for p in particles_list])
+        # only the parameter arrays are merged: concatenating every state
+        # array too cost about a quarter of a second for 7.5M particles
+        merged = _concat_fields(particles_list, self._TEMPLATE_FIELDS)
         super().__init__(handle, total, 0.0, consts_list[0], extras, merged.initial_positions, merged)
         self.counts = list(counts)
         self.first = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
@@ -667,14 +675,13 @@ class BatchedCudaState(CudaState):
         return out
 
 
-def _concat(parts):
-    from dataclasses import fields as _fields
+def _concat_fields(parts, names):
+    """The named fields of every part concatenated (None where any part has
+    none), as attributes of a plain namespace."""
+    from types import SimpleNamespace
 
     out = {}
-    for f in _fields(Particles):
-        vals = [getattr(p, f.name) for p in parts]
-        if any(v is None for v in vals):
-            out[f.name] = None if all(v is None for v in vals) else None
-        else:
-            out[f.name] = np.concatenate(vals) if vals else None
-    return Particles(**out)
+    for name in names:
+        vals = [getattr(p, name) for p in parts]
+        out[name] = None if any(v is None for v in vals) else np.concatenate(vals)
+    return SimpleNamespace(**out)
