@@ -96,21 +96,6 @@ struct MaterialHash {
 
 int build_material(const sv_particles *p, uint64_t i, Material &m, std::string &err);
 
-// Particle i > 0 of a scene has the same flags and parameter words as
-// particle i - 1, so it has the same material and passes the same checks.
-// Bodies are made of runs of identical parameters, and this comparison
-// costs a fraction of build_material.
-bool same_as_previous(const sv_particles *p, uint64_t i) {
-    auto eq = [i](const void *a) {
-        if (!a) return true;
-        const uint32_t *w = static_cast<const uint32_t *>(a);
-        return w[i] == w[i - 1];
-    };
-    return p->flags[i] == p->flags[i - 1] && eq(p->mass) && eq(p->initial_volume) && eq(p->model) &&
-           eq(p->mu) && eq(p->lambda) && eq(p->sand_alpha) && eq(p->exponent) && eq(p->bulk_modulus) &&
-           eq(p->viscosity_dynamic) && eq(p->viscosity_bulk) && eq(p->hardening) && eq(p->crit_compression) &&
-           eq(p->crit_stretch);
-}
 
 // The host pass of sv_create over host threads: per particle its material
 // (deduplicated ParticleParameters, numbered in order of first appearance
@@ -151,45 +136,72 @@ void prepass(const sv_particles *ps, uint32_t n_scenes, const std::vector<uint64
         uint64_t g0, g1;
         range(t, g0, g1);
         uint32_t s = (uint32_t)(std::upper_bound(first.begin(), first.end(), g0) - first.begin()) - 1;
-        for (uint64_t g = g0; g < g1; ++g) {
-            while (g >= first[s + 1]) ++s;
+        uint32_t *mat_index = out.mat_index.data();
+        // one scene's run of this part at a time, its arrays and bounds in locals
+        for (uint64_t a = g0; a < g1; ++s) {
+            while (a >= first[s + 1]) ++s;
             const sv_particles *p = &ps[s];
-            const uint64_t i = g - first[s];
-            if (p->collider_bits && p->collider_bits[i]) pt.any_bits = true;
-            if (!(p->flags[i] & SV_TOMBSTONED)) {
-                for (int a = 0; a < 3; ++a) {
-                    const double x = p->positions[3 * i + a];
-                    if (!std::isfinite(x)) pt.nonfinite = true;
-                    pt.lo[s][a] = std::min(pt.lo[s][a], x), pt.hi[s][a] = std::max(pt.hi[s][a], x);
+            const uint64_t b = std::min<uint64_t>(g1, first[s + 1]), base = first[s];
+            const uint32_t *flags = p->flags, *bits = p->collider_bits;
+            const float *pos = p->positions;
+            // the parameter words same_as_previous compares, non-NULL ones only
+            const uint32_t *words[13];
+            int nw = 0;
+            for (const void *q : {(const void *)p->mass, (const void *)p->initial_volume, (const void *)p->model,
+                                  (const void *)p->mu, (const void *)p->lambda, (const void *)p->sand_alpha,
+                                  (const void *)p->exponent, (const void *)p->bulk_modulus,
+                                  (const void *)p->viscosity_dynamic, (const void *)p->viscosity_bulk,
+                                  (const void *)p->hardening, (const void *)p->crit_compression,
+                                  (const void *)p->crit_stretch})
+                if (q) words[nw++] = static_cast<const uint32_t *>(q);
+            double lo[3] = {pt.lo[s][0], pt.lo[s][1], pt.lo[s][2]}, hi[3] = {pt.hi[s][0], pt.hi[s][1], pt.hi[s][2]};
+            bool nonfinite = false, any_bits = false;
+            for (uint64_t g = a; g < b; ++g) {
+                const uint64_t i = g - base;
+                if (bits && bits[i]) any_bits = true;
+                const uint32_t f = flags[i];
+                if (!(f & SV_TOMBSTONED)) {
+                    for (int c = 0; c < 3; ++c) {
+                        const double x = pos[3 * i + c];
+                        nonfinite |= !std::isfinite(x);
+                        lo[c] = std::min(lo[c], x), hi[c] = std::max(hi[c], x);
+                    }
                 }
+                // the previous particle (same scene, this part) had the material prev_idx
+                if (prev_idx != UINT32_MAX && g > a && f == flags[i - 1]) {
+                    bool same = true;
+                    for (int k = 0; k < nw && same; ++k) same = words[k][i] == words[k][i - 1];
+                    if (same) {
+                        mat_index[g] = prev_idx;
+                        continue;
+                    }
+                }
+                Material m;
+                std::string err;
+                if (build_material(p, i, m, err)) {
+                    pt.err_at = g, pt.err = err;
+                    return;
+                }
+                m.scene = s;
+                if (prev_idx != UINT32_MAX && std::memcmp(&m, &prev, sizeof(m)) == 0) {
+                    mat_index[g] = prev_idx;
+                    continue;
+                }
+                auto it = index.find(MaterialKey{m});
+                uint32_t idx;
+                if (it == index.end()) {
+                    idx = (uint32_t)pt.mats.size();
+                    index.emplace(MaterialKey{m}, idx);
+                    pt.mats.push_back(m);
+                } else {
+                    idx = it->second;
+                }
+                mat_index[g] = idx;  // local to the part until the merge
+                prev = m, prev_idx = idx;
             }
-            // the previous particle (same scene, this part) had the material prev_idx
-            if (prev_idx != UINT32_MAX && i > 0 && g > g0 && g - 1 >= first[s] && same_as_previous(p, i)) {
-                out.mat_index[g] = prev_idx;
-                continue;
-            }
-            Material m;
-            std::string err;
-            if (build_material(p, i, m, err)) {
-                pt.err_at = g, pt.err = err;
-                return;
-            }
-            m.scene = s;
-            if (prev_idx != UINT32_MAX && std::memcmp(&m, &prev, sizeof(m)) == 0) {
-                out.mat_index[g] = prev_idx;
-                continue;
-            }
-            auto it = index.find(MaterialKey{m});
-            uint32_t idx;
-            if (it == index.end()) {
-                idx = (uint32_t)pt.mats.size();
-                index.emplace(MaterialKey{m}, idx);
-                pt.mats.push_back(m);
-            } else {
-                idx = it->second;
-            }
-            out.mat_index[g] = idx;  // local to the part until the merge
-            prev = m, prev_idx = idx;
+            for (int c = 0; c < 3; ++c) pt.lo[s][c] = lo[c], pt.hi[s][c] = hi[c];
+            pt.nonfinite |= nonfinite, pt.any_bits |= any_bits;
+            a = b;
         }
     };
     auto run = [&](auto &&fn) {
