@@ -1020,6 +1020,8 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
     uint32_t status = 0;
     h->adaptive_active = true;
     const bool fused = !h->fin_active;  // with a frame input the substep runs split
+    double t_now = st.time;        // device time after the last batch
+    float dt_last = max_time_step; // its last advance step
     int rc = 0;
     while (true) {
         if (cancel && *cancel) {
@@ -1036,11 +1038,20 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
         if (!use_fused && h->adt_split_batches > 0) h->adt_split_batches -= 1;
         if (!use_fused) h->pending_valid = false;  // the split form scatters each substep itself
         const uint32_t miss0 = h->host_counters[C_ADT_MISS], done0 = h->host_counters[C_SUBSTEPS];
-        for (uint32_t s = 0; s < 16 && rc == 0;) {
+        // Substeps queued past the target run stopped, yet each still copies
+        // the particle state through its passes: queue what the remaining
+        // time needs at the last step taken (at most 16; more batches follow
+        // when the steps shrink).
+        uint32_t want = 16;
+        if (dt_last > 0.f) {
+            const double need = std::ceil((target_time - t_now) / (double)dt_last - 1e-9);
+            want = (uint32_t)std::min(16.0, std::max(1.0, need));
+        }
+        for (uint32_t s = 0; s < want && rc == 0;) {
             // whole binning periods of the fused form replay CUDA graphs, as
             // in sv_step
             if (use_fused && h->use_graphs && !h->profiling && h->pending_valid && h->keys_valid &&
-                h->since_sort >= h->sort_interval && 16 - s >= h->sort_interval) {
+                h->since_sort >= h->sort_interval && want - s >= h->sort_interval) {
                 rc = run_period_graph(h, 0.f, g, true);
                 s += h->sort_interval;
             } else {
@@ -1049,7 +1060,13 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
                 s += 1;
             }
         }
-        if (rc || read_counters(h)) {
+        if (rc == 0) {
+            adaptive::State now;
+            if (cudaMemcpyAsync(&now, h->adt, sizeof(now), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) rc = -1;
+            if (rc == 0 && read_counters(h)) rc = -1;  // synchronises the copy too
+            if (rc == 0) t_now = now.time, dt_last = now.dt_c;
+        }
+        if (rc) {
             rc = -1;
             break;
         }
