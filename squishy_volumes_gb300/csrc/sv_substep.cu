@@ -605,9 +605,10 @@ __device__ __forceinline__ void scatter_records(Shared &sh, int count, const Ste
     const uint32_t gmask = __ballot_sync(0xffffffffu, key == REC_GLOBAL);
     const uint32_t cmask = __ballot_sync(0xffffffffu, key == REC_VARIANT);
     float2 amx = make_float2(0.f, 0.f), ayz = make_float2(0.f, 0.f);
-    // unrolled by 8: the whole-warp unroll grows the kernel past the
-    // instruction cache for no gain
-#pragma unroll 8
+    // unrolled by 4 (measured against 1, 2 and 8: by 8 the kernel grows and
+    // misses the instruction cache, 2.7 % slower on the 1M three-box scene;
+    // by 2 and 1 the 8M dam break is 0.7 and 3 % slower)
+#pragma unroll 4
     for (int r = 0; r < 32; ++r) {
         if ((vmask >> r) & 1u) {
             const float4 p0 = sh.rec[r0 + r].p[li], p1 = sh.rec[r0 + r].p[3 + lj], p2 = sh.rec[r0 + r].p[6 + lk];
