@@ -5,7 +5,9 @@ over a 256^3 domain (fixed-corotated, snow and Drucker-Prager sand boxes,
 dt = 5e-5), synthetic and seeded.  A "step" is one substep over all particles.
 
   value        particle-substeps/s with the state resident in HBM (CUDA events
-               around K substeps on the library's stream)
+               around K substeps on the library's stream; the K-substep
+               region is repeated until the repeats cover --min-seconds and
+               the median repeat is reported)
   e2e          the same metric through the C ABI with host buffers: per e2e step
                sv_create (host->device upload of the state), one frame of
                substeps (1/24 s of simulated time), sv_download (device->host)
@@ -15,6 +17,11 @@ dt = 5e-5), synthetic and seeded.  A "step" is one substep over all particles.
                all host threads) on a bounded sample of the same scene
   adaptive     (--adaptive) sv_step_adaptive over the simulated time of K
                substeps, the scene's dt as the largest step
+  error_vs_fp64  --error-substeps substeps (default 3) from the initial state
+               on the GPU and on the fp64 CPU oracle: relative errors of x, v,
+               C and F
+  secondary    the 8M-particle dam break (--secondary), measured the same way:
+               its own value, roofline, e2e and error against fp64
 
 --impl reference runs only the CPU restatement of the reference substep (the
 reference itself is Rust and cannot be built here) on the same scene.
@@ -62,9 +69,14 @@ def parse():
     ap.add_argument("--bake", type=int, default=0,
                     help="also time this many whole frames with a frame-cache store after each, against the same "
                          "frames without stores")
-    ap.add_argument("--error-substeps", type=int, default=0,
+    ap.add_argument("--error-substeps", type=int, default=3,
                     help="also run this many substeps from the initial state on the GPU and on the fp64 CPU oracle "
-                         "and report the relative errors of x, v, C, F")
+                         "and report the relative errors of x, v, C, F (0: off)")
+    ap.add_argument("--secondary", default="dam_break_8m",
+                    help="a second workload measured the same way and reported under 'secondary' ('' for none)")
+    ap.add_argument("--min-seconds", type=float, default=0.5,
+                    help="repeat the K-substep timed region until the repeats cover this long; the median is reported")
+    ap.add_argument("--max-repeats", type=int, default=2000)
     return ap.parse_args()
 
 
@@ -273,18 +285,33 @@ def algorithmic_bytes(kernel: str, live: int, grid_nodes: int, cell_form: bool):
     return None
 
 
-def run_ours(args, rank, world, local):
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def _max_over_ranks(x, world, dev):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def measure_scene(args, name, rank, world, local, dev, primary):
+    """One workload: the timed region, the per-kernel roofline, the e2e run
+    through the C ABI with host buffers and the error against the fp64
+    oracle.  Returns the fields of the bench line for it."""
     import torch
 
     from squishy_volumes_gb300 import CudaState, FrameInput, Harness, RunParameters, scenes
 
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=dev)
-    made = scenes.SCENES[args.scene]()
+    made = scenes.SCENES[name]()
     if isinstance(made, list):
         # batched configuration: every scene in one handle; the CPU baseline
         # and the fp64 error report use the largest scene alone
@@ -304,92 +331,57 @@ def run_ours(args, rank, world, local):
         scene.extras.sort_interval = args.sort_interval
         make_gpu = lambda: CudaState.from_io_state(scene.io_state, scene.consts, scene.extras)
         h2d_particles = [scene.io_state.particles]
-    p = scene.io_state.particles
     gpu = make_gpu()
     # All work, warm-up included, is queued on a torch stream handed to the
     # library (the CUDA graphs of the binning periods are captured on it).
     stream = torch.cuda.Stream(device=dev)
     gpu.set_stream(stream.cuda_stream)
     closure_info = None
-    if args.closure == "learned":
-        # training data from plain substeps of this scene, then the GPU
-        # training loop; none of this is inside the timed region
-        t0 = time.perf_counter()
-        pool = 0
-        for k in range(8):
-            gpu.step(20, scene.dt, scene.gravity)
-            pool = gpu.closure_harvest(scene.dt, 60000, 0.02, seed=k)
-        t1 = time.perf_counter()
-        loss = gpu.closure_train(4000, 8192, 3e-3, seed=1)
-        torch.cuda.synchronize()
-        t2 = time.perf_counter()
-        ev = gpu.closure_evaluate(scene.dt)
-        gpu.closure_set_mode(1)
-        closure_info = {"mode": "learned", "pool": pool, "harvest_s": round(t1 - t0, 3),
-                        "train_s": round(t2 - t1, 3), "train_iterations": 4000, "loss": loss,
-                        "stress_rel_err_learned": ev["stress_err_learned"],
-                        "stress_rel_err_plain_fp32": ev["stress_err_plain32"],
-                        "projected_f_rel_err_learned": ev["f_err_learned"],
-                        "fallback_fraction": ev["fallbacks"] / max(ev["particles"], 1.0)}
+    if primary and args.closure == "learned":
+        closure_info = train_closure(gpu, scene, args)
     tuned = None
     if args.autotune:
         tuned = gpu.autotune(scene.dt, scene.gravity, 16)
     gpu.set_graphs(not args.no_graphs)
-    # warm-up
     status, done = gpu.step(args.warmup, scene.dt, scene.gravity)
     if status:
         raise RuntimeError(f"warm-up status {status:#x}")
     torch.cuda.synchronize()
-    stats0 = gpu.stats()
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
-
-    # timed region: K substeps bracketed by CUDA events recorded on the
-    # library's stream
+    # Timed region: K substeps bracketed by CUDA events recorded on the
+    # library's stream, with a barrier and a synchronize on both sides.  It
+    # is repeated until the repeats cover at least --min-seconds (so that the
+    # clock sampler sees the GPU under load), and the median repeat is
+    # reported; the state keeps evolving from repeat to repeat.
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
+    reps = []
+    stats0 = gpu.stats()
     with ClockSampler(local) as clocks:
-        barrier()
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        status, done = gpu.step(args.steps, scene.dt, scene.gravity)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-    elapsed = ev0.elapsed_time(ev1) * 1e-3
+        while True:
+            _barrier(world)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            status, done = gpu.step(args.steps, scene.dt, scene.gravity)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            _barrier(world)
+            if status or done != args.steps:
+                raise RuntimeError(f"timed run status {status:#x}, done {done}")
+            reps.append(_max_over_ranks(ev0.elapsed_time(ev1) * 1e-3, world, dev))
+            if (sum(reps) >= args.min_seconds and len(reps) >= 3) or len(reps) >= args.max_repeats:
+                break
     stats1 = gpu.stats()
-    if status or done != args.steps:
-        raise RuntimeError(f"timed run status {status:#x}, done {done}")
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = float(np.median(reps))
     live = stats1["live_particles"]
     value = live * args.steps * world / elapsed
-    launches = stats1["kernel_launches"] - stats0["kernel_launches"]
+    launches = (stats1["kernel_launches"] - stats0["kernel_launches"]) / len(reps)
     if closure_info is not None:
-        # the same K substeps with the return maps, from the state reached
-        closure_info["learned_fraction"] = (stats1["closure_learned"] - stats0["closure_learned"]) / max(
-            1, live * args.steps)
-        gpu.closure_set_mode(0)
-        gpu.step(args.warmup, scene.dt, scene.gravity)
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        gpu.step(args.steps, scene.dt, scene.gravity)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        closure_info["plain_value"] = live * args.steps * world / (ev0.elapsed_time(ev1) * 1e-3)
-        closure_info["learned_over_plain"] = value / closure_info["plain_value"]
-        gpu.closure_set_mode(1)
+        closure_info.update(compare_closure(gpu, scene, args, stream, value, live, world, stats0, stats1))
 
-    # per-kernel durations: the same K substeps again with CUDA events around
-    # every kernel group on the library's stream
+    # per-kernel durations: K more substeps right after the timed region,
+    # with CUDA events around every kernel group on the library's stream
+    # (direct launches: events cannot sit inside a replayed graph)
     gpu.set_profiling(True)
     gpu.step(args.steps, scene.dt, scene.gravity)
     prof = json.loads(gpu.profile_report())
@@ -407,7 +399,7 @@ def run_ours(args, rank, world, local):
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
         try:
-            traffic = json.loads(tfile.read_text()).get(args.scene, {}).get(dom)
+            traffic = json.loads(tfile.read_text()).get(name, {}).get(dom)
         except Exception:
             traffic = None
     roofline = {
@@ -419,6 +411,7 @@ def run_ours(args, rank, world, local):
         "unit": "GB/s",
         "frac": round(achieved / hbm, 4) if achieved else None,
         "traffic": traffic,
+        "bytes_per_launch": int(alg) if alg else None,
         "share": round(prof[dom]["ms"] / total_ms, 4),
         "kernels_ms_per_substep": {k: round(v["ms"] / args.steps, 5) for k, v in prof.items()},
     }
@@ -436,7 +429,7 @@ def run_ours(args, rank, world, local):
     # adaptive time steps (sv_step_adaptive) over the time K fixed substeps
     # span, from the state reached, the scene's dt as the largest step
     adaptive = None
-    if args.adaptive and batch is None:
+    if primary and args.adaptive and batch is None:
         gpu.step_adaptive(gpu.time + args.warmup * scene.dt * (1 - 1e-6), scene.dt, scene.gravity)
         sa0 = gpu.stats()
         torch.cuda.synchronize()
@@ -457,6 +450,7 @@ def run_ours(args, rank, world, local):
             "graph_replays": sa1["graph_replays"] - sa0["graph_replays"],
             "max_time_step": scene.dt,
         }
+    gpu.close()
 
     # end to end through the C ABI with host buffers
     e2e = None
@@ -464,11 +458,11 @@ def run_ours(args, rank, world, local):
         fps = scene.consts.frames_per_second
         frame_substeps = int(math.ceil((1.0 / fps) / scene.dt))
         frame_substeps = min(frame_substeps, scene.substeps)
-        reps = 2
+        reps_e2e = 2
         h2d = sum(q.nbytes() for q in h2d_particles)
         d2h = 0
         t0 = time.perf_counter()
-        for _ in range(reps):
+        for _ in range(reps_e2e):
             st_ = make_gpu()
             params = RunParameters(target_time=frame_substeps * scene.dt * (1 - 1e-9), max_time_step=scene.dt)
             io, err = st_.produce_next_state(Harness(), FrameInput(scene.consts, scene.gravity), params)
@@ -478,7 +472,7 @@ def run_ours(args, rank, world, local):
             st_.close()
         t1 = time.perf_counter()
         e2e = {
-            "value": n * frame_substeps * reps / (t1 - t0),
+            "value": n * frame_substeps * reps_e2e / (t1 - t0),
             "unit": METRIC,
             "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h),
@@ -487,55 +481,142 @@ def run_ours(args, rank, world, local):
         }
 
     bake = None
-    if args.bake > 0 and rank == 0:
+    if primary and args.bake > 0 and rank == 0:
         bake = bake_frames(scene, make_gpu, args.bake)
 
     error = None
     if args.error_substeps > 0 and rank == 0:
         error = error_vs_fp64(scene, args.error_substeps)
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        gpu.close()
-        cpu = cpu_baseline(scene, args.cpu_seconds)
-    line = {
-        "metric": METRIC,
+    config = {
+        "workload": name,
+        "particles": n,
+        "scenes": len(batch) if batch else 1,
+        "live_particles": live,
+        "grid_blocks": st["grid_blocks"],
+        "binning_sort_interval": st["sort_interval"],
+        "binning_sorts_in_timed_region": int(stats1["sorts"] - stats0["sorts"]),
+        "graph_replays_in_timed_region": int(stats1["graph_replays"] - stats0["graph_replays"]),
+        "timed_repeats": len(reps),
+        "timed_seconds_total": round(sum(reps), 4),
+        "ms_per_step_min_median_max": [round(min(reps) / args.steps * 1e3, 5), round(elapsed / args.steps * 1e3, 5),
+                                       round(max(reps) / args.steps * 1e3, 5)],
+        "cta_per_sm": st["cta_per_sm"],
+        "tile_miss_fraction": round((stats1["tile_misses"] - stats0["tile_misses"]) /
+                                    max(1, live * args.steps * len(reps)), 5),
+        "autotuned": tuned,
+        "substep_dt": scene.dt,
+        "position_form": "int32 cell + fp32 offset" if cell_form else "fp32",
+        "l2": "state larger than L2 (no flush)",
+        "parallelism": "replicas" if world > 1 else "single GPU",
+    }
+    return {
         "value": value,
-        "unit": METRIC,
-        "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
         "ms_per_step": elapsed / args.steps * 1e3,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32",
-        "data": "synthetic (seeded jittered boxes)",
-        "config": {
-            "workload": args.scene,
-            "particles": n,
-            "scenes": len(batch) if batch else 1,
-            "live_particles": live,
-            "grid_blocks": st["grid_blocks"],
-            "binning_sort_interval": st["sort_interval"],
-            "binning_sorts_in_timed_region": int(stats1["sorts"] - stats0["sorts"]),
-            "graph_replays_in_timed_region": int(stats1["graph_replays"] - stats0["graph_replays"]),
-            "cta_per_sm": st["cta_per_sm"],
-            "autotuned": tuned,
-            "substep_dt": scene.dt,
-            "l2": "state larger than L2 (no flush)",
-            "parallelism": "replicas" if world > 1 else "single GPU",
-        },
+        "config": config,
         "roofline": roofline,
-        "cpu_baseline": cpu,
         "e2e": e2e,
         "adaptive": adaptive,
-        "gpu_launches": int(launches),
+        "gpu_launches": int(round(launches)),
         "clocks": clocks.summary(),
         "fp64_svd_particles": st["fp64_svd"],
         "error_vs_fp64": error,
         "closure": closure_info,
         "bake": bake,
+        "scene": scene,
+    }
+
+
+def train_closure(gpu, scene, args):
+    """Training data from plain substeps of the scene, then the GPU training
+    loop; none of this is inside the timed region."""
+    import torch
+
+    t0 = time.perf_counter()
+    pool = 0
+    for k in range(8):
+        gpu.step(20, scene.dt, scene.gravity)
+        pool = gpu.closure_harvest(scene.dt, 60000, 0.02, seed=k)
+    t1 = time.perf_counter()
+    loss = gpu.closure_train(4000, 8192, 3e-3, seed=1)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    ev = gpu.closure_evaluate(scene.dt)
+    gpu.closure_set_mode(1)
+    return {"mode": "learned", "pool": pool, "harvest_s": round(t1 - t0, 3),
+            "train_s": round(t2 - t1, 3), "train_iterations": 4000, "loss": loss,
+            "stress_rel_err_learned": ev["stress_err_learned"],
+            "stress_rel_err_plain_fp32": ev["stress_err_plain32"],
+            "projected_f_rel_err_learned": ev["f_err_learned"],
+            "fallback_fraction": ev["fallbacks"] / max(ev["particles"], 1.0)}
+
+
+def compare_closure(gpu, scene, args, stream, value, live, world, stats0, stats1):
+    """The same K substeps with the return maps, from the state reached."""
+    import torch
+
+    out = {"learned_fraction": (stats1["closure_learned"] - stats0["closure_learned"]) / max(1, live * args.steps)}
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    gpu.closure_set_mode(0)
+    gpu.step(args.warmup, scene.dt, scene.gravity)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    gpu.step(args.steps, scene.dt, scene.gravity)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    out["plain_value"] = live * args.steps * world / (ev0.elapsed_time(ev1) * 1e-3)
+    out["learned_over_plain"] = value / out["plain_value"]
+    gpu.closure_set_mode(1)
+    return out
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    main = measure_scene(args, args.scene, rank, world, local, dev, primary=True)
+    scene = main.pop("scene")
+    secondary = None
+    if args.secondary and args.secondary != args.scene:
+        sec = measure_scene(args, args.secondary, rank, world, local, dev, primary=False)
+        sec.pop("scene")
+        secondary = {k: sec[k] for k in ("value", "ms_per_step", "config", "roofline", "e2e", "gpu_launches",
+                                         "clocks", "fp64_svd_particles", "error_vs_fp64")}
+        secondary["unit"] = METRIC
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(scene, args.cpu_seconds)
+    line = {
+        "metric": METRIC,
+        "value": main["value"],
+        "unit": METRIC,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": main["ms_per_step"],
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded jittered boxes)",
+        "config": main["config"],
+        "roofline": main["roofline"],
+        "cpu_baseline": cpu,
+        "e2e": main["e2e"],
+        "adaptive": main["adaptive"],
+        "gpu_launches": main["gpu_launches"],
+        "clocks": main["clocks"],
+        "fp64_svd_particles": main["fp64_svd_particles"],
+        "error_vs_fp64": main["error_vs_fp64"],
+        "closure": main["closure"],
+        "bake": main["bake"],
+        "secondary": secondary,
     }
     if rank == 0:
         print(json.dumps(line))

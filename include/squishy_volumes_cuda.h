@@ -52,6 +52,14 @@ extern "C" {
 #define SV_STATUS_CAPACITY_EXCEEDED (1u << 0) /* grid block capacity too small */
 #define SV_STATUS_PARTICLE_INVERTED (1u << 3) /* det F <= 0: FAILED set */
 #define SV_STATUS_CANCELED (1u << 8)          /* cancel flag seen between substeps */
+/* A sand particle (SV_USE_SAND_ALPHA) with mu <= 0 reached the compressive
+ * branch of the Drucker-Prager return map, where the reference asserts
+ * mu > 0 (rust/crates/cpu/src/phase/advance_particles.rs:57) and its compute
+ * thread panics.  That particle keeps its unprojected F for the substep, the
+ * substeps after it do not run, and sv_step / sv_step_adaptive return -1
+ * with this bit in *status_out.  In expansion mu <= 0 is valid: F becomes
+ * U V^T as in the reference. */
+#define SV_STATUS_SAND_INVALID_MU (1u << 11)
 
 /* Material models.  SV_MODEL_REFERENCE selects what the reference does from
  * the flags: Neo-Hookean solid (plus the sand return map with
@@ -89,7 +97,17 @@ typedef struct sv_consts {
      * device can access pageable memory (a Grace host over NVLink-C2C), else
      * staged copies; 1 = staged copies always.  Same results either way. */
     uint32_t host_transfer;
-    uint32_t reserved[4];
+    /* Addition: 1 = deterministic P2G.  Every substep bins the particles by
+     * (cell, original index) and gathers each grid node's mass and momentum
+     * in one fixed order: the 27 base cells around the node in lexicographic
+     * order, then each cell's particles in ascending original index, left to
+     * right in fp32.  The node masses then equal, bit for bit, the
+     * reference's P2G mass (scatter_momentum.rs:22-93) summed in that order,
+     * and every run of the same input gives the same bits.  Several times
+     * slower than the default scatter; fp32 positions (position_form 0), no
+     * frame input and no learned closure. */
+    uint32_t deterministic_p2g;
+    uint32_t reserved[3];
 } sv_consts;
 
 typedef struct sv_particles {
@@ -130,9 +148,14 @@ int sv_create(const sv_consts *consts, const sv_particles *particles, sv_handle 
 /* The substep loop of CpuState::produce_next_state (cpu_state.rs:167-194)
  * with adaptive_time_steps = false: n_substeps substeps of size dt with the
  * given (already interpolated) gravity.  `cancel` may be NULL; when it points
- * at a nonzero value between substeps, the call stops (Harness::check,
- * xpu/src/harness.rs:69-75) and reports SV_STATUS_CANCELED.  The number of
- * substeps completed is written to *substeps_done when that is not NULL. */
+ * at a nonzero value the call stops (Harness::check, xpu/src/harness.rs:69-75)
+ * and reports SV_STATUS_CANCELED.  Substeps are queued in chunks (16 when
+ * `cancel` is given, 64 otherwise) and the host waits for each chunk by
+ * polling it every 50 us, checking `cancel` meanwhile, like the reference's
+ * GPU backend waits (gpu_state.rs:509-522): a cancel set from another thread
+ * during a call takes effect once the chunk in flight has completed, and the
+ * state stays that of the last completed substep.  The number of substeps
+ * completed is written to *substeps_done when that is not NULL. */
 int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
             const volatile int32_t *cancel, uint32_t *status_out, uint32_t *substeps_done);
 
@@ -193,10 +216,13 @@ int sv_sort_pairs(const uint32_t *keys, uint32_t *perm, uint64_t n);
 /* No counterpart in the reference.  The same stable sort as sv_sort_pairs,
  * for callers that must not allocate device memory: a plugin running inside
  * a host application that hands out the whole device-memory budget from its
- * own pool, or code that records its work into a CUDA graph, where a
- * cudaMalloc would break the budget or the capture.  It allocates nothing:
- * its scratch is one fixed array of about 13 MB compiled into the library,
- * which every GPU that loads the library holds until the process exits.
+ * own pool (an allocation behind the pool's back breaks its accounting), or
+ * a loop with a fixed time budget per iteration that cannot take the
+ * device-wide synchronisation a cudaMalloc / cudaFree may cause.  It
+ * allocates nothing: its scratch is one fixed array of
+ * SV_NOALLOC_SCRATCH_BYTES (16,777,984 bytes, about 16.8 MB) compiled into
+ * the library, which every GPU that loads the library holds until the
+ * process exits.
  *  - keys and perm are DEVICE pointers to n uint32 each, owned by the
  *    caller; perm receives the permutation that stably sorts keys.
  *  - n may be at most SV_NOALLOC_MAX_KEYS; larger n is rejected with an
@@ -212,6 +238,7 @@ int sv_sort_pairs(const uint32_t *keys, uint32_t *perm, uint64_t n);
  *    calls: every value in it is written before it is read.
  *  - Returns 0, or -1 with a message copied into error[0..error_capacity). */
 #define SV_NOALLOC_MAX_KEYS (1u << 20)
+#define SV_NOALLOC_SCRATCH_BYTES 16777984u
 int sv_sort_pairs_noalloc(const uint32_t *keys, uint32_t *perm, uint64_t n, void *stream, char *error,
                           uint64_t error_capacity);
 
@@ -234,6 +261,14 @@ typedef struct sv_stats {
     uint64_t closure_mode;      /* 0 return maps, 1 learned closure */
     uint64_t adaptive_misses;   /* adaptive substeps whose speculative steps failed and were redone */
     uint64_t adaptive_split;    /* adaptive substeps queued in the split form */
+    /* Conservation sums of the grid the last substep gathered from, taken
+     * on the device in fp64 over its nodes in momentum form, before
+     * momentum -> velocity (collider variants included): the total mass and
+     * momentum that the P2G scattered.  Equal to the particles' sum of m and
+     * m v + (the APIC term, which sums to zero) up to fp32 rounding of the
+     * node values. */
+    double grid_mass;
+    double grid_momentum[3];
 } sv_stats;
 
 /* Adaptive time steps: CpuState::produce_next_state with
@@ -377,6 +412,15 @@ int sv_closure_harvest(sv_handle *h, float dt, uint32_t max_samples, float augme
                        uint64_t *total_out);
 int sv_closure_train(sv_handle *h, uint32_t iterations, uint32_t batch, float lr, uint32_t seed, float *loss_out);
 int sv_closure_set_mode(sv_handle *h, int mode);
+
+/* No counterpart in the reference: a failure-detection check.  Runs the
+ * learned closure's bounded tensor-core wait on a CTA whose MMA commit is
+ * never issued, with a limit of max_cycles SM clocks (1 .. 4e9): the kernel
+ * gives up, frees its TMEM and raises the closure's timeout counter, as a
+ * particle pass whose MMA never completed would; the next sv_step then fails
+ * with "a tensor-core wait of the learned closure timed out".  The GPU
+ * context stays usable.  Returns 0 once the kernel has returned. */
+int sv_debug_closure_wait_timeout(sv_handle *h, uint64_t max_cycles);
 int sv_closure_evaluate(sv_handle *h, float dt, double out[8]);
 int sv_closure_get_params(sv_handle *h, float *params);
 

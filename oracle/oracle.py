@@ -118,7 +118,9 @@ def lib() -> ct.CDLL:
             "svo_piola_fixed_corotated": (None, [d, d, f64p, f64p]),
             "svo_cauchy_viscosity": (None, [d, d, f64p, f64p]),
             "svo_svd3": (None, [f64p, f64p, f64p, f64p]),
-            "svo_project_sand": (None, [d, d, d, f64p]),
+            "svo_project_sand": (ct.c_int, [d, d, d, f64p]),
+            "svo_deterministic_grid_mass": (ct.c_uint64, [f32p, f32p, u32p, ct.c_uint64, ct.c_float, i32p, f32p,
+                                                          ct.c_uint64]),
             "svo_project_fluid": (None, [f64p]),
             "svo_project_snow": (None, [d, d, f64p, f64p]),
             "svo_friction_angle_to_alpha": (d, [d]),
@@ -207,9 +209,27 @@ def svd3(F):
 
 
 def project_sand(mu_, lambda__, alpha, F):
+    """Sand return map of F (advance_particles.rs:48-71).  Raises ValueError
+    on the compressive branch with mu <= 0, where the reference asserts."""
     F = _m9(F).copy()
-    lib().svo_project_sand(mu_, lambda__, alpha, _p(F, f64p))
+    if lib().svo_project_sand(mu_, lambda__, alpha, _p(F, f64p)) != 0:
+        raise ValueError("sand return map: mu <= 0 under compression (the reference asserts mu > 0)")
     return F
+
+
+def deterministic_grid_mass(positions, mass, flags, dx):
+    """Node ids [m, 3] and fp32 masses of the reference's P2G mass summed in
+    the canonical order (see svo_deterministic_grid_mass)."""
+    x = np.ascontiguousarray(positions, np.float32)
+    ms = np.ascontiguousarray(mass, np.float32)
+    fl = np.ascontiguousarray(flags, np.uint32)
+    n = len(ms)
+    m = lib().svo_deterministic_grid_mass(_p(x, f32p), _p(ms, f32p), _p(fl, u32p), n, float(dx), None, None, 0)
+    ids = np.zeros((m, 3), np.int32)
+    out = np.zeros(m, np.float32)
+    lib().svo_deterministic_grid_mass(_p(x, f32p), _p(ms, f32p), _p(fl, u32p), n, float(dx), _p(ids, i32p),
+                                      _p(out, f32p), m)
+    return ids, out
 
 
 def project_fluid(F):

@@ -25,6 +25,7 @@
 #include "sv_oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <condition_variable>
@@ -345,9 +346,11 @@ template <class T> T energy_fixed_corotated(T mu, T lambda, const M3<T> &F) {
 }
 
 // rust/crates/cpu/src/phase/advance_particles.rs:48-71 sand (Drucker-Prager
-// return map in Hencky strain).  Returns false when mu <= 0 (the reference
-// asserts mu > 0).
-template <class T> void project_sand(T mu, T lambda, T alpha, M3<T> &F) {
+// return map in Hencky strain).  In expansion (or pure volume change) F
+// becomes U V^T whatever mu is.  Returns false, leaving F as it is, on the
+// compressive branch with mu <= 0, where the reference asserts mu > 0
+// (advance_particles.rs:57).
+template <class T> bool project_sand(T mu, T lambda, T alpha, M3<T> &F) {
     M3<T> U, V;
     V3<T> s;
     svd3(F, U, s, V);
@@ -356,6 +359,7 @@ template <class T> void project_sand(T mu, T lambda, T alpha, M3<T> &F) {
     V3<T> e_hat = e - v3<T>(e_tr / T(3), e_tr / T(3), e_tr / T(3));
     T e_hat_norm = std::sqrt(dot(e_hat, e_hat));
     if (e_tr < T(0) && e_hat_norm > T(0)) {
+        if (!(mu > T(0))) return false;
         T delta_gamma = e_hat_norm + (T(3) * lambda + T(2) * mu) / T(2) / mu * e_tr * alpha;
         if (delta_gamma > T(0)) {
             V3<T> H = e - e_hat * (delta_gamma / e_hat_norm);
@@ -364,6 +368,7 @@ template <class T> void project_sand(T mu, T lambda, T alpha, M3<T> &F) {
     } else {
         F = U * transpose(V);
     }
+    return true;
 }
 
 // rust/crates/cpu/src/phase/advance_particles.rs:77-85 fluid: all singular
@@ -847,7 +852,7 @@ template <class T> struct State : Base {
                 if (q.model == 2) {
                     project_snow<T>((T)q.theta_c, (T)q.theta_s, F[p], plastic_j[p]);
                 } else if (flags[p] & USE_SAND_ALPHA) {
-                    if (mu > T(0)) project_sand<T>(mu, lambda, (T)q.alpha, F[p]);
+                    if (!project_sand<T>(mu, lambda, (T)q.alpha, F[p])) sand_mu_error = true;
                 }
                 T J = det(F[p]);
                 if (!(J > T(0))) {
@@ -881,6 +886,8 @@ template <class T> struct State : Base {
     // cpu/src/cpu_state.rs:146-197 with adaptive_time_steps = false and the
     // phase order of cpu/src/phase/mod.rs:27-41 (InterpolateInput and Collide
     // have no inputs here: gravity is passed in, there are no colliders).
+    // Returns 1 on an energy error, 3 on a sand particle compressed with
+    // mu <= 0 (where the reference asserts mu > 0).
     int step(uint32_t nsub, float dt_f, const float g_f[3]) override {
         T dt = (T)dt_f;
         for (uint32_t s = 0; s < nsub; ++s) {
@@ -894,6 +901,7 @@ template <class T> struct State : Base {
             meld_grid();
             collect_velocity();
             if (advance_particles(dt) > 0) return 1;
+            if (sand_mu_error) return 3;
             cull_particles();
             time += (double)dt_f;
         }
@@ -919,6 +927,9 @@ template <class T> struct State : Base {
         std::vector<int32_t> lmin, lmax;           // frame_input.rs:345-390 padded leaf boxes
     } fin;
     double time = 0;
+    // a sand particle met the compressive branch with mu <= 0, where the
+    // reference asserts mu > 0 (advance_particles.rs:57); the step reports 3
+    std::atomic<bool> sand_mu_error{false};
     // InterpolatedInput (cpu/src/interpolated_input.rs:12-23)
     float ig[3] = {0, 0, 0};
     std::vector<float> igoal, ivpos, ivnorm, itnorm, ifric, idamp;
@@ -1378,7 +1389,8 @@ template <class T> struct State : Base {
 
     // cpu/src/cpu_state.rs:146-197 with adaptive_time_steps = true and the
     // phase order of cpu/src/phase/mod.rs:27-41.  Returns 1 on an energy
-    // error (time not advanced for that substep), 2 on a zero time step.
+    // error (time not advanced for that substep), 2 on a zero time step, 3 on
+    // a sand particle compressed with mu <= 0 (the reference's assert).
     int step_adaptive(double *time, double target, float max_dt, const float g_f[3], uint32_t *substeps,
                       float limits[8]) override {
         ad.max_dt = max_dt;
@@ -1411,6 +1423,11 @@ template <class T> struct State : Base {
             dt_c = ad.allowed();
             if (advance_particles((T)dt_c) > 0) {
                 rc = 1;
+                ++done;
+                break;
+            }
+            if (sand_mu_error) {
+                rc = 3;
                 ++done;
                 break;
             }
@@ -1516,10 +1533,11 @@ void svo_svd3(const double F[9], double U[9], double S[3], double V[9]) {
     store9(u, U), store9(v, V);
     for (int i = 0; i < 3; ++i) S[i] = s[i];
 }
-void svo_project_sand(double mu, double lambda, double alpha, double F[9]) {
+int svo_project_sand(double mu, double lambda, double alpha, double F[9]) {
     M3<double> f = load9<double>(F);
-    project_sand(mu, lambda, alpha, f);
+    if (!project_sand(mu, lambda, alpha, f)) return -1;
     store9(f, F);
+    return 0;
 }
 void svo_project_fluid(double F[9]) {
     M3<double> f = load9<double>(F);
@@ -1586,6 +1604,57 @@ void svo_binning_keys(uint64_t n, const float *pos, const uint32_t *flags, float
 void svo_stable_sort_perm(uint64_t n, const uint32_t *keys, uint32_t *perm) {
     for (uint64_t i = 0; i < n; ++i) perm[i] = (uint32_t)i;
     std::stable_sort(perm, perm + n, [&](uint32_t a, uint32_t b) { return keys[a] < keys[b]; });
+}
+
+// The reference's P2G mass (rust/crates/cpu/src/phase/scatter_momentum.rs:
+// 22-93: w = kernel(n - x/dx) per axis, kernels.rs:17-26, times the mass)
+// with each node's sum taken in one canonical order, in fp32, left to right:
+// over the 27 base cells c = n - (i, j, k), (i, j, k) in lexicographic order
+// (i outermost), and within a cell over its particles in ascending index.
+// The base cell is kernels.rs:46-49's floor(x/dx - 1/2).  Tombstoned
+// particles take no part.  Writes the nodes with mass > 0 in ascending
+// (i, j, k) order, at most `cap`; returns their count.
+uint64_t svo_deterministic_grid_mass(const float *pos, const float *mass, const uint32_t *flags, uint64_t n, float dx,
+                                     int32_t *ids, float *masses, uint64_t cap) {
+    std::map<std::array<int32_t, 3>, std::vector<uint32_t>> cells;  // base cell -> particles, ascending
+    for (uint64_t p = 0; p < n; ++p) {
+        if (flags[p] & TOMBSTONED) continue;
+        std::array<int32_t, 3> c;
+        for (int a = 0; a < 3; ++a) c[a] = (int32_t)std::floor(pos[3 * p + a] / dx - 0.5f);
+        cells[c].push_back((uint32_t)p);
+    }
+    std::vector<std::array<int32_t, 3>> nodes;
+    for (auto &kv : cells)
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) nodes.push_back({kv.first[0] + i, kv.first[1] + j, kv.first[2] + k});
+    std::sort(nodes.begin(), nodes.end());
+    nodes.erase(std::unique(nodes.begin(), nodes.end()), nodes.end());
+    uint64_t count = 0;
+    for (auto &nd : nodes) {
+        float sum = 0.f;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) {
+                    auto it = cells.find({nd[0] - i, nd[1] - j, nd[2] - k});
+                    if (it == cells.end()) continue;
+                    for (uint32_t p : it->second) {
+                        float w = 1.f;
+                        for (int a = 0; a < 3; ++a) {
+                            const float r = (float)nd[a] - pos[3 * p + a] / dx;
+                            w = a == 0 ? kernel_quadratic<float>(r) : w * kernel_quadratic<float>(r);
+                        }
+                        sum = sum + w * mass[p];
+                    }
+                }
+        if (!(sum > 0.f)) continue;
+        if (count < cap && ids && masses) {
+            for (int a = 0; a < 3; ++a) ids[3 * count + a] = nd[a];
+            masses[count] = sum;
+        }
+        ++count;
+    }
+    return count;
 }
 
 }  // extern "C"

@@ -104,8 +104,10 @@ void svo_piola_fixed_corotated(double mu, double lambda, const double F[9], doub
 void svo_cauchy_viscosity(double dynamic, double bulk, const double C[9], double S[9]);
 void svo_svd3(const double F[9], double U[9], double S[3], double V[9]);
 /* Plastic projections in double: sand (advance_particles.rs:48-71), fluid
- * (:77-85), snow (addition). F is updated in place; returns 0. */
-void svo_project_sand(double mu, double lambda, double alpha, double F[9]);
+ * (:77-85), snow (addition). F is updated in place.  svo_project_sand
+ * returns 0, or -1 (F unchanged) on the compressive branch with mu <= 0,
+ * where the reference asserts mu > 0 (advance_particles.rs:57). */
+int svo_project_sand(double mu, double lambda, double alpha, double F[9]);
 void svo_project_fluid(double F[9]);
 void svo_project_snow(double theta_c, double theta_s, double F[9], double *plastic_j);
 double svo_friction_angle_to_alpha(double friction_angle_rad);
@@ -115,7 +117,10 @@ void *svo_create(const svo_particles *p, const svo_consts *c, int fp64, int thre
 void svo_destroy(void *s);
 /* Runs n_substeps substeps of the reference phase cycle with a fixed dt
  * (adaptive_time_steps = false).  Returns 0, or 1 when an energy error stopped
- * the run early (a particle got FAILED, advance_particles.rs:73-74). */
+ * the run early (a particle got FAILED, advance_particles.rs:73-74), or 3
+ * when a sand particle was compressed with mu <= 0 (the reference's assert at
+ * advance_particles.rs:57; that substep's advance is complete, its cull is
+ * not run). */
 int svo_step(void *s, uint32_t n_substeps, float dt, const float gravity[3]);
 /* With a frame input set (copied), every substep starts with the input
  * interpolation at the state's time and runs Collide; gravity then comes from
@@ -127,7 +132,7 @@ void svo_set_time(void *s, double time);
 double svo_get_time(void *s);
 /* Adaptive substeps while *time < target (cpu_state.rs:146-197 with
  * adaptive_time_steps = true); returns 0, 1 on an energy error, 2 on a zero
- * time step.  limits: the last substep's dt of external force, scatter and
+ * time step, 3 on a sand particle compressed with mu <= 0.  limits: the last substep's dt of external force, scatter and
  * advance, then the velocity, deformation, sound and isolated limits and the
  * allowed step (FLT_MAX = none). */
 int svo_step_adaptive(void *s, double *time, double target, float max_dt, const float gravity[3],
@@ -138,6 +143,14 @@ void svo_download(void *s, svo_particles *out);
 /* Grid after P2G + meld of the most recent substep: nodes with mass > 0 only,
  * sorted by (i, j, k, collider_bits).  Returns the node count; writes at most
  * capacity entries. */
+/* The reference's P2G mass (scatter_momentum.rs:22-93) with every node's
+ * fp32 sum taken in one canonical order: over the 27 base cells n - (i, j, k)
+ * in lexicographic order, then the cell's particles in ascending index, left
+ * to right.  Positions [n][3]; tombstoned particles skipped.  Writes the
+ * nodes with mass > 0 in ascending (i, j, k) order (at most cap); returns
+ * their count. */
+uint64_t svo_deterministic_grid_mass(const float *pos, const float *mass, const uint32_t *flags, uint64_t n, float dx,
+                                     int32_t *ids, float *masses, uint64_t cap);
 uint64_t svo_grid(void *s, int32_t *node_ids, float *masses, float *velocities,
                   uint64_t capacity);
 /* Runs the first half of a substep (sort, external force, grid nodes, P2G,

@@ -28,6 +28,7 @@ SV_FAILED = 1 << 6
 SV_STATUS_CAPACITY_EXCEEDED = 1 << 0
 SV_STATUS_PARTICLE_INVERTED = 1 << 3
 SV_STATUS_CANCELED = 1 << 8
+SV_STATUS_SAND_INVALID_MU = 1 << 11
 
 SV_MODEL_REFERENCE = 0
 SV_MODEL_FIXED_COROTATED = 1
@@ -47,7 +48,8 @@ class SvConsts(ct.Structure):
         ("block_capacity", ct.c_uint64),
         ("sort_interval", ct.c_uint32),
         ("host_transfer", ct.c_uint32),
-        ("reserved", ct.c_uint32 * 4),
+        ("deterministic_p2g", ct.c_uint32),
+        ("reserved", ct.c_uint32 * 3),
     ]
 
 
@@ -98,6 +100,8 @@ class SvStats(ct.Structure):
         ("closure_mode", ct.c_uint64),
         ("adaptive_misses", ct.c_uint64),
         ("adaptive_split", ct.c_uint64),
+        ("grid_mass", ct.c_double),
+        ("grid_momentum", ct.c_double * 3),
     ]
 
 
@@ -197,6 +201,7 @@ _SIGNATURES = {
     "sv_get_time": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_double)]),
     "sv_autotune": (ct.c_int, [ct.c_void_p, ct.c_float, f32p, ct.c_uint32, u32p, u32p]),
     "sv_set_profiling": (ct.c_int, [ct.c_void_p, ct.c_int]),
+    "sv_debug_closure_wait_timeout": (ct.c_int, [ct.c_void_p, ct.c_uint64]),
     "sv_profile_report": (ct.c_int, [ct.c_void_p, ct.c_char_p, ct.c_uint64]),
     "sv_mlp_param_count": (ct.c_int, []),
     "sv_mlp_forward": (ct.c_int, [f32p, f32p, ct.c_uint64, f32p]),

@@ -3,6 +3,7 @@
 // CpuState::produce_next_state (rust/crates/cpu/src/cpu_state.rs:146-197).
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <thread>
 #include <cmath>
 #include <cstdio>
@@ -77,6 +78,8 @@ void free_handle(sv_handle *h) {
     free_closure(h);
     free_frame(h);
     cudaFree(h->adt), cudaFree(h->adt_backup);
+    cudaFree(h->det_kbo), cudaFree(h->det_orig), cudaFree(h->det_cstart), cudaFree(h->det_slot_seg), cudaFree(h->det_rec);
+    if (h->wait_event) cudaEventDestroy(h->wait_event);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
 }
@@ -342,10 +345,20 @@ cudaError_t alloc_grid(sv_handle *h, uint64_t capacity) {
             return e;
         }
     }
-    cudaStreamSynchronize(h->stream);
+    // the old slot lists are copied on the handle's stream; nothing is freed
+    // or swapped in until that copy has completed without error
+    for (int s = 0; s < 2 && h->active[s]; ++s)
+        if ((e = cudaMemcpyAsync(active[s], h->active[s], std::min(capacity, h->capacity) * 4, cudaMemcpyDeviceToDevice,
+                                 h->stream)) != cudaSuccess)
+            break;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        for (int t = 0; t < 2; ++t) cudaFree(active[t]), cudaFree(grid[t]);
+        h->device_bytes -= 2 * (capacity * 4 + capacity * 64 * sizeof(float4));
+        return e;
+    }
     for (int s = 0; s < 2; ++s) {
         if (h->active[s]) {
-            cudaMemcpy(active[s], h->active[s], std::min(capacity, h->capacity) * 4, cudaMemcpyDeviceToDevice);
             cudaFree(h->active[s]);
             cudaFree(h->grid[s]);
             h->device_bytes -= h->capacity * 4 + h->capacity * 64 * sizeof(float4);
@@ -359,9 +372,30 @@ cudaError_t alloc_grid(sv_handle *h, uint64_t capacity) {
 
 // Scatter of the current state into grid[gcur] after a fresh binning: the
 // start of a run, or the recovery after a particle left its claimed blocks.
+// The deterministic mode's work buffers, sized for the grid block capacity.
+cudaError_t ensure_det_buffers(sv_handle *h) {
+    if (h->det_kbo && h->det_seg_cap >= h->capacity) return cudaSuccess;
+    cudaError_t e;
+    if (!h->det_kbo) {
+        if ((e = dalloc(h, &h->det_kbo, h->n)) || (e = dalloc(h, &h->det_orig, h->n)) ||
+            (e = dalloc(h, &h->det_rec, 4 * h->n)))
+            return e;
+    }
+    cudaFree(h->det_cstart), cudaFree(h->det_slot_seg);
+    h->det_cstart = nullptr, h->det_slot_seg = nullptr;
+    if ((e = dalloc(h, &h->det_cstart, 65 * h->capacity)) || (e = dalloc(h, &h->det_slot_seg, h->capacity))) return e;
+    h->det_seg_cap = h->capacity;
+    return cudaSuccess;
+}
+
 int standalone_p2g(sv_handle *h, float dt, float3 g) {
     if (!h->keys_valid) SV_CUDA(launch_keys(h));
-    SV_CUDA(launch_sort_and_segments(h));
+    if (h->deterministic) {
+        SV_CUDA(ensure_det_buffers(h));
+        SV_CUDA(launch_det_binning(h));
+    } else {
+        SV_CUDA(launch_sort_and_segments(h));
+    }
     const int which = h->map_cur ^ 1;
     SV_CUDA(launch_activate(h, which));
     h->map_cur = h->map_next = which;
@@ -370,7 +404,8 @@ int standalone_p2g(sv_handle *h, float dt, float3 g) {
         SV_CUDA(launch_interpolate(h, h->time));
         SV_CUDA(launch_clear_variants(h, h->gcur));
     }
-    SV_CUDA(launch_p2g(h, dt, g));
+    if (h->deterministic) SV_CUDA(launch_det_p2g(h, dt, g));
+    else SV_CUDA(launch_p2g(h, dt, g));
     // a scatter that failed (e.g. a record outside the claimed blocks) stops
     // the passes that would gather from it
     SV_CUDA(launch_latch(h));
@@ -393,6 +428,16 @@ bool in_frame(const sv_handle *h, double t) {
 // frame the substep only gathers and advances (the next call scatters once
 // the next frame is loaded).
 int fused_substep(sv_handle *h, float dt, float3 g, double t_next = 0.0) {
+    if (h->deterministic) {
+        // gather and advance, then the next substep's scatter binned afresh
+        // and gathered per node in the fixed order, into the other grid (the
+        // one gathered from keeps the substep's velocities)
+        SV_CUDA(launch_grid_update(h, false));
+        SV_CUDA(launch_g2p_advance(h, dt));
+        h->need_perm = false;
+        h->gcur ^= 1;
+        return standalone_p2g(h, dt, g);
+    }
     if (h->fin_active && !in_frame(h, t_next)) {
         SV_CUDA(launch_grid_update(h, false));
         SV_CUDA(launch_g2p_advance(h, dt));
@@ -584,6 +629,27 @@ int read_counters(sv_handle *h) {
     return 0;
 }
 
+// The same read for the substep loops, waiting like the reference's GPU
+// backend (gpu_state.rs:509-522 polls its device every 100 ms and checks the
+// harness in between): the queued work cannot be recalled, so the wait
+// polls the copy's event every 50 us and notes a cancel request seen
+// meanwhile in *canceled; the caller stops queueing once the chunk in
+// flight has completed.
+int read_counters_polled(sv_handle *h, const volatile int32_t *cancel, bool *canceled) {
+    SV_CUDA(cudaMemcpyAsync(h->host_counters, h->counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+    if (!h->wait_event) SV_CUDA(cudaEventCreateWithFlags(&h->wait_event, cudaEventDisableTiming));
+    SV_CUDA(cudaEventRecord(h->wait_event, h->stream));
+    while (true) {
+        const cudaError_t q = cudaEventQuery(h->wait_event);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) SV_CUDA(q);
+        if (cancel && *cancel && canceled) *canceled = true;
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    if (cancel && *cancel && canceled) *canceled = true;
+    return 0;
+}
+
 }  // namespace
 
 namespace sv {
@@ -662,6 +728,9 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     std::vector<Material> &mats = pre.mats;
     const std::vector<uint32_t> &mat_index = pre.mat_index;
 
+    if (c.deterministic_p2g > 1) return fail("sv_create: deterministic_p2g must be 0 or 1");
+    if (c.deterministic_p2g && (batched || c.position_form != 0))
+        return fail("sv_create: deterministic_p2g needs fp32 positions (position_form 0) and a single scene");
     sv_handle *h = new sv_handle();
     h->n = n;
     h->batched = batched;
@@ -678,6 +747,7 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     L.ground_mode = c.ground_mode, L.ground_axis = c.ground_axis, L.ground_height = c.ground_height;
     L.position_form = batched ? 1u : c.position_form;
     L.svd_policy = c.svd_fp64_policy;
+    h->deterministic = c.deterministic_p2g == 1;
     for (int a = 0; a < 3; ++a) {
         L.domain_min[a] = c.domain_min[a], L.domain_max[a] = c.domain_max[a];
         L.dmin_cells[a] = (double)c.domain_min[a] / (double)L.dx;
@@ -763,6 +833,7 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     uint64_t tiles = (n + 2047) / 2048 + 1;
     arena.add(&h->materials, mats.size()), arena.add(&h->scenes, n_scenes);
     arena.add(&h->keys, n), arena.add(&h->sorted_keys, n), arena.add(&h->perm, n), arena.add(&h->inv, n);
+    arena.add(&h->grid_sums, 8);
     arena.add(&h->seg_start, n + 1), arena.add(&h->seg_block, n), arena.add(&h->counters, C_COUNT);
     arena.add((char **)&h->sort_temp, h->sort_temp_bytes), arena.add(&h->tile_counts, tiles);
     arena.add((char **)&h->scan_temp, scan_temp_bytes(tiles));
@@ -786,7 +857,7 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     if ((e = cudaMemcpy(h->materials, mats.data(), mats.size() * sizeof(Material), cudaMemcpyHostToDevice)) ||
         (e = cudaMemcpy(h->scenes, scenes.data(), n_scenes * sizeof(SceneInfo), cudaMemcpyHostToDevice)) ||
         (e = cudaMemset(h->blockmap[0], 0xFF, total * 4)) || (e = cudaMemset(h->blockmap[1], 0xFF, total * 4)) ||
-        (e = cudaMemset(h->counters, 0, C_COUNT * 4)))
+        (e = cudaMemset(h->counters, 0, C_COUNT * 4)) || (e = cudaMemset(h->grid_sums, 0, 8 * sizeof(double))))
         return cuda_fail(e, "upload");
     h->direct_host = c.host_transfer == 0 && pageable_access();
     if (h->direct_host) {
@@ -873,8 +944,8 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
     h->force_limits_valid = false;  // fixed substeps (graph replays included) move the particles
     // A previous energy error does not carry over: the reference checks each
     // substep afresh (cpu_state.rs:178-183).
-    if (h->host_counters[C_STATUS] & ST_INVERTED) {
-        h->host_counters[C_STATUS] &= ~ST_INVERTED;
+    if (h->host_counters[C_STATUS] & (ST_INVERTED | ST_SAND_MU)) {
+        h->host_counters[C_STATUS] &= ~(ST_INVERTED | ST_SAND_MU);
         SV_CUDA(cudaMemcpyAsync(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice, h->stream));
         h->pending_valid = false;
     }
@@ -888,9 +959,13 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
     uint32_t fallback_before = h->host_counters[C_FALLBACK];
     uint32_t status = 0;
     uint32_t done = 0, timed = 0;
-    const uint32_t chunk = 64;
+    // Substeps are queued in chunks and the counters read after each.  With
+    // a cancel flag the chunks are shorter, so that a cancel request takes
+    // effect within 16 substeps of the one running.
+    const uint32_t chunk = cancel ? 16 : 64;
+    bool canceled = false;
     while (done < n_substeps) {
-        if (cancel && *cancel) {
+        if (canceled || (cancel && *cancel)) {
             status |= SV_STATUS_CANCELED;
             break;
         }
@@ -904,7 +979,7 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
         for (uint32_t s = 0; s < todo;) {
             // whole binning periods go through CUDA graphs once the binning
             // keys come from the previous substep (steady state)
-            if (h->use_graphs && !h->fin_active && !h->profiling && h->since_sort >= h->sort_interval &&
+            if (h->use_graphs && !h->fin_active && !h->deterministic && !h->profiling && h->since_sort >= h->sort_interval &&
                 h->keys_valid && todo - s >= h->sort_interval) {
                 if (run_period_graph(h, dt, g)) return -1;
                 s += h->sort_interval;
@@ -915,7 +990,7 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
                 if (!h->pending_valid) break;  // the frame's last substep: nothing pending
             }
         }
-        if (read_counters(h)) return -1;
+        if (read_counters_polled(h, cancel, &canceled)) return -1;
         const uint32_t st = h->host_counters[C_STATUS];
         done = h->host_counters[C_SUBSTEPS] - base;
         for (; timed < done; ++timed) h->time += (double)dt;  // cpu_state.rs:186-189
@@ -925,6 +1000,13 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
         if (st & ST_OUT_OF_GRID) return fail("sv_step: a live particle left the grid block index");
         if (h->host_counters[C_CLOSURE_ERR]) return fail("sv_step: a tensor-core wait of the learned closure timed out");
         if (st & ST_VARIANT_FULL) return fail("sv_step: the collider variant table is full");
+        if (st & ST_SAND_MU) {
+            // the reference asserts mu > 0 here (advance_particles.rs:57)
+            h->substeps_total += done;
+            if (status_out) *status_out = status | SV_STATUS_SAND_INVALID_MU;
+            if (substeps_done) *substeps_done = done;
+            return fail("sv_step: a sand particle with mu <= 0 was compressed (the reference asserts mu > 0)");
+        }
         if (st & (ST_CAPACITY | ST_MOVED_FAR)) {
             if (st & ST_CAPACITY) {
                 // Grow and redo what was skipped (gpu_state.rs:562-599 redoes a
@@ -945,6 +1027,7 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
             // an inversion in the same substeps is still reported below
             if (!(st & ST_INVERTED)) continue;
         }
+        if (canceled && done < n_substeps) status |= SV_STATUS_CANCELED;
         if (h->adaptive_interval && todo > 0) {
             // Bin more often when many gathers miss their shared tile, less
             // often when almost none do.
@@ -1008,7 +1091,7 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
     h->limits_pass_pending = true;
     SV_CUDA(cudaMemcpyAsync(h->adt, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
     if (read_counters(h)) return -1;
-    h->host_counters[C_STATUS] &= ~(ST_INVERTED | ST_TIME_REACHED | ST_ZERO_DT);
+    h->host_counters[C_STATUS] &= ~(ST_INVERTED | ST_TIME_REACHED | ST_ZERO_DT | ST_SAND_MU);
     SV_CUDA(cudaMemcpyAsync(h->counters + C_STATUS, h->host_counters + C_STATUS, 4, cudaMemcpyHostToDevice, h->stream));
     // the fused path's pending scatter and binning do not survive this call
     h->pending_valid = false;
@@ -1023,8 +1106,9 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
     double t_now = st.time;        // device time after the last batch
     float dt_last = max_time_step; // its last advance step
     int rc = 0;
+    bool canceled = false;
     while (true) {
-        if (cancel && *cancel) {
+        if (canceled || (cancel && *cancel)) {
             status |= SV_STATUS_CANCELED;
             break;
         }
@@ -1063,7 +1147,7 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
         if (rc == 0) {
             adaptive::State now;
             if (cudaMemcpyAsync(&now, h->adt, sizeof(now), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) rc = -1;
-            if (rc == 0 && read_counters(h)) rc = -1;  // synchronises the copy too
+            if (rc == 0 && read_counters_polled(h, cancel, &canceled)) rc = -1;  // waits for the copy too
             if (rc == 0) t_now = now.time, dt_last = now.dt_c;
         }
         if (rc) {
@@ -1087,6 +1171,12 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
         }
         if (stw & ST_VARIANT_FULL) {
             rc = fail("sv_step_adaptive: the collider variant table is full");
+            break;
+        }
+        if (stw & ST_SAND_MU) {
+            // the reference asserts mu > 0 here (advance_particles.rs:57)
+            status |= SV_STATUS_SAND_INVALID_MU;
+            rc = fail("sv_step_adaptive: a sand particle with mu <= 0 was compressed (the reference asserts mu > 0)");
             break;
         }
         if (stw & (STOP_MASK & ~ST_TIME_REACHED)) h->keys_valid = false;  // stopped advances copied in place
@@ -1146,7 +1236,11 @@ int sv_step_adaptive(sv_handle *h, double *time_inout, double target_time, float
     h->keys_valid = false;
     h->pending_valid = false;  // a scatter made at adaptive steps
     h->force_limits_valid = rc == 0;
-    if (rc) return -1;
+    if (rc) {
+        if (status_out) *status_out = status;
+        if (substeps_done) *substeps_done = h->host_counters[C_SUBSTEPS] - base;
+        return -1;
+    }
     SV_CUDA(cudaMemcpyAsync(&st, h->adt, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
     SV_CUDA(cudaStreamSynchronize(h->stream));
     h->host_counters[C_STATUS] &= ~ST_TIME_REACHED;
@@ -1334,6 +1428,13 @@ int sv_get_stats(sv_handle *h, sv_stats *out) {
     out->closure_mode = (uint64_t)h->closure_mode;
     out->adaptive_misses = h->host_counters[C_ADT_MISS];
     out->adaptive_split = h->adt_split_substeps;
+    // the grid the last substep gathered from (its sums were taken by the
+    // grid update that turned it into velocities)
+    double sums[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    SV_CUDA(cudaMemcpy(sums, h->grid_sums, sizeof(sums), cudaMemcpyDeviceToHost));
+    const int gs = h->vel_side >= 0 ? h->vel_side : h->gcur;
+    out->grid_mass = sums[4 * gs];
+    for (int a = 0; a < 3; ++a) out->grid_momentum[a] = sums[4 * gs + 1 + a];
     return 0;
 }
 

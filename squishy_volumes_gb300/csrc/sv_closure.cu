@@ -439,10 +439,39 @@ extern "C" int sv_closure_train(sv_handle *h, uint32_t iterations, uint32_t batc
     return 0;
 }
 
+namespace sv {
+namespace {
+// The learned closure's bounded tensor-core wait made to run out: one CTA
+// sets up the closure's per-CTA control (TMEM columns and the MMA-completion
+// mbarrier), waits at most `max_cycles` for an MMA commit that is never
+// issued, and ends like a particle pass whose wait gave up (ctl_finish: a
+// second bounded wait, the TMEM freed, C_CLOSURE_ERR raised).
+__global__ void __launch_bounds__(128) k_closure_wait_timeout(uint32_t *counters, long long max_cycles) {
+    __shared__ mlp::Ctl ctl;
+    mlp::ctl_init(ctl, mlp::TMEM_COLS_INFER);
+    if (threadIdx.x == 0 && !tc::mbar_wait(&ctl.bar, 0, max_cycles)) ctl.abort = 1, ctl.fail_parity = 0;
+    mlp::ctl_finish(ctl, mlp::TMEM_COLS_INFER, &counters[C_CLOSURE_ERR], max_cycles);
+}
+}  // namespace
+}  // namespace sv
+
+extern "C" int sv_debug_closure_wait_timeout(sv_handle *h, uint64_t max_cycles) {
+    using namespace sv;
+    if (!h) return fail("sv_debug_closure_wait_timeout: NULL handle");
+    if (max_cycles == 0 || max_cycles > 4000000000ull)
+        return fail("sv_debug_closure_wait_timeout: max_cycles must be in [1, 4e9]");
+    k_closure_wait_timeout<<<1, 128, 0, h->stream>>>(h->counters, (long long)max_cycles);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return fail(std::string("sv_debug_closure_wait_timeout: ") + cudaGetErrorString(e));
+    return 0;
+}
+
 extern "C" int sv_closure_set_mode(sv_handle *h, int mode) {
     if (!h) return fail("sv_closure_set_mode: NULL handle");
     if (mode != 0 && mode != 1) return fail("sv_closure_set_mode: mode must be 0 or 1");
     if (mode == 1 && !h->cl_trained) return fail("sv_closure_set_mode: the closure has not been trained");
+    if (mode == 1 && h->deterministic) return fail("sv_closure_set_mode: not with the deterministic P2G mode");
     if (mode != h->closure_mode) {
         CL_CUDA(cudaStreamSynchronize(h->stream));
         drop_graphs(h);

@@ -67,7 +67,6 @@ template <class T> __host__ __device__ inline void return_map(const Material &m,
         return;
     }
     for (int k = 0; k < 3; ++k) s[k] = sig[k];
-    if (!(m.mu > 0.f)) return;
     T e[3];
     for (int k = 0; k < 3; ++k) e[k] = log(sig[k]);
     const T e_tr = e[0] + e[1] + e[2];
@@ -75,6 +74,9 @@ template <class T> __host__ __device__ inline void return_map(const Material &m,
     for (int k = 0; k < 3; ++k) eh[k] = e[k] - e_tr / T(3);
     const T ehn = sqrt(eh[0] * eh[0] + eh[1] * eh[1] + eh[2] * eh[2]);
     if (e_tr < T(0) && ehn > T(0)) {
+        // mu <= 0: the reference asserts mu > 0 (advance_particles.rs:57);
+        // such particles never take the learned path (outside any hull)
+        if (!((T)m.mu > T(0))) return;
         const T dg = ehn + (T(3) * (T)m.lambda + T(2) * (T)m.mu) / T(2) / (T)m.mu * e_tr * (T)m.alpha;
         if (dg > T(0))
             for (int k = 0; k < 3; ++k) s[k] = exp(e[k] - dg / ehn * eh[k]);

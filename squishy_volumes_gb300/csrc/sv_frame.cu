@@ -95,6 +95,7 @@ extern "C" int sv_get_time(sv_handle *h, double *time) {
 
 extern "C" int sv_set_frame_input(sv_handle *h, const sv_frame_input *in) {
     if (!h) return fail("sv_set_frame_input: NULL handle");
+    if (in && h->deterministic) return fail("sv_set_frame_input: the deterministic P2G mode takes no frame input");
     FR_CUDA(cudaStreamSynchronize(h->stream));
     drop_graphs(h);
     h->pending_valid = false;

@@ -31,8 +31,9 @@ constexpr uint32_t ST_TIME_REACHED = 1u << 6; // adaptive steps: the target time
 constexpr uint32_t ST_ZERO_DT = 1u << 7;      // adaptive steps: the allowed time step is 0
 constexpr uint32_t ST_VARIANT_FULL = 1u << 9; // the collider-variant table or a node's variant slots are full
 constexpr uint32_t ST_WRONG_FRAME = 1u << 10; // a substep's time lies outside the loaded frame input
+constexpr uint32_t ST_SAND_MU = SV_STATUS_SAND_INVALID_MU;  // sand with mu <= 0 under compression
 constexpr uint32_t STOP_MASK = ST_CAPACITY | ST_INVERTED | ST_OUT_OF_GRID | ST_MOVED_FAR | ST_TIME_REACHED | ST_ZERO_DT |
-                               ST_VARIANT_FULL | ST_WRONG_FRAME;
+                               ST_VARIANT_FULL | ST_WRONG_FRAME | ST_SAND_MU;
 
 // Device counters (one array so one copy reads them all).
 enum Counter : int {
@@ -160,6 +161,18 @@ struct sv_handle {
     uint32_t max_interval = 8;
     bool adaptive_interval = true;
 
+    // Deterministic P2G (sv_consts::deterministic_p2g): binning keys in
+    // original-index order, the sort's original indices, per sorted particle
+    // records (4 float4), per segment cell starts [65] and the segment of
+    // each grid slot; det_seg_cap segments and slots fit.
+    bool deterministic = false;
+    uint32_t *det_kbo = nullptr, *det_orig = nullptr, *det_cstart = nullptr;
+    int32_t *det_slot_seg = nullptr;
+    float4 *det_rec = nullptr;
+    uint64_t det_seg_cap = 0;
+    // device [2][4] fp64 sums (mass, px, py, pz) of grid[0] and grid[1] in
+    // momentum form, taken by the grid update; zeroed where a grid is cleared
+    double *grid_sums = nullptr;
     uint32_t *counters = nullptr;       // device [C_COUNT]
     uint32_t *host_counters = nullptr;  // pinned mirror
 
@@ -172,6 +185,7 @@ struct sv_handle {
     // status-setting launch was a latch or a self-latching particle pass)
     bool stop_latched = false;
 
+    cudaEvent_t wait_event = nullptr;   // marks the counter copy the substep loops poll for
     cudaStream_t stream = nullptr;      // stream all work is queued on
     cudaStream_t own_stream = nullptr;  // the handle's own stream
     uint64_t device_bytes = 0;
@@ -286,6 +300,10 @@ cudaError_t launch_clear(sv_handle *h, int grid_side, int which);
 // latches the status word's stop bits for the kernels that follow
 cudaError_t launch_latch(sv_handle *h);
 cudaError_t launch_p2g(sv_handle *h, float dt, float3 gravity);
+// deterministic P2G: the binning by (cell, original index), then the
+// records, cell tables and fixed-order node gather into grid[gcur]
+cudaError_t launch_det_binning(sv_handle *h);
+cudaError_t launch_det_p2g(sv_handle *h, float dt, float3 gravity);
 // latch = false: the stop bits are already latched (by the particle pass
 // before it, or by the binning's block claims)
 cudaError_t launch_grid_update(sv_handle *h, bool clear_next, bool latch = true);

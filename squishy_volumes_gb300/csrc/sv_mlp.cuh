@@ -66,15 +66,15 @@ template <class Fn> __device__ __forceinline__ bool issue(Ctl &c, Phase &ph, Fn 
     return true;
 }
 
-// All threads.  After an abort, waits (bounded) once more for the MMA that
-// did not finish, then frees the TMEM and raises `err`.
-__device__ __forceinline__ void ctl_finish(Ctl &c, uint32_t cols, uint32_t *err) {
+// All threads.  After an abort, waits (bounded by `wait_cycles`) once more
+// for the MMA that did not finish, then frees the TMEM and raises `err`.
+__device__ __forceinline__ void ctl_finish(Ctl &c, uint32_t cols, uint32_t *err, long long wait_cycles = MMA_WAIT_CYCLES) {
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
     if (c.abort) {
         if (threadIdx.x == 0) {
-            tc::mbar_wait(&c.bar, c.fail_parity, MMA_WAIT_CYCLES);
+            tc::mbar_wait(&c.bar, c.fail_parity, wait_cycles);
             if (err) atomicOr(err, 1u);
         }
         __syncthreads();

@@ -289,9 +289,10 @@ cudaError_t radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, u
 // Allocation-free sort (sv_sort_pairs_noalloc in the C ABI).
 //
 // Some callers cannot call cudaMalloc: a plugin inside a host application
-// that owns the whole device-memory budget through its own pool, or code
-// recording work into a CUDA graph, where an allocation would break the
-// accounting or the capture.  For them the sort's scratch (the sorted keys,
+// that owns the whole device-memory budget through its own pool (an
+// allocation behind its back breaks that accounting), or a loop with a time
+// budget per iteration that cannot take the device-wide synchronisation a
+// cudaMalloc or cudaFree may cause.  For them the sort's scratch (the sorted keys,
 // the ping-pong pair buffers, the digit histograms and the scan partials)
 // lives in one file-scope device array of fixed size instead, so the call
 // allocates nothing.  The array exists on every GPU that loads the library
@@ -313,6 +314,9 @@ constexpr size_t ce_sort_temp(uint64_t n) {
 // sorted keys, then the radix sort's temporary storage
 constexpr size_t NOALLOC_KEYS_BYTES = ce_align(NOALLOC_MAX_KEYS * 4);
 constexpr size_t NOALLOC_BYTES = NOALLOC_KEYS_BYTES + ce_sort_temp(NOALLOC_MAX_KEYS);
+// 4 MiB of sorted keys + 8 MiB of ping-pong pairs + 4 MiB of digit
+// histograms + 768 B of scan partials; the C header states this figure
+static_assert(NOALLOC_BYTES == 16777984, "no-alloc scratch size changed: update SV_NOALLOC_SCRATCH_BYTES");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
 

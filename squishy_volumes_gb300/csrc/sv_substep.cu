@@ -59,6 +59,13 @@ struct Rec {
     float4 p[9];
 };
 
+// Momentum (x, y, z) and weight (w) of stencil node (li, lj, lk) of a record.
+__device__ __forceinline__ float4 rec_node(const Rec &r, int li, int lj, int lk) {
+    const float4 p0 = r.p[li], p1 = r.p[3 + lj], p2 = r.p[6 + lk];
+    const float2 sxy = __fadd2_rn(__fadd2_rn(make_float2(p0.x, p0.y), make_float2(p1.x, p1.y)), make_float2(p2.x, p2.y));
+    return make_float4(sxy.x, sxy.y, p0.z + p1.z + p2.z, p0.w * p1.w * p2.w);
+}
+
 // MODE_G2P2G_LEARNED is MODE_G2P2G with the learned closure for snow and
 // sand.  Adaptive time steps: MODE_G2P2G_ADAPTIVE is the fused pass at the
 // speculative steps of the adaptive state, reducing the G2P's limits and the
@@ -399,8 +406,10 @@ __global__ void __launch_bounds__(ELEM_THREADS)
 }
 
 __global__ void __launch_bounds__(ELEM_THREADS)
-    k_clear_grid(float4 *grid, uint64_t capacity, uint32_t *counters, int which, const uint32_t *only_if = nullptr) {
+    k_clear_grid(float4 *grid, uint64_t capacity, uint32_t *counters, int which, double *sums,
+                 const uint32_t *only_if = nullptr) {
     if (only_if && !*only_if) return;
+    if (blockIdx.x == 0 && threadIdx.x < 4) sums[threadIdx.x] = 0.0;
     uint64_t slots = counters[C_NSLOT0 + which];
     if (slots > capacity) slots = capacity;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < slots * 64; i += (uint64_t)gridDim.x * blockDim.x)
@@ -409,15 +418,19 @@ __global__ void __launch_bounds__(ELEM_THREADS)
 
 // ------------------------------------------------------------------ grid update
 // Momentum -> velocity on grid_cur (slots of map `wc`), and zeroes grid_next
-// (slots of map `wn`) for the scatter that follows.
+// (slots of map `wn`) for the scatter that follows.  On the way it adds the
+// fp64 sums of mass and momentum over grid_cur's nodes (variants included)
+// into sums_cur, and zeroes sums_next with grid_next.
 __global__ void __launch_bounds__(ELEM_THREADS)
     k_grid_update(float4 *grid_cur, const uint32_t *active_cur, float4 *grid_next, uint64_t capacity, GridLayout L,
-                  uint32_t *counters, int wc, int wn, col::VariantTable var) {
+                  uint32_t *counters, int wc, int wn, col::VariantTable var, double *sums_cur, double *sums_next) {
     if (stopped(counters)) return;
     uint64_t sc = counters[C_NSLOT0 + wc], sn = grid_next ? counters[C_NSLOT0 + wn] : 0;
     if (sc > capacity) sc = capacity;
     if (sn > capacity) sn = capacity;
+    if (grid_next && blockIdx.x == 0 && threadIdx.x < 4) sums_next[threadIdx.x] = 0.0;
     const uint64_t total = (sc > sn ? sc : sn) * 64;
+    double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
         if (i < sc * 64) {
             float4 g = grid_cur[i];
@@ -435,6 +448,7 @@ __global__ void __launch_bounds__(ELEM_THREADS)
                             g.x += a.x, g.y += a.y, g.z += a.z, g.w += a.w;
                         }
             }
+            sm += (double)g.w, sx += (double)g.x, sy += (double)g.y, sz += (double)g.z;
             int x = 0, y = 0, z = 0;
             if (L.ground_mode != 0) {
                 int bx, by, bz;
@@ -445,6 +459,22 @@ __global__ void __launch_bounds__(ELEM_THREADS)
             grid_cur[i] = node_velocity(g, x, y, z, L);
         }
         if (i < sn * 64) grid_next[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sm += __shfl_xor_sync(0xffffffffu, sm, o);
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+        sz += __shfl_xor_sync(0xffffffffu, sz, o);
+    }
+    __shared__ double red[ELEM_THREADS / 32][4];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp][0] = sm, red[warp][1] = sx, red[warp][2] = sy, red[warp][3] = sz;
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int w = 0; w < ELEM_THREADS / 32; ++w) t += red[w][threadIdx.x];
+        if (t != 0.0) atomicAdd(&sums_cur[threadIdx.x], t);
     }
 }
 
@@ -611,14 +641,12 @@ __device__ __forceinline__ void scatter_records(Shared &sh, int count, const Ste
 #pragma unroll 4
     for (int r = 0; r < 32; ++r) {
         if ((vmask >> r) & 1u) {
-            const float4 p0 = sh.rec[r0 + r].p[li], p1 = sh.rec[r0 + r].p[3 + lj], p2 = sh.rec[r0 + r].p[6 + lk];
-            const float w = p0.w * p1.w * p2.w;
+            const float4 nd = rec_node(sh.rec[r0 + r], li, lj, lk);
+            const float w = nd.w;
             const float m = __shfl_sync(0xffffffffu, me.y, r);
-            const float2 sxy = __fadd2_rn(__fadd2_rn(make_float2(p0.x, p0.y), make_float2(p1.x, p1.y)), make_float2(p2.x, p2.y));
-            const float sz = p0.z + p1.z + p2.z;
             if ((start >> r) & 1u) amx = make_float2(0.f, 0.f), ayz = make_float2(0.f, 0.f);
-            amx = __ffma2_rn(make_float2(w, w), make_float2(m, sxy.x), amx);
-            ayz = __ffma2_rn(make_float2(w, w), make_float2(sxy.y, sz), ayz);
+            amx = __ffma2_rn(make_float2(w, w), make_float2(m, nd.x), amx);
+            ayz = __ffma2_rn(make_float2(w, w), make_float2(nd.y, nd.z), ayz);
             if ((end >> r) & 1u) {
                 const int t = (int)__shfl_sync(0xffffffffu, key, r) + off;
                 if (active) {
@@ -633,16 +661,15 @@ __device__ __forceinline__ void scatter_records(Shared &sh, int count, const Ste
     // records outside the tile: straight to global memory
     for (uint32_t g = gmask; g; g &= g - 1) {
         const int r = __ffs(g) - 1;
-        const float4 p0 = sh.rec[r0 + r].p[li], p1 = sh.rec[r0 + r].p[3 + lj], p2 = sh.rec[r0 + r].p[6 + lk];
-        const float w = p0.w * p1.w * p2.w;
+        const float4 nd = rec_node(sh.rec[r0 + r], li, lj, lk);
+        const float w = nd.w;
         const float m = sh.meta[r0 + r].y;
         const int4 gb = sh.gbase[r0 + r];
         if (active) {
             int local;
             const int32_t slot = node_slot(A.map_next, gb.x + li, gb.y + lj, gb.z + lk, A.L, local);
             if (slot >= 0)
-                atomicAdd(&A.grid_next[(uint64_t)slot * 64 + local],
-                          make_float4(w * (p0.x + p1.x + p2.x), w * (p0.y + p1.y + p2.y), w * (p0.z + p1.z + p2.z), w * m));
+                atomicAdd(&A.grid_next[(uint64_t)slot * 64 + local], make_float4(w * nd.x, w * nd.y, w * nd.z, w * m));
             else
                 atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR), sh.raised = 1;
         }
@@ -651,15 +678,14 @@ __device__ __forceinline__ void scatter_records(Shared &sh, int count, const Ste
     // (update_grid_nodes.rs:94-118)
     for (uint32_t g = cmask; g; g &= g - 1) {
         const int r = __ffs(g) - 1;
-        const float4 p0 = sh.rec[r0 + r].p[li], p1 = sh.rec[r0 + r].p[3 + lj], p2 = sh.rec[r0 + r].p[6 + lk];
-        const float w = p0.w * p1.w * p2.w;
+        const float4 nd = rec_node(sh.rec[r0 + r], li, lj, lk);
+        const float w = nd.w;
         const float m = sh.meta[r0 + r].y;
         const int4 gb = sh.gbase[r0 + r];
         if (active) {
             const int64_t s = col::variant_slot(A.vnext, gb.x + li, gb.y + lj, gb.z + lk, (uint32_t)gb.w, true);
             if (s >= 0)
-                atomicAdd(&A.vnext.acc[s],
-                          make_float4(w * (p0.x + p1.x + p2.x), w * (p0.y + p1.y + p2.y), w * (p0.z + p1.z + p2.z), w * m));
+                atomicAdd(&A.vnext.acc[s], make_float4(w * nd.x, w * nd.y, w * nd.z, w * m));
             else
                 atomicOr(&A.counters[C_STATUS], ST_VARIANT_FULL), sh.raised = 1;
         }
@@ -792,8 +818,12 @@ __device__ __forceinline__ void cta_done(const StepArgs &A, uint32_t stop_at_sta
 // learned-closure variant holds the network image as well: four CTAs.
 // FIN: a frame input is loaded -- interpolated gravity and goals, Collide
 // (collide.rs:21-206) before the scatter, collider bits and their variants.
+#ifndef SV_PARTICLE_CTAS_PER_SM
+#define SV_PARTICLE_CTAS_PER_SM 5
+#endif
 template <bool CELL, int MODE, bool FIN = false>
-__global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 5) k_particles(StepArgs A) {
+__global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : SV_PARTICLE_CTAS_PER_SM)
+    k_particles(StepArgs A) {
     constexpr bool LEARNED = MODE == MODE_G2P2G_LEARNED;
     // what the pass does: gather from the grid, advance the particles (and
     // write them out in sorted order), scatter into the next grid
@@ -1033,22 +1063,26 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
                     if (G2P) {
                         if (kind == KIND_SAND) {
                             // Drucker-Prager return map in Hencky strain (advance_particles.rs:48-71)
-                            if (mat.mu > 0.f) {
-                                const float e[3] = {logf(S[0]), logf(S[1]), logf(S[2])};
-                                const float e_tr = e[0] + e[1] + e[2];
-                                const float eh[3] = {e[0] - e_tr / 3.f, e[1] - e_tr / 3.f, e[2] - e_tr / 3.f};
-                                const float ehn = sqrtf(eh[0] * eh[0] + eh[1] * eh[1] + eh[2] * eh[2]);
-                                if (e_tr < 0.f && ehn > 0.f) {
+                            const float e[3] = {logf(S[0]), logf(S[1]), logf(S[2])};
+                            const float e_tr = e[0] + e[1] + e[2];
+                            const float eh[3] = {e[0] - e_tr / 3.f, e[1] - e_tr / 3.f, e[2] - e_tr / 3.f};
+                            const float ehn = sqrtf(eh[0] * eh[0] + eh[1] * eh[1] + eh[2] * eh[2]);
+                            if (e_tr < 0.f && ehn > 0.f) {
+                                if (!(mat.mu > 0.f)) {
+                                    // the reference asserts mu > 0 here (:57)
+                                    atomicOr(&A.counters[C_STATUS], ST_SAND_MU), sh.raised = 1;
+                                } else {
                                     const float dg = ehn + (3.f * mat.lambda + 2.f * mat.mu) / 2.f / mat.mu * e_tr * mat.alpha;
                                     if (dg > 0.f) {
 #pragma unroll
                                         for (int k = 0; k < 3; ++k) S[k] = expf(e[k] - dg / ehn * eh[k]);
                                         F = recompose(U, S, V);
                                     }
-                                } else {
-                                    S[0] = S[1] = S[2] = 1.f;
-                                    F = mat_mul_bt(U, V);
                                 }
+                            } else {
+                                // expansion: U V^T whatever mu is
+                                S[0] = S[1] = S[2] = 1.f;
+                                F = mat_mul_bt(U, V);
                             }
                         } else if (kind == KIND_FLUID) {
                             // advance_particles.rs:77-85: singular values -> geometric mean
@@ -1370,6 +1404,165 @@ __global__ void k_adaptive_finish(adaptive::State *st, uint32_t *counters, bool 
     if (st->time >= st->target) counters[C_STATUS] |= ST_TIME_REACHED;
 }
 
+// ------------------------------------------------------------------ deterministic P2G
+// (sv_consts::deterministic_p2g)  The particles are binned by (cell, original
+// index) -- the binning keys written in original-index order, then the
+// stable radix sort -- and every grid node gathers its mass and momentum in
+// one fixed order: the 27 base cells around it in lexicographic order, each
+// cell's particles in ascending original index.  The mass of each pair is
+// the reference's (scatter_momentum.rs:22-93): w = kernel(n - x/dx) per axis
+// (kernels.rs:17-26), product over x, y, z, times m, summed left to right --
+// every operation rounded on its own, as the CPU computes it.
+
+// keys in original-index order; inv = slot of each original particle
+__global__ void __launch_bounds__(ELEM_THREADS)
+    k_det_order(const uint32_t *orig, const uint32_t *keys, uint64_t n, uint32_t *kbo, uint32_t *inv) {
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t o = orig[s];
+        kbo[o] = keys[s];
+        inv[o] = (uint32_t)s;
+    }
+}
+
+// sorted position -> device slot, from the sort's original indices
+__global__ void __launch_bounds__(ELEM_THREADS)
+    k_det_perm(const uint32_t *sorted_orig, const uint32_t *inv, uint64_t n, uint32_t *perm) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        perm[i] = inv[sorted_orig[i]];
+}
+
+// grid slot -> segment of its block (-1: no particles), cleared per binning
+__global__ void __launch_bounds__(ELEM_THREADS)
+    k_det_slot_reset(int32_t *slot_seg, const uint32_t *counters, int which, uint64_t capacity) {
+    uint64_t cnt = counters[C_NSLOT0 + which];
+    if (cnt > capacity) cnt = capacity;
+    for (uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; s < cnt; s += (uint64_t)gridDim.x * blockDim.x)
+        slot_seg[s] = -1;
+}
+
+// First sorted index of each of the 64 cells of each segment (entry 64: the
+// segment's end), and the segment of each claimed block's slot.
+__global__ void __launch_bounds__(ELEM_THREADS)
+    k_det_cells(const uint32_t *sk, const uint32_t *seg_start, const uint32_t *seg_block, const int32_t *map,
+                const uint32_t *counters, uint32_t *cstart, int32_t *slot_seg, uint64_t max_seg) {
+    uint64_t nseg = counters[C_NSEG];
+    if (nseg > max_seg) nseg = max_seg;  // more segments than claimed blocks: the claim failed (ST_CAPACITY)
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nseg * 65; t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t seg = (uint32_t)(t / 65), c = (uint32_t)(t % 65);
+        const uint32_t b = seg_block[seg];
+        uint32_t lo = seg_start[seg], hi = seg_start[seg + 1];
+        if (c < 64) {
+            const uint32_t key = b << 6 | c;
+            while (lo < hi) {  // first position whose key is not below `key`
+                const uint32_t mid = lo + (hi - lo) / 2;
+                if (sk[mid] < key) lo = mid + 1;
+                else hi = mid;
+            }
+        }
+        cstart[t] = lo;
+        if (c == 0) {
+            const int32_t slot = map[b];
+            if (slot >= 0) slot_seg[slot] = (int32_t)seg;
+        }
+    }
+}
+
+// Per sorted particle: x/dx, the mass, m v after the external force and
+// A = m C - s V0 P F^T (- viscosity), the affine momentum of the scatter
+// (as the fused pass builds it, scatter_momentum.rs:38-90).
+template <bool CELL>
+__global__ void __launch_bounds__(ELEM_THREADS) k_det_records(StepArgs A, float4 *rec) {
+    const uint32_t nlive = A.counters[C_NLIVE];
+    if (stopped(A.counters)) return;
+    uint32_t fp64_dummy = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nlive; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t p = A.perm ? A.perm[i] : (uint32_t)i;
+        const float4 pos = A.in.pos[p];
+        const uint32_t packed = __float_as_uint(pos.w);
+        const Material mat = A.mats[packed >> MATERIAL_SHIFT];
+        m3f F, C, U, V;
+        load_mat9(A.in.F, A.n, p, F);
+        load_mat9(A.in.C, A.n, p, C);
+        const float4 vel = A.in.vel[p];
+        float v[3] = {vel.x + A.dt * A.gravity.x, vel.y + A.dt * A.gravity.y, vel.z + A.dt * A.gravity.z};
+        float S[3] = {1.f, 1.f, 1.f};
+        if (mat.kind == KIND_FIXED_COROTATED || mat.kind == KIND_SNOW) particle_svd(F, U, S, V, A.L.svd_policy, fp64_dummy);
+        const float J = det3(F);
+        const float hard = mat.kind == KIND_SNOW ? expf(mat.xi * (1.f - vel.w)) : 1.f;
+        const m3f PFt = stress_times_ft(mat, F, J, U, S, hard);
+        const float sv0 = A.dt * 4.f / (A.L.dx * A.L.dx) * mat.initial_volume;
+        m3f Am;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Am.a[k] = mat.mass * C.a[k] - sv0 * PFt.a[k];
+        if (mat.use_viscosity) {
+            const float sj = sv0 * J, tr = C.a[0] + C.a[4] + C.a[8];
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                    Am.a[c * 3 + r] -= sj * (mat.visc_dynamic * (C.a[c * 3 + r] + C.a[r * 3 + c]) + (r == c ? mat.visc_bulk * tr : 0.f));
+        }
+        float4 *o = rec + 4 * i;
+        o[0] = make_float4(__fdiv_rn(pos.x, A.L.dx), __fdiv_rn(pos.y, A.L.dx), __fdiv_rn(pos.z, A.L.dx), mat.mass);
+        o[1] = make_float4(mat.mass * v[0], mat.mass * v[1], mat.mass * v[2], Am.a[0]);
+        o[2] = make_float4(Am.a[1], Am.a[2], Am.a[3], Am.a[4]);
+        o[3] = make_float4(Am.a[5], Am.a[6], Am.a[7], Am.a[8]);
+    }
+}
+
+// kernels.rs:17-26 with every operation rounded on its own (no contraction)
+__device__ __forceinline__ float det_kernel(float r) {
+    r = fabsf(r);
+    if (r < 0.5f) return __fsub_rn(0.75f, __fmul_rn(r, r));
+    if (r < 1.5f) {
+        const float t = __fsub_rn(1.5f, r);
+        return __fmul_rn(__fmul_rn(0.5f, t), t);
+    }
+    return 0.f;
+}
+
+// One thread per node of the claimed blocks: the fixed-order gather.
+__global__ void __launch_bounds__(ELEM_THREADS)
+    k_det_gather(const float4 *rec, const uint32_t *active, const int32_t *map, const int32_t *slot_seg,
+                 const uint32_t *cstart, float4 *grid, GridLayout L, const uint32_t *counters, int which,
+                 uint64_t capacity) {
+    if (stopped(counters)) return;
+    uint64_t slots = counters[C_NSLOT0 + which];
+    if (slots > capacity) slots = capacity;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < slots * 64; t += (uint64_t)gridDim.x * blockDim.x) {
+        int bx, by, bz;
+        block_coords(active[t >> 6], L, bx, by, bz);
+        const int l = (int)(t & 63);
+        const int node[3] = {L.origin[0] + 4 * bx + (l >> 4), L.origin[1] + 4 * by + ((l >> 2) & 3), L.origin[2] + 4 * bz + (l & 3)};
+        float mass = 0.f, px = 0.f, py = 0.f, pz = 0.f;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) {
+                    // base cell node - (i, j, k): its block's segment and cell range
+                    int local;
+                    const int32_t slot = node_slot(map, node[0] - i, node[1] - j, node[2] - k, L, local);
+                    if (slot < 0) continue;
+                    const int32_t seg = slot_seg[slot];
+                    if (seg < 0) continue;
+                    const uint32_t lo = cstart[(uint64_t)seg * 65 + local], hi = cstart[(uint64_t)seg * 65 + local + 1];
+                    const float nf[3] = {(float)node[0], (float)node[1], (float)node[2]};
+                    for (uint32_t q = lo; q < hi; ++q) {
+                        const float4 r0 = rec[4 * q], r1 = rec[4 * q + 1], r2 = rec[4 * q + 2], r3 = rec[4 * q + 3];
+                        const float tn[3] = {__fsub_rn(nf[0], r0.x), __fsub_rn(nf[1], r0.y), __fsub_rn(nf[2], r0.z)};
+                        const float w = __fmul_rn(__fmul_rn(det_kernel(tn[0]), det_kernel(tn[1])), det_kernel(tn[2]));
+                        mass = __fadd_rn(mass, __fmul_rn(w, r0.w));
+                        // momentum: w (m v + A (x_i - x_p)), x_i - x_p = tn dx
+                        const float d0 = tn[0] * L.dx, d1 = tn[1] * L.dx, d2 = tn[2] * L.dx;
+                        const float A[9] = {r1.w, r2.x, r2.y, r2.z, r2.w, r3.x, r3.y, r3.z, r3.w};
+                        px += w * (r1.x + A[0] * d0 + A[3] * d1 + A[6] * d2);
+                        py += w * (r1.y + A[1] * d0 + A[4] * d1 + A[7] * d2);
+                        pz += w * (r1.z + A[2] * d0 + A[5] * d1 + A[8] * d2);
+                    }
+                }
+        grid[t] = make_float4(px, py, pz, mass);
+    }
+}
+
 unsigned elem_blocks(uint64_t work) {
     uint64_t b = (work + ELEM_THREADS - 1) / ELEM_THREADS;
     uint64_t cap = (uint64_t)sm_count() * 8;
@@ -1531,7 +1724,8 @@ cudaError_t launch_latch(sv_handle *h) {
 
 cudaError_t launch_clear(sv_handle *h, int grid_side, int which) {
     Scoped s(h, "clear");
-    k_clear_grid<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(h->grid[grid_side], h->capacity, h->counters, which);
+    k_clear_grid<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(h->grid[grid_side], h->capacity, h->counters, which,
+                                                                                  h->grid_sums + 4 * grid_side);
     h->launches += 1;
     return cudaGetLastError();
 }
@@ -1597,8 +1791,8 @@ cudaError_t launch_g2p2g_adaptive(sv_handle *h, float3 g, bool write_keys, bool 
         R.adt_pass = 2;
         launch_particles<MODE_G2P_ADVANCE>(h, R, (unsigned)sm_count() * 5);
         k_dt_next<<<1, 1, 0, h->stream>>>(st, h->counters);
-        k_clear_grid<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(h->grid[h->gcur ^ 1], h->capacity,
-                                                                                      h->counters, h->map_next, &st->p2g_redo);
+        k_clear_grid<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(
+            h->grid[h->gcur ^ 1], h->capacity, h->counters, h->map_next, h->grid_sums + 4 * (h->gcur ^ 1), &st->p2g_redo);
         StepArgs P = make_args(h, 0.f, g);
         P.adt = st;
         P.adt_pass = 4;
@@ -1670,6 +1864,50 @@ cudaError_t launch_p2g(sv_handle *h, float dt, float3 g) {
     return cudaGetLastError();
 }
 
+cudaError_t launch_det_binning(sv_handle *h) {
+    cudaError_t err;
+    if (h->n == 0) return launch_sort_and_segments(h);
+    {
+        Scoped s(h, "radix_sort");
+        k_det_order<<<elem_blocks(h->n), ELEM_THREADS, 0, h->stream>>>(h->side[h->cur].orig, h->keys, h->n, h->det_kbo,
+                                                                       h->inv);
+        err = radix_sort_pairs(h->det_kbo, nullptr, h->sorted_keys, h->det_orig, h->n, h->layout.key_bits, h->sort_temp,
+                               h->stream);
+        if (err != cudaSuccess) return err;
+        k_det_perm<<<elem_blocks(h->n), ELEM_THREADS, 0, h->stream>>>(h->det_orig, h->inv, h->n, h->perm);
+        h->launches += 2 + radix_sort_launches(h->n, h->layout.key_bits);
+        h->sorts += 1;
+        h->need_perm = true;
+    }
+    Scoped s(h, "segments");
+    uint32_t tiles = (uint32_t)((h->n + SEG_TILE - 1) / SEG_TILE);
+    k_seg_count<<<tiles, ELEM_THREADS, 0, h->stream>>>(h->sorted_keys, h->n, h->tile_counts, h->counters);
+    err = exclusive_scan_u32(h->tile_counts, h->tile_counts, tiles, h->scan_temp, h->stream);
+    if (err != cudaSuccess) return err;
+    k_seg_write<<<tiles, ELEM_THREADS, 0, h->stream>>>(h->sorted_keys, h->n, h->tile_counts, tiles, h->seg_start,
+                                                       h->seg_block, h->counters);
+    h->launches += 2 + scan_launches(tiles);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_det_p2g(sv_handle *h, float dt, float3 g) {
+    StepArgs A = make_args(h, dt, g);
+    Scoped s(h, "p2g");
+    const int which = h->map_cur;
+    k_det_slot_reset<<<elem_blocks(h->capacity), ELEM_THREADS, 0, h->stream>>>(h->det_slot_seg, h->counters, which,
+                                                                                 h->capacity);
+    k_det_cells<<<elem_blocks(65 * std::min<uint64_t>(h->n, h->capacity)), ELEM_THREADS, 0, h->stream>>>(
+        h->sorted_keys, h->seg_start, h->seg_block, h->blockmap[which], h->counters, h->det_cstart, h->det_slot_seg,
+        h->det_seg_cap);
+    if (h->layout.position_form) k_det_records<true><<<elem_blocks(h->n), ELEM_THREADS, 0, h->stream>>>(A, h->det_rec);
+    else k_det_records<false><<<elem_blocks(h->n), ELEM_THREADS, 0, h->stream>>>(A, h->det_rec);
+    k_det_gather<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(
+        h->det_rec, h->active[which], h->blockmap[which], h->det_slot_seg, h->det_cstart, h->grid[h->gcur], h->layout,
+        h->counters, which, h->capacity);
+    h->launches += 4;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_grid_update(sv_handle *h, bool clear_next, bool latch) {
     Scoped s(h, "grid_update");
     col::VariantTable var{};
@@ -1683,7 +1921,7 @@ cudaError_t launch_grid_update(sv_handle *h, bool clear_next, bool latch) {
     }
     k_grid_update<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(
         h->grid[h->gcur], h->active[h->map_cur], clear_next ? h->grid[h->gcur ^ 1] : nullptr, h->capacity, h->layout,
-        h->counters, h->map_cur, h->map_next, var);
+        h->counters, h->map_cur, h->map_next, var, h->grid_sums + 4 * h->gcur, h->grid_sums + 4 * (h->gcur ^ 1));
     h->launches += 1;
     if (latch) {
         k_latch<<<1, 1, 0, h->stream>>>(h->counters, -1, -1, h->capacity);

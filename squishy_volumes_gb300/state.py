@@ -247,6 +247,7 @@ class Extras:
     block_capacity: int = 0
     sort_interval: int = 0  # 0 adaptive, 1 every substep, k every k substeps
     host_transfer: int = 0  # 0 direct access to host arrays where possible, 1 staged copies
+    deterministic_p2g: int = 0  # 1: P2G gathered per node in one fixed order (bit-reproducible)
 
 
 @dataclass
@@ -352,6 +353,7 @@ class CudaState:
         c.block_capacity = extras.block_capacity
         c.sort_interval = extras.sort_interval
         c.host_transfer = extras.host_transfer
+        c.deterministic_p2g = extras.deterministic_p2g
         return c
 
     @classmethod
@@ -549,7 +551,11 @@ class CudaState:
     def stats(self) -> dict:
         s = SvStats()
         check(self._lib.sv_get_stats(self._h, ct.byref(s)))
-        return {f[0]: int(getattr(s, f[0])) for f in SvStats._fields_}
+        out = {}
+        for name, typ in SvStats._fields_:
+            v = getattr(s, name)
+            out[name] = [float(x) for x in v] if hasattr(v, "__len__") else (float(v) if typ is ct.c_double else int(v))
+        return out
 
     def set_stream(self, stream_handle: int):
         """Queue all work on a caller-owned cudaStream_t (0 = own stream)."""

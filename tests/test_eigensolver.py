@@ -1,5 +1,5 @@
 """The closed-form 3x3 symmetric eigensolver of the learned closure
-(sym_eig3 in squishy_volumes_gb300/csrc/sv_tc.cuh, host-compiled here by
+(sym_eig3 in squishy_volumes_gb300/csrc/sv_eig.cuh, host-compiled here by
 nvcc) against numpy's eigh, on deformation gradients of the kinds the
 substep produces: near identity down to 1e-13 perturbations (where the
 shifted rows' cross products would underflow without scaling), strong
@@ -17,7 +17,7 @@ CSRC = ROOT / "squishy_volumes_gb300" / "csrc"
 
 DRIVER = r"""
 #include <cstdio>
-#include "sv_tc.cuh"
+#include "sv_eig.cuh"
 int main() {
     float a[6], lam[3], V[9];
     while (scanf("%f %f %f %f %f %f", &a[0], &a[1], &a[2], &a[3], &a[4], &a[5]) == 6) {

@@ -406,3 +406,72 @@ def test_cancel_before_start(cuda_lib):
     status, done = gpu.step(10, s.dt, s.gravity, h)
     assert status & SV_STATUS_CANCELED and done == 0
     gpu.close()
+
+
+# ---------------------------------------------------------------- sand with mu = 0
+def _sand_block(F0, mu=0.0, lam=0.0):
+    from squishy_volumes_gb300 import Particles
+    from squishy_volumes_gb300._abi import SV_USE_SAND_ALPHA
+
+    dx = 0.05
+    g = np.arange(8) * (dx / 2) + 0.4
+    pos = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3).astype(np.float32)
+    n = len(pos)
+    vol = np.full(n, (dx / 2) ** 3, np.float32)
+    p = Particles(flags=np.full(n, SV_IS_SOLID | SV_USE_SAND_ALPHA, np.uint32), positions=pos,
+                  position_gradients=np.tile(np.asarray(F0, np.float32).T.reshape(9), (n, 1)),
+                  velocities=np.zeros((n, 3), np.float32), velocity_gradients=np.zeros((n, 9), np.float32),
+                  mass=vol * 1000.0, initial_volume=vol, mu=np.full(n, mu, np.float32),
+                  lambda_=np.full(n, lam, np.float32),
+                  sand_alpha=np.full(n, scenes.friction_angle_to_alpha(np.deg2rad(30.0)), np.float32))
+    consts = InputConsts(grid_node_size=dx, domain_min=(0.0, 0.0, 0.0), domain_max=(1.0, 1.0, 1.0))
+    return p, consts
+
+
+def test_sand_with_zero_mu_projects_in_expansion(cuda_lib, oracle_mod):
+    """(E, nu) = (0, 0.4), the last of the reference's test_lame_parameters
+    (util/src/elastic.rs:679-689), gives mu = lambda = 0.  In expansion
+    (e_tr >= 0) the reference sets F = U V^T whatever mu is
+    (rust/crates/cpu/src/phase/advance_particles.rs:56-70), so a uniformly
+    stretched block comes back to a rotation."""
+    p, consts = _sand_block(np.diag([1.05, 1.02, 1.03]))
+    gpu = CudaState.from_io_state(IoState(0.0, p), consts)
+    assert gpu.step(2, 1e-4, (0.0, 0.0, 0.0)) == (0, 2)
+    out = gpu.download()
+    gpu.close()
+    ref = oracle_mod.OracleState(p, consts, None, fp64=True)
+    assert ref.step(2, 1e-4, (0.0, 0.0, 0.0)) == 0
+    exp = ref.download()
+    np.testing.assert_array_equal(out.flags, exp.flags)
+    F = out.position_gradients.reshape(-1, 3, 3).astype(np.float64)
+    # U V^T of a diagonal stretch is the identity
+    assert np.abs(F - np.eye(3)).max() < 1e-5
+    assert np.linalg.norm(out.position_gradients - exp.position_gradients) <= 1e-5 * np.linalg.norm(
+        exp.position_gradients)
+
+
+def test_sand_with_zero_mu_under_compression_is_the_references_assert(cuda_lib, oracle_mod):
+    """Under compression with a deviatoric part (e_tr < 0, |e_hat| > 0) the
+    reference asserts mu > 0 (advance_particles.rs:57) and its compute thread
+    panics.  Here sv_step returns -1 with SV_STATUS_SAND_INVALID_MU in
+    *status_out, and the oracle's step returns 3."""
+    import ctypes as ct
+
+    from squishy_volumes_gb300._abi import SV_STATUS_SAND_INVALID_MU, f32p, ptr
+
+    p, consts = _sand_block(np.diag([0.95, 1.0, 1.02]))
+    ref = oracle_mod.OracleState(p, consts, None, fp64=False)
+    assert ref.step(1, 1e-4, (0.0, 0.0, 0.0)) == 3
+    gpu = CudaState.from_io_state(IoState(0.0, p), consts)
+    g = np.zeros(3, np.float32)
+    status, done = ct.c_uint32(0), ct.c_uint32(0)
+    rc = cuda_lib.sv_step(gpu._h, 3, ct.c_float(1e-4), ptr(g, f32p), None, ct.byref(status), ct.byref(done))
+    assert rc == -1
+    assert status.value & SV_STATUS_SAND_INVALID_MU
+    assert b"mu <= 0" in cuda_lib.sv_last_error_string()
+    assert done.value == 1  # the substep that met it completed; none after it ran
+    # a stiff sand block (mu > 0) in the same state is projected, no error
+    p2, consts2 = _sand_block(np.diag([0.95, 1.0, 1.02]), *scenes.lame(1e4, 0.3))
+    gpu2 = CudaState.from_io_state(IoState(0.0, p2), consts2)
+    assert gpu2.step(2, 1e-4, (0.0, 0.0, 0.0)) == (0, 2)
+    gpu.close(), gpu2.close()

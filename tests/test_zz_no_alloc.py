@@ -1,13 +1,14 @@
 """The allocation-free sort entry point, through the C ABI.
 
 sv_sort_pairs_noalloc serves callers that may not allocate device memory (a
-plugin inside an application that owns the whole device-memory budget, or
-work being recorded into a CUDA graph).  Its scratch is a fixed array inside
-the library, so it only takes caller-owned device buffers.  It must give the
-same permutation as the allocating sv_sort_pairs, call after call (the
-shared scratch keeps the previous call's contents), and refuse sizes above
-its limit.  This file is collected last so that a failure here leaves every
-other test already run.
+plugin inside an application that owns the whole device-memory budget
+through its own pool, or a loop that cannot take the device-wide
+synchronisation of an allocation).  Its scratch is a fixed array inside the
+library, so it only takes caller-owned device buffers.  It must give the
+same permutation as the allocating sv_sort_pairs and as a stable CPU
+argsort, call after call (the shared scratch keeps the previous call's
+contents), and refuse sizes above its limit.  This file is collected last so
+that a failure here leaves every other test already run.
 """
 
 import ctypes as ct
@@ -51,6 +52,8 @@ def test_noalloc_sort_matches_allocating_sort_twice(cuda_lib):
     for keys in (first, second):
         got = _run(fn, torch, keys)
         np.testing.assert_array_equal(got, sort_pairs(keys))
+        # independent of the GPU sort's kernels: the stable CPU argsort
+        np.testing.assert_array_equal(got, np.argsort(keys, kind="stable").astype(np.uint32))
 
 
 def test_noalloc_sort_rejects_oversize(cuda_lib):
