@@ -56,8 +56,9 @@ def parse():
     ap.add_argument("--scene", default="three_boxes_1m")
     ap.add_argument("--sort-interval", type=int, default=0,
                     help="substeps between binning sorts (0 adaptive, 1 every substep like the reference)")
-    ap.add_argument("--autotune", action="store_true",
-                    help="time binning interval x CTAs/SM candidates first and keep the fastest (sv_autotune)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip sv_autotune (by default the binning interval x CTAs/SM candidates are timed first "
+                         "and the fastest is kept; the handle's defaults win unless beaten by more than 2 %%)")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel directly (no CUDA graphs)")
     ap.add_argument("--closure", default="plain", choices=["plain", "learned"],
                     help="snow/sand constitutive update: SVD + return map, or the learned closure (trained first)")
@@ -340,8 +341,12 @@ def measure_scene(args, name, rank, world, local, dev, primary):
     if primary and args.closure == "learned":
         closure_info = train_closure(gpu, scene, args)
     tuned = None
-    if args.autotune:
-        tuned = gpu.autotune(scene.dt, scene.gravity, 16)
+    if not args.no_autotune:
+        st0 = gpu.stats()
+        t0 = time.perf_counter()
+        tuned = gpu.autotune(scene.dt, scene.gravity, 48)
+        tuned["default"] = {"sort_interval": "adaptive, at most 8", "cta_per_sm": st0["cta_per_sm"]}
+        tuned["seconds"] = round(time.perf_counter() - t0, 2)
     gpu.set_graphs(not args.no_graphs)
     status, done = gpu.step(args.warmup, scene.dt, scene.gravity)
     if status:

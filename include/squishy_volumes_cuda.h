@@ -347,11 +347,16 @@ int sv_set_host_transfer(sv_handle *h, uint32_t mode, uint32_t *direct);
 int sv_prepare_host(void *const *arrays, const uint64_t *bytes, uint32_t count);
 int sv_get_stats(sv_handle *h, sv_stats *out);
 
-/* Addition: picks the substeps between binning sorts and the CTAs per SM of
- * the particle kernels by timing `substeps_per_trial` substeps of each
- * candidate from a snapshot of the current state; the state is restored
- * afterwards and the fastest configuration is kept for later sv_step calls.
- * The chosen values are written to the out pointers when not NULL. */
+/* Addition: picks the substeps between binning sorts (2, 4, 8, 16) and the
+ * CTAs per SM of the particle kernels (8, 16, 32, 64) by timing each
+ * candidate from a snapshot of the current state: two binning periods of
+ * warm-up (first scatter, graph capture, steady binning), then three repeats
+ * of at least max(substeps_per_trial, 48) substeps, ranked by the median
+ * repeat.  The handle's own configuration is a candidate and is kept unless
+ * another is more than 2 % faster.  The state is restored afterwards.  The
+ * chosen values are written to the out pointers when not NULL.  One launch
+ * covers all scenes of a batched handle, so these settings apply to all of
+ * them alike. */
 int sv_autotune(sv_handle *h, float dt, const float gravity[3], uint32_t substeps_per_trial,
                 uint32_t *sort_interval_out, uint32_t *cta_per_sm_out);
 

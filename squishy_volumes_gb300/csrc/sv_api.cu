@@ -1482,35 +1482,63 @@ int sv_autotune(sv_handle *h, float dt, const float gravity[3], uint32_t substep
         uint32_t zero = 0;
         cudaMemcpy(h->counters + C_STATUS, &zero, 4, cudaMemcpyHostToDevice);
     };
-    uint32_t best_si = h->sort_interval, best_cta = h->cta_per_sm;
-    double best_ms = 1e300;
+    // Every candidate starts from the snapshot, warms up over two of its
+    // binning periods (its first scatter, the CUDA graph capture, the
+    // binning pattern of its steady state), then times three repeats of at
+    // least 48 substeps; the median repeat ranks it.  The configuration the
+    // handle had is a candidate too, and it is kept unless another one is
+    // faster by more than 2 %.
+    const uint32_t si0 = h->sort_interval, cta0 = h->cta_per_sm;
+    const bool adaptive0 = h->adaptive_interval;
+    struct Cand {
+        uint32_t si, cta;
+    };
+    std::vector<Cand> cands = {{si0, cta0}};
+    for (uint32_t si : {2u, 4u, 8u, 16u})
+        for (uint32_t cta : {8u, 16u, 32u, 64u})
+            if (si != si0 || cta != cta0) cands.push_back({si, cta});
+    const uint32_t trial = std::max<uint32_t>(substeps_per_trial, 48);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0), cudaEventCreate(&e1);
     h->adaptive_interval = false;
-    for (uint32_t si : {1u, 2u, 4u, 8u, 16u}) {
-        for (uint32_t cta : {8u, 16u, 32u, 64u, 128u}) {
-            restore();
-            clear_graphs(h);
-            h->sort_interval = h->max_interval = si;
-            h->cta_per_sm = cta;
-            uint32_t st = 0, done = 0;
-            // warm-up covers the first scatter and one graph capture
-            if (sv_step(h, 2 * si + 2, dt, gravity, nullptr, &st, &done) < 0 || st) continue;
+    double ms_default = 0.0, best_ms = 1e300;
+    uint32_t best_si = si0, best_cta = cta0;
+    for (size_t ci = 0; ci < cands.size(); ++ci) {
+        const Cand c = cands[ci];
+        restore();
+        clear_graphs(h);
+        h->sort_interval = h->max_interval = c.si;
+        h->cta_per_sm = c.cta;
+        uint32_t st = 0, done = 0;
+        if (sv_step(h, 2 * c.si + 2, dt, gravity, nullptr, &st, &done) < 0 || st) continue;
+        double rep[3];
+        bool ok = true;
+        for (int r = 0; r < 3 && ok; ++r) {
+            const uint32_t k = ((trial + c.si - 1) / c.si) * c.si;  // whole binning periods
             cudaEventRecord(e0, h->stream);
-            if (sv_step(h, substeps_per_trial, dt, gravity, nullptr, &st, &done) < 0 || st) continue;
+            ok = sv_step(h, k, dt, gravity, nullptr, &st, &done) == 0 && st == 0;
             cudaEventRecord(e1, h->stream);
             cudaEventSynchronize(e1);
             float ms = 0.f;
             cudaEventElapsedTime(&ms, e0, e1);
-            if (ms < best_ms) best_ms = ms, best_si = si, best_cta = cta;
+            rep[r] = (double)ms / k;
         }
+        if (!ok) continue;
+        std::sort(rep, rep + 3);
+        const double med = rep[1];
+        if (ci == 0) ms_default = med;
+        if (med < best_ms) best_ms = med, best_si = c.si, best_cta = c.cta;
     }
+    if (ms_default > 0.0 && best_ms > ms_default * 0.98) best_si = si0, best_cta = cta0;
+    const bool keep_default = best_si == si0 && best_cta == cta0;
     cudaEventDestroy(e0), cudaEventDestroy(e1);
     restore();
     release();
     clear_graphs(h);
-    h->adaptive_interval = false;  // the tuned interval is kept fixed
-    h->sort_interval = h->max_interval = best_si;
+    // a kept default keeps its adaptive interval; a tuned interval is fixed
+    h->adaptive_interval = keep_default && adaptive0;
+    h->sort_interval = best_si;
+    h->max_interval = keep_default && adaptive0 ? 8 : best_si;
     h->cta_per_sm = best_cta;
     h->substeps_total = substeps0, h->fp64_total = fp64_0;
     if (sort_interval_out) *sort_interval_out = best_si;

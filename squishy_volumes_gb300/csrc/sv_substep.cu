@@ -1459,7 +1459,7 @@ __global__ void __launch_bounds__(ELEM_THREADS)
                 else hi = mid;
             }
         }
-        cstart[t] = lo;
+        cstart[t] = c < 64 ? lo : hi;  // entry 64: the segment's end
         if (c == 0) {
             const int32_t slot = map[b];
             if (slot >= 0) slot_seg[slot] = (int32_t)seg;
