@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel directly (no CUDA graphs)")
     ap.add_argument("--closure", default="plain", choices=["plain", "learned"],
                     help="snow/sand constitutive update: SVD + return map, or the learned closure (trained first)")
+    ap.add_argument("--closure-source", default="batched_64",
+                    help="workload whose plain runs give the closure's training pairs (its snow and sand scenes)")
+    ap.add_argument("--closure-pairs", type=int, default=50_000_000, help="training pairs to harvest")
+    ap.add_argument("--closure-iters", type=int, default=20000, help="Adam steps of 65536 pairs")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bound on the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -382,7 +386,8 @@ def measure_scene(args, name, rank, world, local, dev, primary):
     value = live * args.steps * world / elapsed
     launches = (stats1["kernel_launches"] - stats0["kernel_launches"]) / len(reps)
     if closure_info is not None:
-        closure_info.update(compare_closure(gpu, scene, args, stream, value, live, world, stats0, stats1))
+        closure_info.update(compare_closure(gpu, scene, args, stream, value, live, world, stats0, stats1,
+                                            args.steps * len(reps)))
 
     # per-kernel durations: K more substeps right after the timed region,
     # with CUDA events around every kernel group on the library's stream
@@ -533,34 +538,71 @@ def measure_scene(args, name, rank, world, local, dev, primary):
 
 
 def train_closure(gpu, scene, args):
-    """Training data from plain substeps of the scene, then the GPU training
-    loop; none of this is inside the timed region."""
+    """Training pairs harvested from plain runs of another workload (by
+    default the 64-scene batched one: its snow and sand scenes), fp64
+    labels, then the GPU training loop on that handle; the trained network
+    is handed to the measured scene's handle.  None of this is inside the
+    timed region."""
     import torch
 
+    from squishy_volumes_gb300 import CudaState, scenes
+    from squishy_volumes_gb300.state import BatchedCudaState
+
     t0 = time.perf_counter()
+    made = scenes.SCENES[args.closure_source]()
+    if isinstance(made, list):
+        src = BatchedCudaState.from_scenes([s.io_state for s in made], [s.consts for s in made], made[0].extras)
+        ref = made[0]
+    else:
+        src = CudaState.from_io_state(made.io_state, made.consts, made.extras)
+        ref = made
+    rounds, per_round = 10, max(1, ref.substeps // 10)
     pool = 0
-    for k in range(8):
-        gpu.step(20, scene.dt, scene.gravity)
-        pool = gpu.closure_harvest(scene.dt, 60000, 0.02, seed=k)
+    for k in range(rounds):
+        status, _ = src.step(per_round, ref.dt, ref.gravity)
+        if status:
+            raise RuntimeError(f"closure harvest run status {status:#x}")
+        pool = src.closure_harvest(ref.dt, int(math.ceil(args.closure_pairs / rounds)), 0.0, seed=k)
+    torch.cuda.synchronize()
     t1 = time.perf_counter()
-    loss = gpu.closure_train(4000, 8192, 3e-3, seed=1)
+    loss = src.closure_train(args.closure_iters, 65536, 3e-3, seed=1)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    ev = gpu.closure_evaluate(scene.dt)
+    yielding = src.closure_pool()["yielding_pairs"]
+    gpu.closure_copy_from(src)
+    src.close()
     gpu.closure_set_mode(1)
-    return {"mode": "learned", "pool": pool, "harvest_s": round(t1 - t0, 3),
-            "train_s": round(t2 - t1, 3), "train_iterations": 4000, "loss": loss,
-            "stress_rel_err_learned": ev["stress_err_learned"],
+    return {"mode": "learned", "source": args.closure_source, "pairs": pool, "yielding_pairs": yielding,
+            "harvest_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3), "train_iterations": args.closure_iters,
+            "batch": 65536, "loss_normalised": loss}
+
+
+def closure_accuracy(gpu, scene):
+    """Errors of the learned closure against the fp64 return map, and the
+    per-phase costs, on the state the timed run reached (the scene starts
+    undeformed, where every stress is zero)."""
+    ev = gpu.closure_evaluate(scene.dt)
+    phases = gpu.closure_phase_times(scene.dt)
+    return {"stress_rel_err_learned": ev["stress_err_learned"],
             "stress_rel_err_plain_fp32": ev["stress_err_plain32"],
             "projected_f_rel_err_learned": ev["f_err_learned"],
-            "fallback_fraction": ev["fallbacks"] / max(ev["particles"], 1.0)}
+            "projected_f_rel_err_plain_fp32": ev["f_err_plain32"],
+            "fallback_fraction": ev["fallbacks"] / max(ev["particles"], 1.0),
+            "network_fraction": ev["network"] / max(ev["particles"], 1.0),
+            "residual_rejects": ev["residual_rejects"],
+            "stress_rel_err_network_part": ev["stress_err_network_part"],
+            "stress_rel_err_elastic_part": ev["stress_err_elastic_part"],
+            "phase_ms": {k: phases[k] for k in ("plain_ms", "closed_form_ms", "network_all_ms",
+                                                "network_yielding_ms")},
+            "phase_particles": phases["particles"], "phase_yielding": phases["yielding"]}
 
 
-def compare_closure(gpu, scene, args, stream, value, live, world, stats0, stats1):
+def compare_closure(gpu, scene, args, stream, value, live, world, stats0, stats1, substeps):
     """The same K substeps with the return maps, from the state reached."""
     import torch
 
-    out = {"learned_fraction": (stats1["closure_learned"] - stats0["closure_learned"]) / max(1, live * args.steps)}
+    out = closure_accuracy(gpu, scene)
+    out["learned_fraction"] = (stats1["closure_learned"] - stats0["closure_learned"]) / max(1, live * substeps)
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     gpu.closure_set_mode(0)

@@ -372,20 +372,24 @@ int sv_set_profiling(sv_handle *h, int enable);
 int sv_profile_report(sv_handle *h, char *buffer, uint64_t capacity);
 
 /* ------------------------------------------------------------------ learned closure
- * Addition (not in the reference): a small MLP that maps principal stretches
- * and material parameters to principal Kirchhoff stress and projected
- * stretch, evaluated on the tensor cores (bf16 operands, fp32 accumulation).
- * Network: x (16) -> ReLU (32) -> ReLU (32) -> y (16, the first 6 used).
- * Parameters are an fp32 vector of sv_mlp_param_count() values:
- * W1[32][16], b1[32], W2[32][32], b2[32], W3[16][32], b3[16] (row-major,
- * out x in).
+ * Addition (not in the reference): a learned return map for snow and sand,
+ * replacing rust/crates/cpu/src/phase/advance_particles.rs:48-71 when
+ * switched on.  An MLP maps the principal Hencky strains and the material
+ * parameters (normalised) to the plastic correction of the strains and the
+ * principal Kirchhoff stress of the projected state (normalised), evaluated
+ * on the tensor cores.
+ * Network: x (16; input 15 is reserved and read as 0) -> 4 hidden layers of
+ * width 64 with SiLU (bf16 operands, fp32 accumulation) -> an fp32 head of
+ * 8 outputs, the first 6 used.  Parameters are an fp32 vector of
+ * sv_mlp_param_count() = 14088 values: W1[64][16], b1[64], W2[64][64], b2,
+ * W3[64][64], b3, W4[64][64], b4, W5[8][64], b5[8] (row-major, out x in).
  *
  * The two entry points below are stateless inspection calls on host
  * buffers (they allocate device memory per call) used to check the kernels:
- *   sv_mlp_forward: y[n][16] = network(x[n][16]);
- *   sv_mlp_grad:    loss = sum_r w[r] sum_{o<6} (y[r][o] - t[r][o])^2 / n, its
- *                   gradient with respect to the parameters into grad[], and
- *                   y[n][16] when y is not NULL. */
+ *   sv_mlp_forward: y[n][8] = network(x[n][16]);
+ *   sv_mlp_grad:    loss = sum_r w[r] sum_{o<6} (y[r][o] - t[r][o])^2 / n
+ *                   (t[n][8]), its gradient with respect to the parameters
+ *                   into grad[], and y[n][8] when y is not NULL. */
 int sv_mlp_param_count(void);
 int sv_mlp_forward(const float *params, const float *x, uint64_t n, float *y);
 int sv_mlp_grad(const float *params, const float *x, const float *t, const float *w, uint64_t n, float *y,
@@ -393,17 +397,28 @@ int sv_mlp_grad(const float *params, const float *x, const float *t, const float
 
 /* The closure of a handle's snow and sand particles.
  *
+ * In sv_step with the learned closure on, a snow/sand particle's principal
+ * stretches come from a closed-form eigen-decomposition of F^T F; the yield
+ * test (closed form) keeps elastic particles on their stretches, and the
+ * network decides the yielding ones.  A yielding particle outside the
+ * training hull, or whose network stress disagrees with the closed-form
+ * stress of its projected stretches by more than 1e-3 mu h, takes the SVD +
+ * return map.
+ *
  * sv_closure_harvest: adds up to max_samples trial deformation gradients
  *   F + dt C F of the live snow/sand particles of the current state (states
- *   the plain solver produced) to the handle's training pool (at most 2^22);
+ *   the plain solver produced) to the handle's training pool (at most 2^26);
  *   with augment > 0 half of them are multiplied by I + augment R, R
  *   symmetric with entries in [-1, 1).  *total_out = pool size.
- * sv_closure_train: labels the pool with the fp64 SVD + return map, records
- *   the range of the features (the hull outside which the return map is
- *   used), and runs `iterations` Adam steps (minibatches of `batch`,
- *   learning rate lr with a cosine decay) on the GPU from the current
- *   weights (He-initialised from `seed` on the first call).  *loss_out =
- *   mean squared error over the pool afterwards.
+ * sv_closure_train: labels the pool with the fp64 SVD + return map, keeps
+ *   the yielding samples, records the range of their features (the hull)
+ *   and the normalisation of inputs and outputs, and runs `iterations` Adam
+ *   steps (minibatches of `batch`, 0 = 65536; learning rate lr with a cosine
+ *   decay to 1 %) on the GPU from the current weights (He-initialised from
+ *   `seed` on the first call).  *loss_out = mean squared error (normalised
+ *   units) over the yielding samples afterwards.
+ * sv_closure_copy: gives dst the trained network, hull and normalisation of
+ *   src (e.g. trained on a batched handle, used on another).
  * sv_closure_set_mode: 0 = return maps (default), 1 = learned closure in
  *   sv_step (needs a trained network).
  * sv_closure_evaluate: on the trial F of the current state, out[0] / out[1]
@@ -411,12 +426,32 @@ int sv_mlp_grad(const float *params, const float *x, const float *t, const float
  *   particles) of the learned closure (with its fallbacks) / of the fp32
  *   return map, both against the fp64 return map; out[2] / out[3] the same
  *   for the projected F; out[4] particles evaluated, out[5] fallbacks,
- *   out[6] |tau_fp64|, out[7] |F_fp64|.
+ *   out[6] |tau_fp64|, out[7] |F_fp64|, out[8] particles handed to the
+ *   network (yielding, inside the hull), out[9] of which failed the
+ *   residual check, out[10] / out[11] the parts of out[0] from the
+ *   particles the network decided / from the elastic ones (out[0]^2 =
+ *   out[10]^2 + out[11]^2 + the fallbacks' part).
+ * sv_closure_phase_times: per-phase costs on the trial F of the current
+ *   state (mean of 5 launches, ms): out[0] SVD + return map + stress (the
+ *   plain path), out[1] eigen-decomposition + yield test + closed-form
+ *   stress (the learned path without its network), out[2] the network over
+ *   every snow/sand particle, out[3] snow/sand particles, out[4] of which
+ *   yield inside the hull, out[5] the network over those only.
+ * sv_closure_pool: the pool size and the yielding samples of the last
+ *   sv_closure_train (0 before).
+ * sv_closure_get_pool: rows [first, first + count) of the normalised
+ *   training pool of the last sv_closure_train (the yielding samples in
+ *   their shuffled order: X[count][16], Y[count][8]) and the hull (80
+ *   floats: lo[16], hi[16], xm[16], xs[16], ym[8], ys[8]); NULL skips one.
  * sv_closure_get_params: the fp32 master weights (sv_mlp_param_count()). */
 int sv_closure_harvest(sv_handle *h, float dt, uint32_t max_samples, float augment, uint32_t seed,
                        uint64_t *total_out);
 int sv_closure_train(sv_handle *h, uint32_t iterations, uint32_t batch, float lr, uint32_t seed, float *loss_out);
 int sv_closure_set_mode(sv_handle *h, int mode);
+int sv_closure_copy(sv_handle *dst, sv_handle *src);
+int sv_closure_phase_times(sv_handle *h, float dt, double out[6]);
+int sv_closure_pool(sv_handle *h, uint64_t *pairs, uint64_t *yielding);
+int sv_closure_get_pool(sv_handle *h, uint64_t first, uint64_t count, float *X, float *Y, float *hull);
 
 /* No counterpart in the reference: a failure-detection check.  Runs the
  * learned closure's bounded tensor-core wait on a CTA whose MMA commit is
@@ -426,7 +461,7 @@ int sv_closure_set_mode(sv_handle *h, int mode);
  * with "a tensor-core wait of the learned closure timed out".  The GPU
  * context stays usable.  Returns 0 once the kernel has returned. */
 int sv_debug_closure_wait_timeout(sv_handle *h, uint64_t max_cycles);
-int sv_closure_evaluate(sv_handle *h, float dt, double out[8]);
+int sv_closure_evaluate(sv_handle *h, float dt, double out[12]);
 int sv_closure_get_params(sv_handle *h, float *params);
 
 /* ---- Frame files and the frame cache ----------------------------------

@@ -1,8 +1,8 @@
 """Host side of the learned stress closure: thin wrappers over the C ABI.
 
-The network (x 16 -> 32 -> 32 -> 16, ReLU, bf16 tensor-core operands with
-fp32 accumulation) runs only in the CUDA library; these functions move host
-arrays in and out.
+The network (x 16 -> four hidden layers of width 64 with SiLU, bf16
+tensor-core operands with fp32 accumulation -> an fp32 head of 8 outputs)
+runs only in the CUDA library; these functions move host arrays in and out.
 """
 
 from __future__ import annotations
@@ -13,7 +13,7 @@ import numpy as np
 
 from ._abi import check, f32p, load, ptr
 
-NIN, NH, NOUT, N_USED_OUT = 16, 32, 16, 6
+NIN, NH, NOUT, N_USED_OUT = 16, 64, 8, 6
 
 
 def param_count() -> int:
@@ -21,7 +21,7 @@ def param_count() -> int:
 
 
 def mlp_forward(params, x) -> np.ndarray:
-    """y[n, 16] = network(x[n, 16]) on the GPU."""
+    """y[n, 8] = network(x[n, 16]) on the GPU (input 15 is read as 0)."""
     params = np.ascontiguousarray(params, np.float32)
     x = np.ascontiguousarray(x, np.float32).reshape(-1, NIN)
     y = np.zeros((x.shape[0], NOUT), np.float32)

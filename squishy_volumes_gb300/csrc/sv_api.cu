@@ -916,6 +916,9 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     if (!batched && ps[0].collider_bits && pre.any_bits)
         h->collider_bits.assign(ps[0].collider_bits, ps[0].collider_bits + n);
     h->keys_valid = false;
+    // the uploads and fills above ran on the legacy default stream, with
+    // which the handle's non-blocking stream does not synchronise
+    if ((e = cudaDeviceSynchronize())) return cuda_fail(e, "upload");
     *out = h;
     return 0;
 }
@@ -1466,7 +1469,7 @@ int sv_autotune(sv_handle *h, float dt, const float gravity[3], uint32_t substep
             release();
             return fail(std::string("sv_autotune: ") + cudaGetErrorString(e));
         }
-        cudaMemcpy(s.copy, s.dev, s.bytes, cudaMemcpyDeviceToDevice);
+        cudaMemcpyAsync(s.copy, s.dev, s.bytes, cudaMemcpyDeviceToDevice, h->stream);
     }
     const int cur0 = h->cur;
     const uint64_t substeps0 = h->substeps_total, fp64_0 = h->fp64_total;
@@ -1475,12 +1478,13 @@ int sv_autotune(sv_handle *h, float dt, const float gravity[3], uint32_t substep
         h->cur = cur0;
         ParticleArrays &b = h->side[h->cur];
         void *dst[] = {b.pos, b.vel, b.C, b.F, b.energy, b.orig, b.cell};
-        for (size_t i = 0; i < spans.size(); ++i) cudaMemcpy(dst[i], spans[i].copy, spans[i].bytes, cudaMemcpyDeviceToDevice);
+        // on the handle's stream: the kernels that follow read the restored state
+        for (size_t i = 0; i < spans.size(); ++i)
+            cudaMemcpyAsync(dst[i], spans[i].copy, spans[i].bytes, cudaMemcpyDeviceToDevice, h->stream);
         h->pending_valid = false;
         h->keys_valid = false;
         h->since_sort = 0;
-        uint32_t zero = 0;
-        cudaMemcpy(h->counters + C_STATUS, &zero, 4, cudaMemcpyHostToDevice);
+        cudaMemsetAsync(h->counters + C_STATUS, 0, 4, h->stream);
     };
     // Every candidate starts from the snapshot, warms up over two of its
     // binning periods (its first scatter, the CUDA graph capture, the

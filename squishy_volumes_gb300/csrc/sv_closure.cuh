@@ -4,22 +4,34 @@
 // Plain path (the reference's and this library's default): SVD of the trial
 // F, the return map on its singular values, the stress from the projected
 // ones.  Learned path: the principal stretches come from a closed-form
-// eigen-decomposition of F^T F (no iteration), and a small MLP on the tensor
-// cores maps the principal Hencky strains and the material parameters to
-// the projected strains and the principal Kirchhoff stress.  The stress
-// applied is the closed-form Kirchhoff stress of the learned projected
-// stretches; the network's own stress output is the residual check.  A
-// particle outside the training hull, or whose residual check fails, takes
-// the plain path.
+// eigen-decomposition of F^T F (no iteration); the yield test, closed form
+// and cheap, sorts the particle:
+//   elastic  -- the return map leaves the stretches alone: the Kirchhoff
+//               stress of the stretches, no network;
+//   yielding -- the network (4 hidden layers of width 64, SiLU, on the
+//               tensor cores; fp32 head) maps the principal Hencky strains
+//               and the material parameters to the plastic correction of
+//               the strains and the principal Kirchhoff stress of the
+//               projected state.  The stress applied is the closed-form
+//               Kirchhoff stress of the corrected stretches; the network's
+//               own stress output is the residual check.
+// A yielding particle outside the training hull, or whose residual check
+// fails, takes the plain path.
 //
-// Features x (NIN = 16, unused entries 0):
-//   x0..2 = e_i / ES   principal Hencky strains ln sigma_i, sigma descending
-//   x3 = snow, x4 = sand, x5 = (lambda / mu) / 4,
-//   x6 = theta_c / ES, x7 = theta_s / ES (snow), x8 = 4 alpha (sand)
-// Targets y (first N_USED_OUT = 6 outputs):
-//   y0..2 = (ln s_i - e_i) / ES   plastic correction of the strains
-//   y3..5 = tau_i / (mu h) / TS   principal Kirchhoff stress of the
-//                                 projected state, h the snow hardening
+// Raw features (the network sees (x - xm) xs, both from the training pool):
+//   x0..2 = e_i    principal Hencky strains ln sigma_i, sigma descending
+//   x3 = snow, x4 = sand, x5 = lambda / mu,
+//   x6 = theta_c, x7 = theta_s (snow), x8 = alpha (sand),
+//   x9..11 = the branch of each stretch under the snow limits (-1 below
+//            1 - theta_c, +1 above 1 + theta_s, 0 between; 0 for sand),
+//   x12 = 1 on sand's expansion / hydrostatic branch (0 otherwise);
+//   x13..15 = 0.  The branch features come from the closed-form yield test:
+//   with them the network fits a function that is smooth on each branch
+//   instead of locating the branches' kinks itself.
+// Raw targets (the network predicts (y - ym) / ys):
+//   y0..2 = ln s_i - e_i            plastic correction of the strains
+//   y3..5 = tau_i / (mu h)          principal Kirchhoff stress of the
+//                                   projected state, h the snow hardening
 #pragma once
 #include "sv_math.cuh"
 #include "sv_tc.cuh"
@@ -27,29 +39,39 @@
 namespace sv {
 namespace closure {
 
-constexpr float ES = 0.05f;
-constexpr float TS = 0.1f;
-constexpr float RES_TOL = 5e-3f;  // |tau_net - tau(s)| / (mu h), max over i
-constexpr int N_FEAT = 9;         // features that carry information
+constexpr float RES_TOL = 1e-3f;  // |tau_net - tau(s)| / (mu h), max over i
+constexpr int N_FEAT = 13;        // features that carry information
 
+// The accepted feature range (lo, hi) and the normalisation of the inputs
+// and outputs, all from the training pool.
 struct Hull {
     float lo[tc::NIN], hi[tc::NIN];
+    float xm[tc::NIN], xs[tc::NIN];
+    float ym[tc::NOUT], ys[tc::NOUT];
 };
+
+enum LearnedClass { L_PLAIN = 0, L_ELASTIC = 1, L_NET = 2 };
 
 __host__ __device__ inline bool applies(uint32_t kind) { return kind == KIND_SNOW || kind == KIND_SAND; }
 
 __host__ __device__ inline void features(const Material &m, const float e[3], float x[tc::NIN]) {
     for (int k = 0; k < tc::NIN; ++k) x[k] = 0.f;
-    x[0] = e[0] / ES, x[1] = e[1] / ES, x[2] = e[2] / ES;
+    x[0] = e[0], x[1] = e[1], x[2] = e[2];
     const bool snow = m.kind == KIND_SNOW;
     x[3] = snow ? 1.f : 0.f;
     x[4] = snow ? 0.f : 1.f;
-    x[5] = m.mu > 0.f ? m.lambda / m.mu / 4.f : 0.f;
+    x[5] = m.mu > 0.f ? m.lambda / m.mu : 0.f;
     if (snow) {
-        x[6] = m.theta_c / ES;
-        x[7] = m.theta_s / ES;
+        x[6] = m.theta_c;
+        x[7] = m.theta_s;
+        const float lo = logf(1.f - m.theta_c), hi = logf(1.f + m.theta_s);
+        for (int k = 0; k < 3; ++k) x[9 + k] = e[k] < lo ? -1.f : (e[k] > hi ? 1.f : 0.f);
     } else {
-        x[8] = 4.f * m.alpha;
+        x[8] = m.alpha;
+        const float e_tr = e[0] + e[1] + e[2];
+        float eh2 = 0.f;
+        for (int k = 0; k < 3; ++k) eh2 += (e[k] - e_tr / 3.f) * (e[k] - e_tr / 3.f);
+        x[12] = (e_tr < 0.f && eh2 > 0.f) ? 0.f : 1.f;
     }
 }
 
@@ -75,7 +97,7 @@ template <class T> __host__ __device__ inline void return_map(const Material &m,
     const T ehn = sqrt(eh[0] * eh[0] + eh[1] * eh[1] + eh[2] * eh[2]);
     if (e_tr < T(0) && ehn > T(0)) {
         // mu <= 0: the reference asserts mu > 0 (advance_particles.rs:57);
-        // such particles never take the learned path (outside any hull)
+        // such particles never take the learned path
         if (!((T)m.mu > T(0))) return;
         const T dg = ehn + (T(3) * (T)m.lambda + T(2) * (T)m.mu) / T(2) / (T)m.mu * e_tr * (T)m.alpha;
         if (dg > T(0))
@@ -83,6 +105,26 @@ template <class T> __host__ __device__ inline void return_map(const Material &m,
     } else {
         s[0] = s[1] = s[2] = T(1);
     }
+}
+
+// The closed-form yield test: true when the return map changes the
+// stretches (snow: one outside [1 - theta_c, 1 + theta_s]; sand: the
+// expansion / hydrostatic branch, or a positive Drucker-Prager yield
+// function on the compressive branch).  Needs mu > 0 for sand.
+template <class T> __host__ __device__ inline bool yields(const Material &m, const T sig[3]) {
+    if (m.kind == KIND_SNOW) {
+        const T lo = T(1) - (T)m.theta_c, hi = T(1) + (T)m.theta_s;
+        return sig[0] < lo || sig[0] > hi || sig[1] < lo || sig[1] > hi || sig[2] < lo || sig[2] > hi;
+    }
+    T e[3];
+    for (int k = 0; k < 3; ++k) e[k] = log(sig[k]);
+    const T e_tr = e[0] + e[1] + e[2];
+    T eh[3];
+    for (int k = 0; k < 3; ++k) eh[k] = e[k] - e_tr / T(3);
+    const T ehn = sqrt(eh[0] * eh[0] + eh[1] * eh[1] + eh[2] * eh[2]);
+    if (!(e_tr < T(0) && ehn > T(0))) return !(sig[0] == T(1) && sig[1] == T(1) && sig[2] == T(1));  // s = 1
+    const T dg = ehn + (T(3) * (T)m.lambda + T(2) * (T)m.mu) / T(2) / (T)m.mu * e_tr * (T)m.alpha;
+    return dg > T(0);
 }
 
 // Hardening factor of the projected state and the updated plastic J (snow).
@@ -119,7 +161,7 @@ template <class T> __host__ __device__ inline T energy(const Material &m, const 
     return (T)m.mu / T(2) * (s[0] * s[0] + s[1] * s[1] + s[2] * s[2] - T(3)) - (T)m.mu * lj + (T)m.lambda / T(2) * lj * lj;
 }
 
-// Training targets from the principal stretches (double precision).
+// Raw training targets from the principal stretches (double precision).
 __host__ __device__ inline void targets(const Material &m, const double sig[3], double jp, float y[tc::NOUT]) {
     double s[3], tau[3], jp_out;
     return_map<double>(m, sig, s);
@@ -128,16 +170,18 @@ __host__ __device__ inline void targets(const Material &m, const double sig[3], 
     for (int k = 0; k < tc::NOUT; ++k) y[k] = 0.f;
     const double muh = (double)m.mu * h;
     for (int k = 0; k < 3; ++k) {
-        y[k] = (float)((log(s[k]) - log(sig[k])) / ES);
-        y[3 + k] = muh > 0 ? (float)(tau[k] / muh / TS) : 0.f;
+        y[k] = (float)(log(s[k]) - log(sig[k]));
+        y[3 + k] = muh > 0 ? (float)(tau[k] / muh) : 0.f;
     }
 }
 
 // Learned path, part 1: principal stretches of the trial F from the
-// closed-form eigen-decomposition of F^T F, and the features.  Returns false
-// when the particle must take the plain path (outside the hull).
-__device__ __forceinline__ bool learned_features(const Material &m, const m3f &F, const Hull &hull, float sig[3],
-                                                 float V[9], float x[tc::NIN]) {
+// closed-form eigen-decomposition of F^T F, the yield test, and the
+// normalised features of a yielding particle.  Returns L_PLAIN when the
+// particle must take the plain path (degenerate F, mu <= 0, outside the
+// hull), L_ELASTIC when the stretches stand, L_NET when the network decides.
+__device__ __forceinline__ int learned_features(const Material &m, const m3f &F, const Hull &hull, float sig[3],
+                                                float V[9], float x[tc::NIN]) {
     float c[6];  // F^T F: column dot products (column-major F)
     const float *a = F.a;
     c[0] = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
@@ -148,37 +192,43 @@ __device__ __forceinline__ bool learned_features(const Material &m, const m3f &F
     c[5] = a[6] * a[6] + a[7] * a[7] + a[8] * a[8];
     float lam[3];
     sym_eig3(c, lam, V);
-    if (!(lam[2] > 0.f) || !(lam[0] < 1e30f)) return false;
+    if (!(lam[2] > 0.f) || !(lam[0] < 1e30f) || !(m.mu > 0.f)) return L_PLAIN;
     float e[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         sig[k] = sqrtf(lam[k]);
         e[k] = 0.5f * logf(lam[k]);
     }
+    if (!yields<float>(m, sig)) return L_ELASTIC;
     features(m, e, x);
 #pragma unroll
-    for (int k = 0; k < N_FEAT; ++k)
-        if (!(x[k] >= hull.lo[k] && x[k] <= hull.hi[k])) return false;
-    return true;
+    for (int k = 0; k < N_FEAT; ++k) {
+        if (!(x[k] >= hull.lo[k] && x[k] <= hull.hi[k])) return L_PLAIN;
+        x[k] = (x[k] - hull.xm[k]) * hull.xs[k];
+    }
+    return L_NET;
 }
 
-// Learned path, part 2: from the network output y, the projected F, the
-// Kirchhoff stress tensor P F^T (= tau), the energy and the plastic J.
-// Returns false when the residual check fails.
+// Learned path, part 2: from the network output y (normalised; NULL for
+// an elastic particle: the stretches stand), the projected F, the Kirchhoff
+// stress tensor P F^T (= tau), the energy and the plastic J.  Returns false
+// when the residual check fails.
 __device__ __forceinline__ bool learned_apply(const Material &m, const m3f &F, const float sig[3], const float V[9],
-                                              const float y[tc::NOUT], float jp_in, m3f &Fnew, m3f &tau_t,
+                                              const float *y, const Hull &hull, float jp_in, m3f &Fnew, m3f &tau_t,
                                               float &energy_out, float &jp_out, float &J_out) {
     float s[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) s[k] = sig[k] * expf(ES * y[k]);
+    for (int k = 0; k < 3; ++k) s[k] = y ? sig[k] * expf(hull.ym[k] + hull.ys[k] * y[k]) : sig[k];
     const float h = hardening<float>(m, sig, s, jp_in, jp_out);
     float tau[3];
     kirchhoff<float>(m, s, h, tau);
-    const float muh = m.mu * h;
-    float res = 0.f;
+    if (y) {
+        const float muh = m.mu * h;
+        float res = 0.f;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) res = fmaxf(res, fabsf(TS * y[3 + k] - tau[k] / muh));
-    if (!(res <= RES_TOL)) return false;
+        for (int k = 0; k < 3; ++k) res = fmaxf(res, fabsf(hull.ym[3 + k] + hull.ys[3 + k] * y[3 + k] - tau[k] / muh));
+        if (!(res <= RES_TOL)) return false;
+    }
     // G = F V; F' = G diag(s / sig) V^T; tau = G diag(tau / sig^2) G^T
     float G[9];
 #pragma unroll

@@ -267,6 +267,9 @@ extern "C" int sv_set_frame_input(sv_handle *h, const sv_frame_input *in) {
         }
         h->var_cap = cap;
     }
+    // the uploads and fills above ran on the legacy default stream, with
+    // which the handle's non-blocking stream does not synchronise
+    FR_CUDA(cudaDeviceSynchronize());
     h->fin_active = true;
     return 0;
 }

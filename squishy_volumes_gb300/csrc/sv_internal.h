@@ -283,6 +283,7 @@ struct sv_handle {
     float *cl_X = nullptr, *cl_Y = nullptr, *cl_W = nullptr;  // features, targets, weights
     uint64_t cl_xy_cap = 0;
     int cl_step = 0;                // Adam steps taken
+    uint64_t cl_yielding = 0;       // yielding (weighted) samples of the last labelling
     float *cl_loss = nullptr;       // device scalar
     uint32_t *cl_err = nullptr;     // device flag
     uint64_t *cl_count = nullptr;   // device counter of the harvest

@@ -4,9 +4,10 @@
 // stateless C entry points sv_mlp_forward / sv_mlp_grad used to check the
 // kernels against a CPU evaluation of the same network.
 //
-// Precision: weights and activations enter the tensor core as bf16, every
-// product is accumulated in fp32 (TMEM), biases, ReLU, the loss and the Adam
-// state are fp32.
+// Precision: weights and activations of the hidden layers enter the tensor
+// core as bf16, every product is accumulated in fp32 (TMEM); biases, SiLU,
+// the head (which reads the last hidden layer in fp32), the loss and the
+// Adam state are fp32.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -33,22 +34,30 @@ __device__ __forceinline__ void put_bf16(uint8_t *img, int off, float v) {
 // Writes master parameter `idx` (value v) into the packed image.
 __device__ __forceinline__ void image_write(uint8_t *img, int idx, float v) {
     if (idx < P_B1) {
-        const int r = idx / NIN, k = idx % NIN;
+        const int r = idx / NIN, k = idx % NIN;  // W1[r][k]: out r, in k
         put_bf16(img, IMG_W1 + kmaj(r, k, NIN), v);
-    } else if (idx < P_W2) {
-        reinterpret_cast<float *>(img + IMG_B1)[idx - P_B1] = v;
-    } else if (idx < P_B2) {
-        const int e = idx - P_W2, r = e / NH, k = e % NH;  // W2[r][k]: out r, in k
-        put_bf16(img, IMG_W2 + kmaj(r, k, NH), v);
-        put_bf16(img, IMG_W2T + kmaj(k, r, NH), v);
-    } else if (idx < P_W3) {
-        reinterpret_cast<float *>(img + IMG_B2)[idx - P_B2] = v;
-    } else if (idx < P_B3) {
-        const int e = idx - P_W3, r = e / NH, k = e % NH;  // W3[r][k]: out r, in k
-        put_bf16(img, IMG_W3 + kmaj(r, k, NH), v);
-        put_bf16(img, IMG_W3T + kmaj(k, r, NOUT), v);
-    } else {
-        reinterpret_cast<float *>(img + IMG_B3)[idx - P_B3] = v;
+        return;
+    }
+    if (idx >= P_W5) {
+        if (idx < P_B5) reinterpret_cast<float *>(img + IMG_W5)[idx - P_W5] = v;
+        else reinterpret_cast<float *>(img + IMG_B5)[idx - P_B5] = v;
+        return;
+    }
+    for (int layer = 1; layer <= N_HIDDEN; ++layer) {
+        const int pb = p_bias(layer);
+        if (idx >= pb && idx < pb + NH) {
+            reinterpret_cast<float *>(img + IMG_BH)[(layer - 1) * NH + idx - pb] = v;
+            return;
+        }
+        if (layer >= 2) {
+            const int pw = p_weight(layer);
+            if (idx >= pw && idx < pw + NH * NH) {
+                const int e = idx - pw, r = e / NH, k = e % NH;  // out r, in k
+                put_bf16(img, img_weight(layer) + kmaj(r, k, NH), v);
+                put_bf16(img, img_weight_t(layer) + kmaj(k, r, NH), v);
+                return;
+            }
+        }
     }
 }
 
@@ -79,13 +88,16 @@ __device__ __forceinline__ void copy_to_smem(uint8_t *dst, const uint8_t *src, i
 }
 
 // ------------------------------------------------------------------ forward
+// Dynamic shared memory: the forward image, then the two operand buffers.
+constexpr int FW_A0 = IMG_FWD_BYTES;
+constexpr int FW_A1 = FW_A0 + T * NIN * 2;
+constexpr int FW_BYTES = FW_A1 + T * NH * 2;
+
 __global__ void __launch_bounds__(T) k_mlp_forward(const uint8_t *img, const float *X, uint64_t n, float *Y,
                                                    uint32_t *err) {
-    __shared__ __align__(1024) uint8_t s_img[IMG_BYTES];
-    __shared__ __align__(1024) uint8_t s_a0[T * NIN * 2];
-    __shared__ __align__(1024) uint8_t s_a1[T * NH * 2];
+    extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ Ctl ctl;
-    copy_to_smem(s_img, img, IMG_BYTES);
+    copy_to_smem(sm, img, IMG_FWD_BYTES);
     ctl_init(ctl, TMEM_COLS_INFER);
     Phase ph;
     const uint64_t tiles = (n + T - 1) / T;
@@ -93,8 +105,8 @@ __global__ void __launch_bounds__(T) k_mlp_forward(const uint8_t *img, const flo
         const uint64_t row = tile * T + threadIdx.x;
         float x[NIN], y[NOUT];
 #pragma unroll
-        for (int k = 0; k < NIN; ++k) x[k] = row < n ? X[row * NIN + k] : 0.f;
-        infer_tile(ctl, ph, s_img, s_a0, s_a1, x, y);
+        for (int k = 0; k < NIN; ++k) x[k] = (row < n && k < NIN - 1) ? X[row * NIN + k] : 0.f;  // input 15 reserved
+        infer_tile(ctl, ph, sm, sm + FW_A0, sm + FW_A1, x, y);
         if (row < n)
 #pragma unroll
             for (int k = 0; k < NOUT; ++k) Y[row * NOUT + k] = y[k];
@@ -103,172 +115,216 @@ __global__ void __launch_bounds__(T) k_mlp_forward(const uint8_t *img, const flo
 }
 
 // ------------------------------------------------------------------ training
-// Dynamic shared memory of the training kernel (operand buffers 1 KB aligned).
+// Dynamic shared memory of the training kernel.  K-major bf16 operands:
+//   A0   X              [128 samples x NIN]     layer 1 (forward, recompute)
+//   AH   H_l            [128 x NH]              the next layer's A operand
+//   G    dZ_l           [128 x NH]              A operand of dH_(l-1) = dZ_l W_l
+//   TA   H4^T, dZ_l^T   [128 rows x 128 samples] A operand of the weight
+//        gradients (rows = units; row NH is ones: dW5^T's row NH is db5)
+//   DYT  dY^T           [16 x 128 samples]      B operand of dW5^T
+//   TB0  X^T            [NIN x 128]             row NIN-1 is ones (db1)
+//   TB1..TB3 H_l^T      [NH + 16 x 128]          row NH is ones (db2..db4)
+constexpr int TB_ROWS = NH + 16;
 constexpr int TR_IMG = 0;
-constexpr int TR_A0 = 8192;                     // X tile          [128 x NIN]
-constexpr int TR_A1 = TR_A0 + T * NIN * 2;      // H1              [128 x NH]
-constexpr int TR_A2 = TR_A1 + T * NH * 2;       // H2              [128 x NH]
-constexpr int TR_G3 = TR_A2 + T * NH * 2;       // dY              [128 x NOUT]
-constexpr int TR_G2 = TR_G3 + T * NOUT * 2;     // dZ2             [128 x NH]
-constexpr int TR_TA = TR_G2 + T * NH * 2;       // dY^T / dZ2^T / dZ1^T [128 rows x 128 samples]
-constexpr int TR_TB2 = TR_TA + T * T * 2;       // H2^T            [NH x 128]
-constexpr int TR_TB1 = TR_TB2 + NH * T * 2;     // H1^T            [NH x 128]
-constexpr int TR_TB0 = TR_TB1 + NH * T * 2;     // X^T             [NIN x 128]
-constexpr int TR_DB = TR_TB0 + NIN * T * 2;     // bias gradient sums (fp32)
-constexpr int TR_BYTES = TR_DB + (NH + NH + NOUT + 1) * 4;
-static_assert(IMG_BYTES <= TR_A0, "image slot");
-// TMEM columns: layer outputs / backward products, then the three weight
-// gradient accumulators (rows = output units of the layer).
-constexpr int TM_OUT = 0, TM_DW2 = 32, TM_DW3 = 64, TM_DW1 = 96, TM_COLS = 128;
+constexpr int TR_A0 = IMG_BYTES;
+constexpr int TR_AH = TR_A0 + T * NIN * 2;
+constexpr int TR_G = TR_AH + T * NH * 2;
+constexpr int TR_TA = TR_G + T * NH * 2;
+constexpr int TR_DYT = TR_TA + T * T * 2;
+constexpr int TR_TB0 = TR_DYT + 16 * T * 2;
+constexpr int TR_TB1 = TR_TB0 + NIN * T * 2;
+constexpr int TR_TB2 = TR_TB1 + TB_ROWS * T * 2;
+constexpr int TR_TB3 = TR_TB2 + TB_ROWS * T * 2;
+constexpr int TR_BYTES = TR_TB3 + TB_ROWS * T * 2;
+static_assert(TR_A0 % 128 == 0 && TR_TA % 128 == 0 && TR_BYTES <= 227 * 1024, "training shared memory");
+// TMEM columns: the pre-activations z2..z4 (z1 lands in Z3's columns in the
+// forward pass and is recomputed there in the backward pass; each input
+// gradient reuses the columns of the layer it was taken from), then the
+// weight-gradient accumulators (rows = output units; their last used column
+// is the bias gradient).
+constexpr int TM_Z2 = 0, TM_Z3 = 64, TM_Z4 = 128;
+constexpr int TM_DW2 = 192, TM_DW3 = TM_DW2 + TB_ROWS, TM_DW4 = TM_DW3 + TB_ROWS;
+constexpr int TM_DW1 = TM_DW4 + TB_ROWS, TM_DW5 = TM_DW1 + 16, TM_COLS = 512;
+static_assert(TM_DW5 + 16 <= TM_COLS, "TMEM columns");
 
-__device__ __forceinline__ void store_col_t(uint8_t *buf, int t, const float *v, int rows) {
-    // column t (sample) of a [rows x 128] K-major operand
-    for (int r = 0; r < rows; ++r) put_bf16(buf, kmaj(r, t, T), v[r]);
-}
+__device__ __forceinline__ void put_col(uint8_t *buf, int t, int r, float v) { put_bf16(buf, kmaj(r, t, T), v); }
 
 __global__ void __launch_bounds__(T) k_mlp_train(const uint8_t *img, const float *X, const float *Ytgt,
                                                  const float *Wt, uint64_t n, float inv_n, float *grad, float *loss,
                                                  float *Yout, uint32_t *err) {
     extern __shared__ __align__(1024) uint8_t sm[];
     __shared__ Ctl ctl;
+    const int t = threadIdx.x;
     uint8_t *s_img = sm + TR_IMG;
-    float *s_db = reinterpret_cast<float *>(sm + TR_DB);
     copy_to_smem(s_img, img, IMG_BYTES);
-    for (int i = threadIdx.x; i < NH + NH + NOUT + 1; i += T) s_db[i] = 0.f;
+    // the constant rows: ones for the bias gradients, zero padding
+    put_col(sm + TR_TB0, t, NIN - 1, 1.f);
+    for (int r = NH; r < TB_ROWS; ++r) {
+        const float v = r == NH ? 1.f : 0.f;
+        put_col(sm + TR_TB1, t, r, v), put_col(sm + TR_TB2, t, r, v), put_col(sm + TR_TB3, t, r, v);
+    }
+    for (int r = NH; r < T; ++r) put_col(sm + TR_TA, t, r, r == NH ? 1.f : 0.f);
+    for (int r = NOUT; r < 16; ++r) put_col(sm + TR_DYT, t, r, 0.f);
     ctl_init(ctl, TM_COLS);
     Phase ph;
-    const int t = threadIdx.x;
     const uint32_t tm = ctl.tmem;
+    const float *bh = reinterpret_cast<const float *>(s_img + IMG_BH);
+    const float *w5 = reinterpret_cast<const float *>(s_img + IMG_W5);
+    const float *b5 = reinterpret_cast<const float *>(s_img + IMG_B5);
     const uint64_t tiles = (n + T - 1) / T;
     bool first = true;
     float lsum = 0.f;
-    const float *b1 = reinterpret_cast<const float *>(s_img + IMG_B1);
-    const float *b2 = reinterpret_cast<const float *>(s_img + IMG_B2);
-    const float *b3 = reinterpret_cast<const float *>(s_img + IMG_B3);
     for (uint64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const uint64_t row = tile * T + t;
         const bool valid = row < n;
         float x[NIN];
 #pragma unroll
-        for (int k = 0; k < NIN; ++k) x[k] = valid ? X[row * NIN + k] : 0.f;
+        for (int k = 0; k < NIN; ++k) x[k] = (valid && k < NIN - 1) ? X[row * NIN + k] : 0.f;  // input 15 reserved
         store_row8(sm + TR_A0, t, 0, NIN, x);
         store_row8(sm + TR_A0, t, 8, NIN, x + 8);
-        store_col_t(sm + TR_TB0, t, x, NIN);
-        // layer 1
-        if (!issue(ctl, ph, [&] { mma_bf16(tm + TM_OUT, smem_u32(sm + TR_A0), smem_u32(s_img + IMG_W1), NIN, NH, false); }))
+        for (int r = 0; r < NIN - 1; ++r) put_col(sm + TR_TB0, t, r, x[r]);
+        // ---- forward: hidden layers 1..3 into AH and TB1..TB3
+        if (!issue(ctl, ph, [&] { mma_bf16(tm + TM_Z3, smem_u32(sm + TR_A0), smem_u32(s_img + IMG_W1), NIN, NH, false); }))
             break;
-        float h1[NH];
-        tmem_ld16(tmem_lane_addr(tm, TM_OUT), h1);
-        tmem_ld16(tmem_lane_addr(tm, TM_OUT + 16), h1 + 16);
-        uint32_t mask1 = 0;
-#pragma unroll
-        for (int j = 0; j < NH; ++j) {
-            const float z = h1[j] + b1[j];
-            mask1 |= (z > 0.f ? 1u : 0u) << j;
-            h1[j] = fmaxf(z, 0.f);
+        bool ok = true;
+#pragma unroll 1
+        for (int layer = 1; layer <= 3 && ok; ++layer) {
+            const int zc = layer == 1 ? TM_Z3 : layer == 2 ? TM_Z2 : TM_Z3;
+            uint8_t *tb = sm + (layer == 1 ? TR_TB1 : layer == 2 ? TR_TB2 : TR_TB3);
+            for (int q = 0; q < NH / 16; ++q) {
+                float h[16];
+                tmem_ld16(tmem_lane_addr(tm, zc + 16 * q), h);
+                for (int j = 0; j < 16; ++j) {
+                    const float z = h[j] + bh[(layer - 1) * NH + 16 * q + j];
+                    h[j] = z * sigmoid_f(z);
+                    put_col(tb, t, 16 * q + j, h[j]);
+                }
+                store_row8(sm + TR_AH, t, 16 * q, NH, h);
+                store_row8(sm + TR_AH, t, 16 * q + 8, NH, h + 8);
+            }
+            const int dst = layer == 1 ? TM_Z2 : layer == 2 ? TM_Z3 : TM_Z4;
+            ok = issue(ctl, ph, [&] {
+                mma_bf16(tm + dst, smem_u32(sm + TR_AH), smem_u32(s_img + img_weight(layer + 1)), NH, NH, false);
+            });
         }
-#pragma unroll
-        for (int c = 0; c < NH / 8; ++c) store_row8(sm + TR_A1, t, 8 * c, NH, h1 + 8 * c);
-        store_col_t(sm + TR_TB1, t, h1, NH);
-        // layer 2
-        if (!issue(ctl, ph, [&] { mma_bf16(tm + TM_OUT, smem_u32(sm + TR_A1), smem_u32(s_img + IMG_W2), NH, NH, false); }))
-            break;
-        float h2[NH];
-        tmem_ld16(tmem_lane_addr(tm, TM_OUT), h2);
-        tmem_ld16(tmem_lane_addr(tm, TM_OUT + 16), h2 + 16);
-        uint32_t mask2 = 0;
-#pragma unroll
-        for (int j = 0; j < NH; ++j) {
-            const float z = h2[j] + b2[j];
-            mask2 |= (z > 0.f ? 1u : 0u) << j;
-            h2[j] = fmaxf(z, 0.f);
-        }
-#pragma unroll
-        for (int c = 0; c < NH / 8; ++c) store_row8(sm + TR_A2, t, 8 * c, NH, h2 + 8 * c);
-        store_col_t(sm + TR_TB2, t, h2, NH);
-        // layer 3
-        if (!issue(ctl, ph, [&] { mma_bf16(tm + TM_OUT, smem_u32(sm + TR_A2), smem_u32(s_img + IMG_W3), NH, NOUT, false); }))
-            break;
+        if (!ok) break;
+        // ---- layer 4 and the fp32 head; h4^T into TA for dW5^T
         float y[NOUT];
-        tmem_ld16(tmem_lane_addr(tm, TM_OUT), y);
+        for (int o = 0; o < NOUT; ++o) y[o] = b5[o];
+        for (int q = 0; q < NH / 16; ++q) {
+            float h[16];
+            tmem_ld16(tmem_lane_addr(tm, TM_Z4 + 16 * q), h);
+            for (int j = 0; j < 16; ++j) {
+                const float z = h[j] + bh[3 * NH + 16 * q + j];
+                h[j] = z * sigmoid_f(z);
+                put_col(sm + TR_TA, t, 16 * q + j, h[j]);
+            }
+            for (int o = 0; o < NOUT; ++o) {
+                float acc = y[o];
+                for (int j = 0; j < 16; ++j) acc = fmaf(w5[o * NH + 16 * q + j], h[j], acc);
+                y[o] = acc;
+            }
+        }
         // loss = sum_rows w sum_{o < N_USED_OUT} (y - t)^2 * inv_n
         float dy[NOUT];
-        const float wr = valid ? Wt[row] : 0.f;
-#pragma unroll
+        const float wr = valid ? (Wt ? Wt[row] : 1.f) : 0.f;
         for (int o = 0; o < NOUT; ++o) {
-            y[o] += b3[o];
             const float tg = (valid && o < N_USED_OUT) ? Ytgt[row * NOUT + o] : y[o];
             const float d = y[o] - tg;
             lsum += wr * d * d * inv_n;
             dy[o] = (o < N_USED_OUT) ? 2.f * wr * d * inv_n : 0.f;
+            put_col(sm + TR_DYT, t, o, dy[o]);
         }
         if (Yout && valid)
-#pragma unroll
             for (int o = 0; o < NOUT; ++o) Yout[row * NOUT + o] = y[o];
-#pragma unroll
-        for (int o = 0; o < NOUT; ++o) atomicAdd(&s_db[NH + NH + o], dy[o]);
-        store_row8(sm + TR_G3, t, 0, NOUT, dy);
-        store_row8(sm + TR_G3, t, 8, NOUT, dy + 8);
-        store_col_t(sm + TR_TA, t, dy, NOUT);
-        // dH2 = dY W3, dW3 (+)= dY^T H2
+        // dW5^T (+)= H4^T dY (row NH: db5)
         if (!issue(ctl, ph, [&] {
-                mma_bf16(tm + TM_OUT, smem_u32(sm + TR_G3), smem_u32(s_img + IMG_W3T), NOUT, NH, false);
-                mma_bf16(tm + TM_DW3, smem_u32(sm + TR_TA), smem_u32(sm + TR_TB2), T, NH, !first);
+                mma_bf16(tm + TM_DW5, smem_u32(sm + TR_TA), smem_u32(sm + TR_DYT), T, 16, !first);
             }))
             break;
-        float g2[NH];
-        tmem_ld16(tmem_lane_addr(tm, TM_OUT), g2);
-        tmem_ld16(tmem_lane_addr(tm, TM_OUT + 16), g2 + 16);
-#pragma unroll
-        for (int j = 0; j < NH; ++j) {
-            g2[j] = ((mask2 >> j) & 1u) ? g2[j] : 0.f;
-            atomicAdd(&s_db[NH + j], g2[j]);
+        // ---- backward through layers 4..1
+#pragma unroll 1
+        for (int layer = 4; layer >= 1 && ok; --layer) {
+            // the layer's pre-activation and the gradient of its output
+            const int zc = layer == 4 ? TM_Z4 : layer == 3 ? TM_Z3 : layer == 2 ? TM_Z2 : TM_Z3;
+            const int gc = layer == 3 ? TM_Z4 : layer == 2 ? TM_Z3 : TM_Z2;  // dH_layer (layers 1..3)
+            for (int q = 0; q < NH / 16; ++q) {
+                float z[16], dh[16];
+                tmem_ld16(tmem_lane_addr(tm, zc + 16 * q), z);
+                if (layer == 4) {
+                    for (int j = 0; j < 16; ++j) {
+                        float a = 0.f;
+                        for (int o = 0; o < N_USED_OUT; ++o) a = fmaf(dy[o], w5[o * NH + 16 * q + j], a);
+                        dh[j] = a;
+                    }
+                } else {
+                    tmem_ld16(tmem_lane_addr(tm, gc + 16 * q), dh);
+                }
+                for (int j = 0; j < 16; ++j) {
+                    const float zz = z[j] + bh[(layer - 1) * NH + 16 * q + j];
+                    const float sg = sigmoid_f(zz);
+                    dh[j] *= sg * (1.f + zz * (1.f - sg));  // dZ
+                    put_col(sm + TR_TA, t, 16 * q + j, dh[j]);
+                }
+                if (layer > 1) {
+                    store_row8(sm + TR_G, t, 16 * q, NH, dh);
+                    store_row8(sm + TR_G, t, 16 * q + 8, NH, dh + 8);
+                }
+            }
+            if (layer == 4) {
+                ok = issue(ctl, ph, [&] {
+                    mma_bf16(tm + TM_Z4, smem_u32(sm + TR_G), smem_u32(s_img + IMG_W4T), NH, NH, false);
+                    mma_bf16(tm + TM_DW4, smem_u32(sm + TR_TA), smem_u32(sm + TR_TB3), T, TB_ROWS, !first);
+                });
+            } else if (layer == 3) {
+                ok = issue(ctl, ph, [&] {
+                    mma_bf16(tm + TM_Z3, smem_u32(sm + TR_G), smem_u32(s_img + IMG_W3T), NH, NH, false);
+                    mma_bf16(tm + TM_DW3, smem_u32(sm + TR_TA), smem_u32(sm + TR_TB2), T, TB_ROWS, !first);
+                });
+            } else if (layer == 2) {
+                // dH1, dW2, and z1 recomputed into Z3's columns
+                ok = issue(ctl, ph, [&] {
+                    mma_bf16(tm + TM_Z2, smem_u32(sm + TR_G), smem_u32(s_img + IMG_W2T), NH, NH, false);
+                    mma_bf16(tm + TM_DW2, smem_u32(sm + TR_TA), smem_u32(sm + TR_TB1), T, TB_ROWS, !first);
+                    mma_bf16(tm + TM_Z3, smem_u32(sm + TR_A0), smem_u32(s_img + IMG_W1), NIN, NH, false);
+                });
+            } else {
+                ok = issue(ctl, ph, [&] {
+                    mma_bf16(tm + TM_DW1, smem_u32(sm + TR_TA), smem_u32(sm + TR_TB0), T, NIN, !first);
+                });
+            }
         }
-#pragma unroll
-        for (int c = 0; c < NH / 8; ++c) store_row8(sm + TR_G2, t, 8 * c, NH, g2 + 8 * c);
-        store_col_t(sm + TR_TA, t, g2, NH);
-        // dH1 = dZ2 W2, dW2 (+)= dZ2^T H1
-        if (!issue(ctl, ph, [&] {
-                mma_bf16(tm + TM_OUT, smem_u32(sm + TR_G2), smem_u32(s_img + IMG_W2T), NH, NH, false);
-                mma_bf16(tm + TM_DW2, smem_u32(sm + TR_TA), smem_u32(sm + TR_TB1), T, NH, !first);
-            }))
-            break;
-        float g1[NH];
-        tmem_ld16(tmem_lane_addr(tm, TM_OUT), g1);
-        tmem_ld16(tmem_lane_addr(tm, TM_OUT + 16), g1 + 16);
-#pragma unroll
-        for (int j = 0; j < NH; ++j) {
-            g1[j] = ((mask1 >> j) & 1u) ? g1[j] : 0.f;
-            atomicAdd(&s_db[j], g1[j]);
-        }
-        store_col_t(sm + TR_TA, t, g1, NH);
-        // dW1 (+)= dZ1^T X
-        if (!issue(ctl, ph, [&] { mma_bf16(tm + TM_DW1, smem_u32(sm + TR_TA), smem_u32(sm + TR_TB0), T, NIN, !first); }))
-            break;
+        if (!ok) break;
         first = false;
     }
-    // weight gradients: warp 0 reads rows 0..31 of the accumulators
+    // weight gradients: threads t < NH read row t of each accumulator (the
+    // rows of the output units); column NH (NIN - 1 for layer 1) is the bias
     fence_before();
     __syncthreads();
     fence_after();
-    if (!first && !ctl.abort && threadIdx.x < 32) {  // abort is uniform after the barrier
+    if (!first && !ctl.abort && t < 96) {  // warps 0..2 (abort is uniform after the barrier)
         float r[16];
-        for (int c = 0; c < NH; c += 16) {  // dW2[t][c..c+15]
-            tmem_ld16(tmem_lane_addr(tm, TM_DW2 + c), r);
-            for (int k = 0; k < 16; ++k) atomicAdd(&grad[P_W2 + t * NH + c + k], r[k]);
+        for (int layer = 2; layer <= 4; ++layer) {
+            const int col0 = layer == 2 ? TM_DW2 : layer == 3 ? TM_DW3 : TM_DW4;
+            for (int c = 0; c < TB_ROWS; c += 16) {
+                tmem_ld16(tmem_lane_addr(tm, col0 + c), r);
+                if (t < NH)
+                    for (int k = 0; k < 16; ++k) {
+                        if (c + k < NH) atomicAdd(&grad[p_weight(layer) + t * NH + c + k], r[k]);
+                        else if (c + k == NH) atomicAdd(&grad[p_bias(layer) + t], r[k]);
+                    }
+            }
         }
-        for (int c = 0; c < NH; c += 16) {  // dW3[t][..] for t < NOUT
-            tmem_ld16(tmem_lane_addr(tm, TM_DW3 + c), r);
-            if (t < NOUT)
-                for (int k = 0; k < 16; ++k) atomicAdd(&grad[P_W3 + t * NH + c + k], r[k]);
+        tmem_ld16(tmem_lane_addr(tm, TM_DW1), r);
+        if (t < NH) {
+            for (int k = 0; k < NIN - 1; ++k) atomicAdd(&grad[P_W1 + t * NIN + k], r[k]);
+            atomicAdd(&grad[P_B1 + t], r[NIN - 1]);
         }
-        tmem_ld16(tmem_lane_addr(tm, TM_DW1), r);  // dW1[t][0..15]
-        for (int k = 0; k < 16; ++k) atomicAdd(&grad[P_W1 + t * NIN + k], r[k]);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < NH + NH + NOUT; i += T) {
-        const int dst = i < NH ? P_B1 + i : i < 2 * NH ? P_B2 + (i - NH) : P_B3 + (i - 2 * NH);
-        atomicAdd(&grad[dst], s_db[i]);
+        tmem_ld16(tmem_lane_addr(tm, TM_DW5), r);  // row j: dW5[o][j]; row NH: db5[o]
+        if (t < NH)
+            for (int o = 0; o < NOUT; ++o) atomicAdd(&grad[P_W5 + o * NH + t], r[o]);
+        else if (t == NH)
+            for (int o = 0; o < NOUT; ++o) atomicAdd(&grad[P_B5 + o], r[o]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
@@ -278,7 +334,7 @@ __global__ void __launch_bounds__(T) k_mlp_train(const uint8_t *img, const float
 
 }  // namespace
 
-int train_blocks() { return sm_count() * 2; }
+int train_blocks() { return sm_count(); }  // one CTA per SM: all of its TMEM and most of its shared memory
 
 cudaError_t pack_image(const float *params, uint8_t *img, cudaStream_t s) {
     k_pack_image<<<(N_PARAMS + 255) / 256, 256, 0, s>>>(params, img);
@@ -288,8 +344,14 @@ cudaError_t pack_image(const float *params, uint8_t *img, cudaStream_t s) {
 cudaError_t forward(const uint8_t *img, const float *X, uint64_t n, float *Y, uint32_t *err, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     const uint64_t tiles = (n + T - 1) / T;
-    const unsigned blocks = (unsigned)std::min<uint64_t>(tiles, (uint64_t)sm_count() * 8);
-    k_mlp_forward<<<blocks, T, 0, s>>>(img, X, n, Y, err);
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, FW_BYTES);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const unsigned blocks = (unsigned)std::min<uint64_t>(tiles, (uint64_t)sm_count() * 4);
+    k_mlp_forward<<<blocks, T, FW_BYTES, s>>>(img, X, n, Y, err);
     return cudaGetLastError();
 }
 

@@ -9,7 +9,7 @@
 namespace sv {
 namespace mlp {
 
-constexpr int TMEM_COLS_INFER = 32;
+constexpr int TMEM_COLS_INFER = 64;  // one NH-wide fp32 accumulator
 constexpr long long MMA_WAIT_CYCLES = 2000000000ll;  // about one second
 
 // Shared per-CTA state.  `abort` is only written between two barriers, so
@@ -82,51 +82,53 @@ __device__ __forceinline__ void ctl_finish(Ctl &c, uint32_t cols, uint32_t *err,
     if (threadIdx.x < 32) tc::tmem_dealloc(c.tmem, cols);
 }
 
-// One 128-row tile through the network: thread t's input row x, output y.
-// a0 [128 x NIN] and a1 [128 x NH] are operand buffers (1 KB aligned), img
-// the packed weight image in shared memory.  Returns this thread's status:
+// One 128-row tile through the network: thread t's input row x, outputs
+// y[0 .. nout).  a0 [128 x NIN] and a1 [128 x NH] are operand buffers
+// (16-byte aligned), img the packed weight image (forward part) in shared
+// memory.  Each hidden layer's accumulator is read from TMEM 16 columns at a
+// time, given its bias and SiLU, and written as the next layer's bf16
+// operand; the last one feeds the fp32 head.  Returns this thread's status:
 // false when a wait gave up (y is then meaningless).
 __device__ __forceinline__ bool infer_tile(Ctl &c, Phase &ph, const uint8_t *img, uint8_t *a0, uint8_t *a1,
-                                           const float x[tc::NIN], float y[tc::NOUT]) {
+                                           const float x[tc::NIN], float *y, int nout = tc::NOUT) {
     using namespace tc;
     const int t = threadIdx.x;
     const uint32_t tm = c.tmem;
     store_row8(a0, t, 0, NIN, x);
     store_row8(a0, t, 8, NIN, x + 8);
-    if (!issue(c, ph, [&] { mma_bf16(tm, smem_u32(a0), smem_u32(img + IMG_W1), NIN, NH, false); })) {
+    const float *bh = reinterpret_cast<const float *>(img + IMG_BH);
+    const float *w5 = reinterpret_cast<const float *>(img + IMG_W5);
+    const float *b5 = reinterpret_cast<const float *>(img + IMG_B5);
+    for (int o = 0; o < nout; ++o) y[o] = b5[o];
+    if (!issue(c, ph, [&] { mma_bf16(tm, smem_u32(a0), smem_u32(img + IMG_W1), NIN, NH, false); })) return false;
+#pragma unroll 1
+    for (int layer = 1; layer <= N_HIDDEN; ++layer) {
+        const float *b = bh + (layer - 1) * NH;
 #pragma unroll
-        for (int k = 0; k < NOUT; ++k) y[k] = 0.f;
-        return false;
+        for (int q = 0; q < NH / 16; ++q) {
+            float h[16];
+            tmem_ld16(tmem_lane_addr(tm, 16 * q), h);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float z = h[j] + b[16 * q + j];
+                h[j] = z * sigmoid_f(z);
+            }
+            if (layer < N_HIDDEN) {
+                store_row8(a1, t, 16 * q, NH, h);
+                store_row8(a1, t, 16 * q + 8, NH, h + 8);
+            } else {
+                for (int o = 0; o < nout; ++o) {
+                    float acc = y[o];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) acc = fmaf(w5[o * NH + 16 * q + j], h[j], acc);
+                    y[o] = acc;
+                }
+            }
+        }
+        if (layer < N_HIDDEN &&
+            !issue(c, ph, [&] { mma_bf16(tm, smem_u32(a1), smem_u32(img + img_weight(layer + 1)), NH, NH, false); }))
+            return false;
     }
-    float h[NH];
-    tmem_ld16(tmem_lane_addr(tm, 0), h);
-    tmem_ld16(tmem_lane_addr(tm, 16), h + 16);
-    const float *b1 = reinterpret_cast<const float *>(img + IMG_B1);
-#pragma unroll
-    for (int j = 0; j < NH; ++j) h[j] = fmaxf(h[j] + b1[j], 0.f);
-#pragma unroll
-    for (int k = 0; k < NH / 8; ++k) store_row8(a1, t, 8 * k, NH, h + 8 * k);
-    if (!issue(c, ph, [&] { mma_bf16(tm, smem_u32(a1), smem_u32(img + IMG_W2), NH, NH, false); })) {
-#pragma unroll
-        for (int k = 0; k < NOUT; ++k) y[k] = 0.f;
-        return false;
-    }
-    tmem_ld16(tmem_lane_addr(tm, 0), h);
-    tmem_ld16(tmem_lane_addr(tm, 16), h + 16);
-    const float *b2 = reinterpret_cast<const float *>(img + IMG_B2);
-#pragma unroll
-    for (int j = 0; j < NH; ++j) h[j] = fmaxf(h[j] + b2[j], 0.f);
-#pragma unroll
-    for (int k = 0; k < NH / 8; ++k) store_row8(a1, t, 8 * k, NH, h + 8 * k);
-    if (!issue(c, ph, [&] { mma_bf16(tm, smem_u32(a1), smem_u32(img + IMG_W3), NH, NOUT, false); })) {
-#pragma unroll
-        for (int k = 0; k < NOUT; ++k) y[k] = 0.f;
-        return false;
-    }
-    tmem_ld16(tmem_lane_addr(tm, 0), y);
-    const float *b3 = reinterpret_cast<const float *>(img + IMG_B3);
-#pragma unroll
-    for (int k = 0; k < NOUT; ++k) y[k] += b3[k];
     tc::fence_before();
     return ph.ok;
 }

@@ -27,6 +27,7 @@
 //             the 27-block neighbourhood of every particle block.
 // Particles that drift out of their segment's tile take a global-memory path;
 // a particle that leaves the claimed blocks makes the host redo the binning.
+#include <cstddef>
 #include <cstdio>
 
 #include <type_traits>
@@ -780,14 +781,21 @@ __device__ __forceinline__ void gather_global(const StepArgs &A, const int base[
             }
 }
 
-// Shared state of the learned closure (network image, feature hull, TMEM and
-// MMA-completion control); its two operand buffers overlay the records.
+// Shared state of the learned closure (feature hull, TMEM and MMA-completion
+// control).  The network image (its forward part) sits in dynamic shared
+// memory; the two operand buffers overlay the records, their metadata and
+// global bases, which are free between the previous chunk's replay and this
+// chunk's record writes.
 struct SharedLearned {
-    __align__(16) uint8_t img[tc::IMG_BYTES];
     closure::Hull hull;
     mlp::Ctl ctl;
 };
-static_assert(sizeof(Rec) * PT >= tc::NIN * PT * 2 + tc::NH * PT * 2, "closure operands overlay the records");
+constexpr int LEARNED_SMEM_BYTES = tc::IMG_FWD_BYTES;
+static_assert(offsetof(Shared, meta) == offsetof(Shared, rec) + sizeof(Rec) * PT &&
+                  offsetof(Shared, gbase) == offsetof(Shared, meta) + sizeof(float2) * PT &&
+                  sizeof(Rec) * PT + (sizeof(float2) + sizeof(int4)) * PT >= (tc::NIN + tc::NH) * PT * 2 &&
+                  offsetof(Shared, rec) % 16 == 0,
+              "closure operands overlay the records");
 
 // End of a self-latching pass (one call per CTA, by all its threads): the
 // last CTA to finish latches the stop bits for the kernels that follow and
@@ -815,14 +823,15 @@ __device__ __forceinline__ void cta_done(const StepArgs &A, uint32_t stop_at_sta
 
 // Five CTAs per SM (at most 102 registers): measured faster than the
 // unconstrained 150-register build despite a few spilled values.  The
-// learned-closure variant holds the network image as well: four CTAs.
+// learned-closure variant holds the network image as well: three CTAs; the
+// frame-input variant four.
 // FIN: a frame input is loaded -- interpolated gravity and goals, Collide
 // (collide.rs:21-206) before the scatter, collider bits and their variants.
 #ifndef SV_PARTICLE_CTAS_PER_SM
 #define SV_PARTICLE_CTAS_PER_SM 5
 #endif
 template <bool CELL, int MODE, bool FIN = false>
-__global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : SV_PARTICLE_CTAS_PER_SM)
+__global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 : SV_PARTICLE_CTAS_PER_SM)
     k_particles(StepArgs A) {
     constexpr bool LEARNED = MODE == MODE_G2P2G_LEARNED;
     // what the pass does: gather from the grid, advance the particles (and
@@ -849,11 +858,12 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
     if (threadIdx.x == 0) sh.raised = 0;
     mlp::Phase ph;
     uint32_t n_learned = 0, n_closure_fb = 0;
+    extern __shared__ __align__(128) uint8_t learned_img[];
     if constexpr (LEARNED) {
-        for (int t = threadIdx.x * 16; t < tc::IMG_BYTES; t += PT * 16)
-            *reinterpret_cast<uint4 *>(shl.img + t) = *reinterpret_cast<const uint4 *>(A.closure_img + t);
-        for (int t = threadIdx.x; t < 2 * tc::NIN; t += PT)
-            (&shl.hull.lo[0])[t] = (&A.closure_hull->lo[0])[t];
+        for (int t = threadIdx.x * 16; t < LEARNED_SMEM_BYTES; t += PT * 16)
+            *reinterpret_cast<uint4 *>(learned_img + t) = *reinterpret_cast<const uint4 *>(A.closure_img + t);
+        for (int t = threadIdx.x; t < (int)(sizeof(closure::Hull) / 4); t += PT)
+            reinterpret_cast<float *>(&shl.hull)[t] = reinterpret_cast<const float *>(A.closure_hull)[t];
         mlp::ctl_init(shl.ctl, mlp::TMEM_COLS_INFER);
     }
     const uint32_t nseg = A.counters[C_NSEG];
@@ -1014,22 +1024,25 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
             // ---- learned closure (snow, sand): closed-form principal
             // stretches, then one network pass for the whole chunk on the
             // tensor cores (all threads take part)
-            bool learned = false;
+            int l_class = closure::L_PLAIN;  // after the network: L_PLAIN, L_ELASTIC or L_NET
             float l_sig[3], l_V[9], l_y[tc::NOUT];
             if constexpr (LEARNED) {
                 float x[tc::NIN];
-                bool want = false;
                 if (work) {
                     const Material &lm = A.mats[packed >> MATERIAL_SHIFT];
-                    if (closure::applies(lm.kind)) want = closure::learned_features(lm, F, shl.hull, l_sig, l_V, x);
+                    if (closure::applies(lm.kind)) l_class = closure::learned_features(lm, F, shl.hull, l_sig, l_V, x);
                 }
+                const bool want = l_class == closure::L_NET;
                 if (!want)
 #pragma unroll
                     for (int k = 0; k < tc::NIN; ++k) x[k] = 0.f;
-                if (__syncthreads_or(want) && !shl.ctl.abort) {
-                    uint8_t *a0 = reinterpret_cast<uint8_t *>(sh.rec);
-                    const bool ok = mlp::infer_tile(shl.ctl, ph, shl.img, a0, a0 + tc::NIN * PT * 2, x, l_y);
-                    learned = want && ok;
+                if (__syncthreads_or(want)) {
+                    bool ok = false;
+                    if (!shl.ctl.abort) {
+                        uint8_t *a0 = reinterpret_cast<uint8_t *>(sh.rec);
+                        ok = mlp::infer_tile(shl.ctl, ph, learned_img, a0, a0 + tc::NIN * PT * 2, x, l_y);
+                    }
+                    if (want && !ok) l_class = closure::L_PLAIN;
                 }
             }
             if (work && (G2P || SCATTER)) {
@@ -1042,10 +1055,11 @@ __global__ void __launch_bounds__(PT, (MODE == MODE_G2P2G_LEARNED || FIN) ? 4 : 
                 m3f tau_l{};  // learned path: Kirchhoff stress P F^T
                 bool use_l = false;
                 if constexpr (LEARNED) {
-                    if (learned) {
+                    if (l_class != closure::L_PLAIN) {
                         m3f Fn;
                         float e_l, jp_l, J_l;
-                        if (closure::learned_apply(mat, F, l_sig, l_V, l_y, plastic_j, Fn, tau_l, e_l, jp_l, J_l)) {
+                        if (closure::learned_apply(mat, F, l_sig, l_V, l_class == closure::L_NET ? l_y : nullptr, shl.hull,
+                                                   plastic_j, Fn, tau_l, e_l, jp_l, J_l)) {
                             use_l = true;
                             F = Fn;
                             plastic_j = jp_l;
@@ -1646,6 +1660,17 @@ template <int MODE> void launch_particles(sv_handle *h, const StepArgs &A, unsig
             else k_particles<false, MODE, true><<<blocks, PT, 0, h->stream>>>(A);
             return;
         }
+    }
+    if constexpr (MODE == MODE_G2P2G_LEARNED) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(k_particles<true, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, LEARNED_SMEM_BYTES);
+            cudaFuncSetAttribute(k_particles<false, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, LEARNED_SMEM_BYTES);
+            attr = true;
+        }
+        if (h->layout.position_form) k_particles<true, MODE><<<blocks, PT, LEARNED_SMEM_BYTES, h->stream>>>(A);
+        else k_particles<false, MODE><<<blocks, PT, LEARNED_SMEM_BYTES, h->stream>>>(A);
+        return;
     }
     if (h->layout.position_form) k_particles<true, MODE><<<blocks, PT, 0, h->stream>>>(A);
     else k_particles<false, MODE><<<blocks, PT, 0, h->stream>>>(A);

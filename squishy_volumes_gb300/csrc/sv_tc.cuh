@@ -18,15 +18,25 @@ namespace sv {
 namespace tc {
 
 // ------------------------------------------------------------------ MLP shape
-// x (NIN) -> relu(W1 x + b1) (NH) -> relu(W2 h + b2) (NH) -> W3 h + b3 (NOUT)
+// x (NIN, input NIN-1 reserved and zero) -> four hidden layers of width NH,
+// h = silu(W h_prev + b) on the tensor cores (bf16 operands, fp32
+// accumulation) -> an fp32 head y = W5 h4 + b5 (NOUT outputs, the first
+// N_USED_OUT used) on the CUDA cores, reading the last hidden layer in fp32.
 constexpr int NIN = 16;   // padded input width (one K = 16 MMA step)
-constexpr int NH = 32;    // hidden width
-constexpr int NOUT = 16;  // padded output width (M = 128 needs N % 16 == 0)
+constexpr int NH = 64;    // hidden width
+constexpr int N_HIDDEN = 4;
+constexpr int NOUT = 8;   // head outputs
 constexpr int N_USED_OUT = 6;
-constexpr int N_PARAMS = NH * NIN + NH + NH * NH + NH + NOUT * NH + NOUT;  // fp32 master parameters
-// parameter offsets in the fp32 master vector
-constexpr int P_W1 = 0, P_B1 = P_W1 + NH * NIN, P_W2 = P_B1 + NH, P_B2 = P_W2 + NH * NH, P_W3 = P_B2 + NH,
-              P_B3 = P_W3 + NOUT * NH;
+// fp32 master parameters: W1 [NH x NIN], b1, then W2..W4 [NH x NH] with
+// their biases, then W5 [NOUT x NH], b5 (row-major, out x in)
+constexpr int P_W1 = 0, P_B1 = P_W1 + NH * NIN;
+constexpr int P_W2 = P_B1 + NH, P_B2 = P_W2 + NH * NH;
+constexpr int P_W3 = P_B2 + NH, P_B3 = P_W3 + NH * NH;
+constexpr int P_W4 = P_B3 + NH, P_B4 = P_W4 + NH * NH;
+constexpr int P_W5 = P_B4 + NH, P_B5 = P_W5 + NOUT * NH;
+constexpr int N_PARAMS = P_B5 + NOUT;
+__host__ __device__ constexpr int p_weight(int layer) { return layer == 1 ? P_W1 : layer == 2 ? P_W2 : layer == 3 ? P_W3 : P_W4; }
+__host__ __device__ constexpr int p_bias(int layer) { return layer == 1 ? P_B1 : layer == 2 ? P_B2 : layer == 3 ? P_B3 : P_B4; }
 
 // Byte offset of element (r, k) of an R x K bf16 matrix in the canonical
 // K-major layout without swizzle: 8-row x 16-byte core matrices, the core
@@ -36,22 +46,32 @@ __host__ __device__ constexpr int kmaj(int r, int k, int K) {
     return (r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
 }
 
-// Packed bf16 weight image (copied verbatim into shared memory):
-//   W1 [NH x NIN], W2 [NH x NH], W3 [NOUT x NH] as B operands of the forward
-//   pass (N = output units, K = input units), W2^T [NH x NH] and W3^T
-//   [NH x NOUT] as B operands of the backward pass, then b1, b2, b3 in fp32.
+// Packed weight image (copied verbatim into shared memory).  The forward
+// part first (all an inference pass reads): W1 [NH x NIN] and W2..W4
+// [NH x NH] as bf16 B operands (N = output units, K = input units), the
+// hidden biases b1..b4 in fp32, the head W5 [NOUT x NH] and b5 in fp32.
+// Then, for the backward pass, W2^T..W4^T [NH x NH] as bf16 B operands of the
+// input-gradient products (N = input units, K = output units).
 constexpr int IMG_W1 = 0;
 constexpr int IMG_W2 = IMG_W1 + NH * NIN * 2;
 constexpr int IMG_W3 = IMG_W2 + NH * NH * 2;
-constexpr int IMG_W2T = IMG_W3 + NOUT * NH * 2;
+constexpr int IMG_W4 = IMG_W3 + NH * NH * 2;
+constexpr int IMG_BH = IMG_W4 + NH * NH * 2;        // b1..b4, fp32 [4][NH]
+constexpr int IMG_W5 = IMG_BH + N_HIDDEN * NH * 4;  // fp32 [NOUT][NH]
+constexpr int IMG_B5 = IMG_W5 + NOUT * NH * 4;      // fp32 [NOUT]
+constexpr int IMG_FWD_BYTES = (IMG_B5 + NOUT * 4 + 127) / 128 * 128;
+constexpr int IMG_W2T = IMG_FWD_BYTES;
 constexpr int IMG_W3T = IMG_W2T + NH * NH * 2;
-constexpr int IMG_B1 = IMG_W3T + NH * NOUT * 2;
-constexpr int IMG_B2 = IMG_B1 + NH * 4;
-constexpr int IMG_B3 = IMG_B2 + NH * 4;
-constexpr int IMG_BYTES = IMG_B3 + NOUT * 4;
-constexpr int IMG_FWD_BYTES = IMG_W2T;  // forward weights only (inference)
-static_assert(IMG_W2 % 128 == 0 && IMG_W3 % 128 == 0 && IMG_W2T % 128 == 0 && IMG_W3T % 128 == 0 && IMG_B1 % 16 == 0,
+constexpr int IMG_W4T = IMG_W3T + NH * NH * 2;
+constexpr int IMG_BYTES = IMG_W4T + NH * NH * 2;
+__host__ __device__ constexpr int img_weight(int layer) { return layer == 1 ? IMG_W1 : layer == 2 ? IMG_W2 : layer == 3 ? IMG_W3 : IMG_W4; }
+__host__ __device__ constexpr int img_weight_t(int layer) { return layer == 2 ? IMG_W2T : layer == 3 ? IMG_W3T : IMG_W4T; }
+static_assert(IMG_W2 % 128 == 0 && IMG_W3 % 128 == 0 && IMG_W4 % 128 == 0 && IMG_W2T % 128 == 0 &&
+                  IMG_W3T % 128 == 0 && IMG_W4T % 128 == 0 && IMG_BH % 16 == 0 && IMG_W5 % 16 == 0,
               "operand images must stay 128-byte aligned");
+
+// silu(z) = z sigmoid(z) and its derivative sigmoid(z) (1 + z (1 - sigmoid(z)))
+__device__ __forceinline__ float sigmoid_f(float z) { return __frcp_rn(1.f + __expf(-z)); }
 
 // Instruction descriptor of tcgen05.mma kind::f16: D fp32 (bits 4-5 = 1),
 // A and B bf16 (bits 7-9 and 10-12 = 1), both K-major (bits 15, 16 = 0),

@@ -568,7 +568,7 @@ class CudaState:
                                            ct.byref(total)))
         return int(total.value)
 
-    def closure_train(self, iterations: int, batch: int = 8192, lr: float = 3e-3, seed: int = 0) -> float:
+    def closure_train(self, iterations: int, batch: int = 65536, lr: float = 3e-3, seed: int = 0) -> float:
         loss = ct.c_float(0.0)
         check(self._lib.sv_closure_train(self._h, int(iterations), int(batch), float(lr), int(seed), ct.byref(loss)))
         return float(loss.value)
@@ -576,11 +576,47 @@ class CudaState:
     def closure_set_mode(self, mode: int):
         check(self._lib.sv_closure_set_mode(self._h, int(mode)))
 
+    def closure_pool(self) -> dict:
+        """Harvested pairs, and the yielding ones of the last training."""
+        a, b = ct.c_uint64(0), ct.c_uint64(0)
+        check(self._lib.sv_closure_pool(self._h, ct.byref(a), ct.byref(b)))
+        return {"pairs": int(a.value), "yielding_pairs": int(b.value)}
+
+    def closure_training_pool(self, first: int = 0, count: int = 0):
+        """(X [count, 16], Y [count, 8], hull dict) of the normalised pool of
+        the last training (count 0: all of it)."""
+        from .closure import NIN, NOUT
+
+        if count == 0:
+            count = self.closure_pool()["yielding_pairs"] - first
+        X = np.zeros((count, NIN), np.float32)
+        Y = np.zeros((count, NOUT), np.float32)
+        hull = np.zeros(80, np.float32)
+        check(self._lib.sv_closure_get_pool(self._h, int(first), int(count), ptr(X, f32p), ptr(Y, f32p),
+                                            ptr(hull, f32p)))
+        keys = (("lo", 16), ("hi", 16), ("xm", 16), ("xs", 16), ("ym", 8), ("ys", 8))
+        out, o = {}, 0
+        for k, n in keys:
+            out[k] = hull[o:o + n].copy()
+            o += n
+        return X, Y, out
+
+    def closure_copy_from(self, other):
+        """Take over the trained network, hull and normalisation of another state."""
+        check(self._lib.sv_closure_copy(self._h, other._h))
+
+    def closure_phase_times(self, dt: float) -> dict:
+        out = (ct.c_double * 6)()
+        check(self._lib.sv_closure_phase_times(self._h, float(dt), out))
+        keys = ("plain_ms", "closed_form_ms", "network_all_ms", "particles", "yielding", "network_yielding_ms")
+        return {k: float(v) for k, v in zip(keys, out)}
+
     def closure_evaluate(self, dt: float) -> dict:
-        out = (ct.c_double * 8)()
+        out = (ct.c_double * 12)()
         check(self._lib.sv_closure_evaluate(self._h, float(dt), out))
         keys = ("stress_err_learned", "stress_err_plain32", "f_err_learned", "f_err_plain32", "particles",
-                "fallbacks", "stress_norm", "f_norm")
+                "fallbacks", "stress_norm", "f_norm", "network", "residual_rejects", "stress_err_network_part",
+                "stress_err_elastic_part")
         return {k: float(v) for k, v in zip(keys, out)}
 
     def closure_params(self) -> np.ndarray:

