@@ -62,10 +62,13 @@ def parse():
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel directly (no CUDA graphs)")
     ap.add_argument("--closure", default="plain", choices=["plain", "learned"],
                     help="snow/sand constitutive update: SVD + return map, or the learned closure (trained first)")
-    ap.add_argument("--closure-source", default="batched_64",
-                    help="workload whose plain runs give the closure's training pairs (its snow and sand scenes)")
+    ap.add_argument("--closure-source", default="batched_64,self",
+                    help="comma-separated workloads whose plain runs give the closure's training pairs (their snow "
+                         "and sand particles); 'self' is the measured scene's own first substeps")
     ap.add_argument("--closure-pairs", type=int, default=50_000_000, help="training pairs to harvest")
     ap.add_argument("--closure-iters", type=int, default=20000, help="Adam steps of 65536 pairs")
+    ap.add_argument("--closure-augment", type=float, default=0.1,
+                    help="half of the harvested pairs are widened by F (I + a R), R symmetric with entries in [-1, 1)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="bound on the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -538,41 +541,63 @@ def measure_scene(args, name, rank, world, local, dev, primary):
 
 
 def train_closure(gpu, scene, args):
-    """Training pairs harvested from plain runs of another workload (by
-    default the 64-scene batched one: its snow and sand scenes), fp64
-    labels, then the GPU training loop on that handle; the trained network
-    is handed to the measured scene's handle.  None of this is inside the
-    timed region."""
+    """Training pairs harvested from plain runs of the --closure-source
+    workloads (by default the 64-scene batched one -- its snow and sand
+    scenes -- and the measured scene's own first 200 substeps) into the
+    measured handle's pool, fp64 labels over the batched workload's material
+    ranges, then the GPU training loop.  None of this is inside the timed
+    region."""
     import torch
 
     from squishy_volumes_gb300 import CudaState, scenes
     from squishy_volumes_gb300.state import BatchedCudaState
 
     t0 = time.perf_counter()
-    made = scenes.SCENES[args.closure_source]()
-    if isinstance(made, list):
-        src = BatchedCudaState.from_scenes([s.io_state for s in made], [s.consts for s in made], made[0].extras)
-        ref = made[0]
-    else:
-        src = CudaState.from_io_state(made.io_state, made.consts, made.extras)
-        ref = made
-    rounds, per_round = 10, max(1, ref.substeps // 10)
-    pool = 0
-    for k in range(rounds):
-        status, _ = src.step(per_round, ref.dt, ref.gravity)
-        if status:
-            raise RuntimeError(f"closure harvest run status {status:#x}")
-        pool = src.closure_harvest(ref.dt, int(math.ceil(args.closure_pairs / rounds)), 0.0, seed=k)
+    sources = [x for x in args.closure_source.split(",") if x]
+    per_source = int(math.ceil(args.closure_pairs / max(1, len(sources))))
+    pool, harvested = 0, {}
+    for si, name in enumerate(sources):
+        if name == "self":
+            made, run = scene, gpu
+        else:
+            made = scenes.SCENES[name]()
+            if isinstance(made, list):
+                run = BatchedCudaState.from_scenes([s.io_state for s in made], [s.consts for s in made],
+                                                   made[0].extras)
+            else:
+                run = CudaState.from_io_state(made.io_state, made.consts, made.extras)
+        ref = made[0] if isinstance(made, list) else made
+        rounds = 10
+        # the batched scenes over their stated run; the measured scene over
+        # its first 200 substeps (the timed region comes after them)
+        per_round = max(1, (200 if name == "self" else ref.substeps) // rounds)
+        before = pool
+        for k in range(rounds):
+            status, _ = run.step(per_round, ref.dt, ref.gravity)
+            if status:
+                raise RuntimeError(f"closure harvest run status {status:#x}")
+            # half of the pairs widened by F (I + a R), R symmetric in
+            # [-1, 1)^6: the batched scenes fall gently and barely yield, so
+            # their own strains do not reach a collision's
+            pool = gpu.closure_harvest_from(run, ref.dt, int(math.ceil(per_source / rounds)), args.closure_augment,
+                                            seed=k + 100 * si)
+        harvested[name] = pool - before
+        if run is not gpu:
+            run.close()
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    loss = src.closure_train(args.closure_iters, 65536, 3e-3, seed=1)
+    # the batched workload's material ranges (nu in [0.2, 0.4], friction
+    # angle in [25, 40] deg), a little wider so that their ends lie inside
+    # the hull: the labels draw from them
+    gpu.closure_set_material_ranges((0.18, 0.42), (23.0, 42.0))
+    loss = gpu.closure_train(args.closure_iters, 65536, 3e-3, seed=1)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    yielding = src.closure_pool()["yielding_pairs"]
-    gpu.closure_copy_from(src)
-    src.close()
+    yielding = gpu.closure_pool()["yielding_pairs"]
     gpu.closure_set_mode(1)
-    return {"mode": "learned", "source": args.closure_source, "pairs": pool, "yielding_pairs": yielding,
+    return {"mode": "learned", "sources": harvested, "augment": args.closure_augment,
+            "material_ranges": {"nu": [0.18, 0.42], "friction_deg": [23.0, 42.0]},
+            "pairs": pool, "yielding_pairs": yielding,
             "harvest_s": round(t1 - t0, 3), "train_s": round(t2 - t1, 3), "train_iterations": args.closure_iters,
             "batch": 65536, "loss_normalised": loss}
 

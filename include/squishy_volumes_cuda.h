@@ -266,7 +266,10 @@ typedef struct sv_stats {
      * momentum -> velocity (collider variants included): the total mass and
      * momentum that the P2G scattered.  Equal to the particles' sum of m and
      * m v + (the APIC term, which sums to zero) up to fp32 rounding of the
-     * node values. */
+     * node values.  sv_step takes them on the last substep of each call
+     * only (on every substep they would cost about 7 % of the substep's
+     * time); a call that stops early leaves them 0.  The other stepping
+     * calls take them on every substep. */
     double grid_mass;
     double grid_momentum[3];
 } sv_stats;
@@ -410,6 +413,9 @@ int sv_mlp_grad(const float *params, const float *x, const float *t, const float
  *   the plain solver produced) to the handle's training pool (at most 2^26);
  *   with augment > 0 half of them are multiplied by I + augment R, R
  *   symmetric with entries in [-1, 1).  *total_out = pool size.
+ * sv_closure_harvest_from: the same from the current state of another
+ *   handle `src` into h's pool (the samples carry their material
+ *   parameters), so that one pool gathers several workloads' states.
  * sv_closure_train: labels the pool with the fp64 SVD + return map, keeps
  *   the yielding samples, records the range of their features (the hull)
  *   and the normalisation of inputs and outputs, and runs `iterations` Adam
@@ -417,6 +423,12 @@ int sv_mlp_grad(const float *params, const float *x, const float *t, const float
  *   decay to 1 %) on the GPU from the current weights (He-initialised from
  *   `seed` on the first call).  *loss_out = mean squared error (normalised
  *   units) over the yielding samples afterwards.
+ * sv_closure_set_material_ranges: from the next sv_closure_train on, each
+ *   sample keeps its harvested deformation and shear modulus but is labelled
+ *   with a Poisson's ratio drawn uniformly from [nu_lo, nu_hi] and, for
+ *   sand, a friction angle from [phi_lo_deg, phi_hi_deg] (degrees), so that
+ *   the pool covers those material ranges evenly whichever scenes the
+ *   samples came from.  All four 0: the harvested materials (default).
  * sv_closure_copy: gives dst the trained network, hull and normalisation of
  *   src (e.g. trained on a batched handle, used on another).
  * sv_closure_set_mode: 0 = return maps (default), 1 = learned closure in
@@ -446,9 +458,12 @@ int sv_mlp_grad(const float *params, const float *x, const float *t, const float
  * sv_closure_get_params: the fp32 master weights (sv_mlp_param_count()). */
 int sv_closure_harvest(sv_handle *h, float dt, uint32_t max_samples, float augment, uint32_t seed,
                        uint64_t *total_out);
+int sv_closure_harvest_from(sv_handle *h, sv_handle *src, float dt, uint32_t max_samples, float augment,
+                            uint32_t seed, uint64_t *total_out);
 int sv_closure_train(sv_handle *h, uint32_t iterations, uint32_t batch, float lr, uint32_t seed, float *loss_out);
 int sv_closure_set_mode(sv_handle *h, int mode);
 int sv_closure_copy(sv_handle *dst, sv_handle *src);
+int sv_closure_set_material_ranges(sv_handle *h, float nu_lo, float nu_hi, float phi_lo_deg, float phi_hi_deg);
 int sv_closure_phase_times(sv_handle *h, float dt, double out[6]);
 int sv_closure_pool(sv_handle *h, uint64_t *pairs, uint64_t *yielding);
 int sv_closure_get_pool(sv_handle *h, uint64_t first, uint64_t count, float *X, float *Y, float *hull);

@@ -211,6 +211,9 @@ _SIGNATURES = {
     "sv_closure_train": (ct.c_int, [ct.c_void_p, ct.c_uint32, ct.c_uint32, ct.c_float, ct.c_uint32, f32p]),
     "sv_closure_set_mode": (ct.c_int, [ct.c_void_p, ct.c_int]),
     "sv_closure_copy": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "sv_closure_harvest_from": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_float, ct.c_uint32, ct.c_float, ct.c_uint32,
+                                           ct.POINTER(ct.c_uint64)]),
+    "sv_closure_set_material_ranges": (ct.c_int, [ct.c_void_p, ct.c_float, ct.c_float, ct.c_float, ct.c_float]),
     "sv_closure_get_pool": (ct.c_int, [ct.c_void_p, ct.c_uint64, ct.c_uint64, f32p, f32p, f32p]),
     "sv_closure_pool": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_uint64), ct.POINTER(ct.c_uint64)]),
     "sv_closure_phase_times": (ct.c_int, [ct.c_void_p, ct.c_float, ct.POINTER(ct.c_double)]),

@@ -958,6 +958,14 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
                              (h->fin_active || (h->pending_g[0] == g.x && h->pending_g[1] == g.y && h->pending_g[2] == g.z));
     if (!same_inputs) h->pending_valid = false;
     const uint32_t base = h->host_counters[C_SUBSTEPS];
+    // the fp64 conservation sums of sv_get_stats: only the call's last
+    // substep takes them (reset to every substep when the call returns)
+    struct SumsAt {
+        sv_handle *h;
+        ~SumsAt() { cudaMemsetAsync(h->counters + C_SUMS_AT, 0, 4, h->stream); }
+    } sums_at{h};
+    h->host_counters[C_SUMS_AT] = n_substeps ? base + n_substeps - 1 : 0;
+    SV_CUDA(cudaMemcpyAsync(h->counters + C_SUMS_AT, h->host_counters + C_SUMS_AT, 4, cudaMemcpyHostToDevice, h->stream));
     const uint32_t fp64_before = h->host_counters[C_FP64];
     uint32_t fallback_before = h->host_counters[C_FALLBACK];
     uint32_t status = 0;

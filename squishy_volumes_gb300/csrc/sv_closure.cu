@@ -33,7 +33,10 @@ namespace sv {
 
 namespace {
 
-constexpr int CL_SAMPLE = 12;  // trial F (9), plastic J, material index bits, spare
+// A pool sample carries its material's parameters, so that a pool may
+// gather samples from several handles: trial F (9), plastic J, kind bits,
+// mu, lambda, alpha, theta_c, theta_s, xi.
+constexpr int CL_SAMPLE = 16;
 constexpr uint64_t CL_MAX_SAMPLES = 1ull << 26;
 constexpr int EVAL_SUMS = 12;
 
@@ -87,18 +90,42 @@ __global__ void k_harvest(ParticleArrays s, const Material *mats, uint64_t n, fl
         float *o = out + slot * CL_SAMPLE;
         for (int k = 0; k < 9; ++k) o[k] = F.a[k];
         o[9] = m.kind == KIND_SNOW ? s.vel[i].w : 1.f;
-        o[10] = __uint_as_float(mi);
-        o[11] = 0.f;
+        o[10] = __uint_as_float(m.kind);
+        o[11] = m.mu, o[12] = m.lambda, o[13] = m.alpha, o[14] = m.theta_c, o[15] = m.theta_s;
     }
 }
 
+// Material ranges the labels draw from (sv_closure_set_material_ranges);
+// on = 0: every sample keeps the material it was harvested with.
+struct MatRanges {
+    int on;
+    float nu_lo, nu_hi, phi_lo, phi_hi;  // Poisson's ratio, friction angle (radians)
+};
+
 // Raw features and targets of each sample, written at position perm[i];
 // weight 1 for the samples that yield (the only ones the network sees).
-__global__ void k_label(const float *samples, uint64_t n, const Material *mats, const uint32_t *perm, float *X,
-                        float *Y, float *W) {
+// With material ranges, a sample keeps its harvested deformation and shear
+// modulus but takes a Poisson's ratio (lambda = 2 mu nu / (1 - 2 nu)) and,
+// for sand, a friction angle (alpha = sqrt(2/3) 2 sin phi / (3 - sin phi))
+// drawn uniformly from the ranges by a hash of its index.
+__global__ void k_label(const float *samples, uint64_t n, const uint32_t *perm, float *X,
+                        float *Y, float *W, MatRanges mr, uint32_t seed) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const float *smp = samples + i * CL_SAMPLE;
-        const Material m = mats[__float_as_uint(smp[10])];
+        Material m{};
+        m.kind = __float_as_uint(smp[10]);
+        m.mu = smp[11], m.lambda = smp[12], m.alpha = smp[13], m.theta_c = smp[14], m.theta_s = smp[15];
+        m.xi = 0.f;  // the targets do not depend on the hardening
+        if (mr.on) {
+            const uint32_t h1 = hash32((uint32_t)i ^ hash32(seed ^ 0x51ed270bu)), h2 = hash32(h1 ^ 0x2545f491u);
+            const double u1 = (double)(h1 >> 8) / 16777216.0, u2 = (double)(h2 >> 8) / 16777216.0;
+            const double nu = mr.nu_lo + (mr.nu_hi - mr.nu_lo) * u1;
+            m.lambda = (float)(2.0 * (double)m.mu * nu / (1.0 - 2.0 * nu));
+            if (m.kind == KIND_SAND) {
+                const double sp = sin(mr.phi_lo + (mr.phi_hi - mr.phi_lo) * u2);
+                m.alpha = (float)(sqrt(2.0 / 3.0) * 2.0 * sp / (3.0 - sp));
+            }
+        }
         m3d Fd, U, V;
         double S[3];
         for (int k = 0; k < 9; ++k) Fd.a[k] = (double)smp[k];
@@ -501,22 +528,25 @@ void free_closure(sv_handle *h) {
 
 using namespace sv;
 
-extern "C" int sv_closure_harvest(sv_handle *h, float dt, uint32_t max_samples, float augment, uint32_t seed,
-                                  uint64_t *total_out) {
-    if (!h) return fail("sv_closure_harvest: NULL handle");
+extern "C" int sv_closure_harvest_from(sv_handle *h, sv_handle *src, float dt, uint32_t max_samples, float augment,
+                                       uint32_t seed, uint64_t *total_out) {
+    if (!h || !src) return fail("sv_closure_harvest: NULL handle");
     if (!(dt > 0.f)) return fail("sv_closure_harvest: dt must be positive");
     if (!(augment >= 0.f && augment < 0.5f)) return fail("sv_closure_harvest: augment must be in [0, 0.5)");
     if (!h->cl_count) CL_CUDA(cudaMalloc(&h->cl_count, sizeof(uint64_t)));
     const uint64_t room = CL_MAX_SAMPLES - std::min(CL_MAX_SAMPLES, h->cl_n);
     const uint64_t want = std::min<uint64_t>(max_samples, room);
-    if (want > 0 && h->n > 0) {
+    if (want > 0 && src->n > 0) {
         CL_CUDA(grow(&h->cl_samples, h->cl_cap, h->cl_n + want, CL_SAMPLE, h->stream));
-        const double keep = std::min(1.0, (double)want / (double)h->n);
+        // the source's state is read on the pool's stream once the source's
+        // queued work is done
+        if (src != h) CL_CUDA(cudaStreamSynchronize(src->stream));
+        const double keep = std::min(1.0, (double)want / (double)src->n);
         const uint32_t threshold = keep >= 1.0 ? 0xFFFFFFFFu : (uint32_t)(keep * 4294967295.0);
         CL_CUDA(cudaMemsetAsync(h->cl_count, 0, sizeof(uint64_t), h->stream));
-        const unsigned blocks = (unsigned)std::min<uint64_t>((h->n + 255) / 256, (uint64_t)sm_count() * 8);
-        k_harvest<<<blocks, 256, 0, h->stream>>>(h->side[h->cur], h->materials, h->n, dt, threshold, seed, augment,
-                                                 h->cl_samples + h->cl_n * CL_SAMPLE, h->cl_count, want);
+        const unsigned blocks = (unsigned)std::min<uint64_t>((src->n + 255) / 256, (uint64_t)sm_count() * 8);
+        k_harvest<<<blocks, 256, 0, h->stream>>>(src->side[src->cur], src->materials, src->n, dt, threshold, seed,
+                                                 augment, h->cl_samples + h->cl_n * CL_SAMPLE, h->cl_count, want);
         CL_CUDA(cudaGetLastError());
         uint64_t got = 0;
         CL_CUDA(cudaMemcpyAsync(&got, h->cl_count, sizeof(uint64_t), cudaMemcpyDeviceToHost, h->stream));
@@ -525,6 +555,11 @@ extern "C" int sv_closure_harvest(sv_handle *h, float dt, uint32_t max_samples, 
     }
     if (total_out) *total_out = h->cl_n;
     return 0;
+}
+
+extern "C" int sv_closure_harvest(sv_handle *h, float dt, uint32_t max_samples, float augment, uint32_t seed,
+                                  uint64_t *total_out) {
+    return sv_closure_harvest_from(h, h, dt, max_samples, augment, seed, total_out);
 }
 
 extern "C" int sv_closure_train(sv_handle *h, uint32_t iterations, uint32_t batch, float lr, uint32_t seed,
@@ -554,7 +589,8 @@ extern "C" int sv_closure_train(sv_handle *h, uint32_t iterations, uint32_t batc
         e = cudaMemcpyAsync(dperm, perm.data(), n * 4, cudaMemcpyHostToDevice, h->stream);
     }
     if (e == cudaSuccess) {
-        k_label<<<blocks, 256, 0, h->stream>>>(h->cl_samples, n, h->materials, dperm, rX, rY, rW);
+        const MatRanges mr{h->cl_ranges_on, h->cl_ranges[0], h->cl_ranges[1], h->cl_ranges[2], h->cl_ranges[3]};
+        k_label<<<blocks, 256, 0, h->stream>>>(h->cl_samples, n, dperm, rX, rY, rW, mr, seed);
         e = cudaGetLastError();
     }
     // 2. the yielding samples, compacted in order
@@ -847,5 +883,22 @@ extern "C" int sv_closure_get_pool(sv_handle *h, uint64_t first, uint64_t count,
     if (count && X) CL_CUDA(cudaMemcpy(X, h->cl_X + first * tc::NIN, count * tc::NIN * 4, cudaMemcpyDeviceToHost));
     if (count && Y) CL_CUDA(cudaMemcpy(Y, h->cl_Y + first * tc::NOUT, count * tc::NOUT * 4, cudaMemcpyDeviceToHost));
     if (hull) CL_CUDA(cudaMemcpy(hull, h->cl_hull, sizeof(closure::Hull), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+extern "C" int sv_closure_set_material_ranges(sv_handle *h, float nu_lo, float nu_hi, float phi_lo_deg,
+                                              float phi_hi_deg) {
+    if (!h) return fail("sv_closure_set_material_ranges: NULL handle");
+    if (nu_lo == 0.f && nu_hi == 0.f && phi_lo_deg == 0.f && phi_hi_deg == 0.f) {
+        h->cl_ranges_on = 0;
+        return 0;
+    }
+    if (!(nu_lo >= 0.f && nu_lo <= nu_hi && nu_hi < 0.5f))
+        return fail("sv_closure_set_material_ranges: need 0 <= nu_lo <= nu_hi < 0.5");
+    if (!(phi_lo_deg >= 0.f && phi_lo_deg <= phi_hi_deg && phi_hi_deg < 90.f))
+        return fail("sv_closure_set_material_ranges: need 0 <= phi_lo <= phi_hi < 90 degrees");
+    h->cl_ranges_on = 1;
+    h->cl_ranges[0] = nu_lo, h->cl_ranges[1] = nu_hi;
+    h->cl_ranges[2] = phi_lo_deg * (float)(M_PI / 180.0), h->cl_ranges[3] = phi_hi_deg * (float)(M_PI / 180.0);
     return 0;
 }

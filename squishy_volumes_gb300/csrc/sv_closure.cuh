@@ -30,6 +30,10 @@
 //   instead of locating the branches' kinks itself.
 // Raw targets (the network predicts (y - ym) / ys):
 //   y0..2 = ln s_i - e_i            plastic correction of the strains
+//                                   (measured more accurate than predicting
+//                                   ln s_i itself: the error then scales
+//                                   with the correction, which is small for
+//                                   most yielding particles)
 //   y3..5 = tau_i / (mu h)          principal Kirchhoff stress of the
 //                                   projected state, h the snow hardening
 #pragma once

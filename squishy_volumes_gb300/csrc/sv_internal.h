@@ -52,7 +52,8 @@ enum Counter : int {
     C_CTA_DONE = 12,     // CTAs of a self-latching particle pass that have finished
     C_TRANSFER_BAD = 13, // a direct download met an original index out of range or repeated
     C_ADT_MISS = 14,     // adaptive substeps whose speculative steps failed (fused form)
-    C_COUNT = 15,
+    C_SUMS_AT = 15,      // the grid updates take the fp64 conservation sums from this substep on
+    C_COUNT = 16,
 };
 
 // One side of the particle state (ping-pong).  Structure of arrays: pos and
@@ -284,6 +285,8 @@ struct sv_handle {
     uint64_t cl_xy_cap = 0;
     int cl_step = 0;                // Adam steps taken
     uint64_t cl_yielding = 0;       // yielding (weighted) samples of the last labelling
+    int cl_ranges_on = 0;           // labels draw nu / the friction angle from cl_ranges
+    float cl_ranges[4] = {0, 0, 0, 0};  // nu_lo, nu_hi, phi_lo, phi_hi (radians)
     float *cl_loss = nullptr;       // device scalar
     uint32_t *cl_err = nullptr;     // device flag
     uint64_t *cl_count = nullptr;   // device counter of the harvest

@@ -421,7 +421,9 @@ __global__ void __launch_bounds__(ELEM_THREADS)
 // Momentum -> velocity on grid_cur (slots of map `wc`), and zeroes grid_next
 // (slots of map `wn`) for the scatter that follows.  On the way it adds the
 // fp64 sums of mass and momentum over grid_cur's nodes (variants included)
-// into sums_cur, and zeroes sums_next with grid_next.
+// into sums_cur -- from substep counters[C_SUMS_AT] on (sv_step sets it to
+// the last substep of the call: the fp64 work costs 7 % of a substep) --
+// and zeroes sums_next with grid_next.
 __global__ void __launch_bounds__(ELEM_THREADS)
     k_grid_update(float4 *grid_cur, const uint32_t *active_cur, float4 *grid_next, uint64_t capacity, GridLayout L,
                   uint32_t *counters, int wc, int wn, col::VariantTable var, double *sums_cur, double *sums_next) {
@@ -430,6 +432,7 @@ __global__ void __launch_bounds__(ELEM_THREADS)
     if (sc > capacity) sc = capacity;
     if (sn > capacity) sn = capacity;
     if (grid_next && blockIdx.x == 0 && threadIdx.x < 4) sums_next[threadIdx.x] = 0.0;
+    const bool want_sums = counters[C_SUBSTEPS] >= counters[C_SUMS_AT];
     const uint64_t total = (sc > sn ? sc : sn) * 64;
     double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -449,7 +452,7 @@ __global__ void __launch_bounds__(ELEM_THREADS)
                             g.x += a.x, g.y += a.y, g.z += a.z, g.w += a.w;
                         }
             }
-            sm += (double)g.w, sx += (double)g.x, sy += (double)g.y, sz += (double)g.z;
+            if (want_sums) sm += (double)g.w, sx += (double)g.x, sy += (double)g.y, sz += (double)g.z;
             int x = 0, y = 0, z = 0;
             if (L.ground_mode != 0) {
                 int bx, by, bz;
@@ -461,6 +464,7 @@ __global__ void __launch_bounds__(ELEM_THREADS)
         }
         if (i < sn * 64) grid_next[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
+    if (!want_sums) return;  // uniform over the grid
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         sm += __shfl_xor_sync(0xffffffffu, sm, o);

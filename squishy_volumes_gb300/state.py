@@ -568,6 +568,13 @@ class CudaState:
                                            ct.byref(total)))
         return int(total.value)
 
+    def closure_harvest_from(self, other, dt: float, max_samples: int, augment: float = 0.0, seed: int = 0) -> int:
+        """Harvest the current state of another state into this one's pool."""
+        total = ct.c_uint64(0)
+        check(self._lib.sv_closure_harvest_from(self._h, other._h, float(dt), int(max_samples), float(augment),
+                                                int(seed), ct.byref(total)))
+        return int(total.value)
+
     def closure_train(self, iterations: int, batch: int = 65536, lr: float = 3e-3, seed: int = 0) -> float:
         loss = ct.c_float(0.0)
         check(self._lib.sv_closure_train(self._h, int(iterations), int(batch), float(lr), int(seed), ct.byref(loss)))
@@ -600,6 +607,12 @@ class CudaState:
             out[k] = hull[o:o + n].copy()
             o += n
         return X, Y, out
+
+    def closure_set_material_ranges(self, nu=(0.0, 0.0), friction_deg=(0.0, 0.0)):
+        """Label training samples with Poisson's ratios / friction angles drawn
+        from these ranges (all zero: the harvested materials)."""
+        check(self._lib.sv_closure_set_material_ranges(self._h, float(nu[0]), float(nu[1]), float(friction_deg[0]),
+                                                       float(friction_deg[1])))
 
     def closure_copy_from(self, other):
         """Take over the trained network, hull and normalisation of another state."""

@@ -181,3 +181,43 @@ def test_pool_counts(cuda_lib, trained):
     p = g.closure_pool()
     assert p["pairs"] == total
     assert 128 <= p["yielding_pairs"] <= total
+
+
+def test_material_ranges_cover_the_hull(cuda_lib):
+    """Labels drawn over material ranges: the pool's lambda / mu feature then
+    spans the ranges' ends whichever scenes the samples came from."""
+    s = _scene()
+    g, _ = _harvested(s, rounds=2)
+    with pytest.raises(SvError):
+        g.closure_set_material_ranges((0.3, 0.2), (25.0, 40.0))
+    with pytest.raises(SvError):
+        g.closure_set_material_ranges((0.2, 0.4), (25.0, 95.0))
+    g.closure_set_material_ranges((0.18, 0.42), (23.0, 42.0))
+    g.closure_train(0, 8192, 3e-3, seed=1)
+    _, _, hull = g.closure_training_pool(0, 1)
+    lo, hi = 2 * 0.18 / (1 - 0.36), 2 * 0.42 / (1 - 0.84)
+    assert hull["lo"][5] <= lo * 1.01 and hull["hi"][5] >= hi * 0.99, hull
+    # alpha of 23 and 42 degrees (feature 8, sand)
+    a = lambda d: np.sqrt(2 / 3) * 2 * np.sin(np.radians(d)) / (3 - np.sin(np.radians(d)))
+    assert hull["hi"][8] >= a(42.0) * 0.99, hull
+    g.close()
+
+
+def test_harvest_from_another_handle(cuda_lib):
+    """One pool gathers another handle's states: the samples carry their
+    materials, so the labels do not depend on the pool handle's table."""
+    s = _scene()
+    pool = CudaState.from_io_state(s.io_state, s.consts, s.extras)
+    other = CudaState.from_io_state(s.io_state, s.consts, s.extras)
+    for k in range(4):
+        assert other.step(20, s.dt, s.gravity) == (0, 20)
+        total = pool.closure_harvest_from(other, s.dt, 20000, 0.02, seed=k)
+    assert 20000 < total <= 80000
+    pool.closure_train(0, 8192, 3e-3, seed=1)
+    X, Y, hull = pool.closure_training_pool()
+    assert pool.closure_pool()["yielding_pairs"] == X.shape[0] > 0
+    # snow and sand both in the pool (features 3 and 4 are the one-hot kinds)
+    raw = X[:, 3] / hull["xs"][3] + hull["xm"][3]
+    assert (raw > 0.5).any() and (raw < 0.5).any()
+    other.close()
+    pool.close()
