@@ -230,8 +230,7 @@ int sv_sort_pairs(const uint32_t *keys, uint32_t *perm, uint64_t n);
  *  - The work is queued on `stream` (a cudaStream_t passed as void*, NULL for
  *    the default stream) and the call returns without waiting for it.
  *  - The first call on a device looks up the scratch array's device address
- *    (with that device current) and keeps it; make that first call before
- *    any stream capture.
+ *    (with that device current) and keeps it for later calls.
  *  - All calls share the one scratch array, so calls that can overlap on the
  *    GPU (other streams, other host threads) race: order them on one stream
  *    or synchronise between them.  The scratch needs no clearing between
