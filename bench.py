@@ -80,8 +80,12 @@ def parse():
     ap.add_argument("--error-substeps", type=int, default=3,
                     help="also run this many substeps from the initial state on the GPU and on the fp64 CPU oracle "
                          "and report the relative errors of x, v, C, F (0: off)")
-    ap.add_argument("--secondary", default="dam_break_8m",
-                    help="a second workload measured the same way and reported under 'secondary' ('' for none)")
+    ap.add_argument("--secondary", default="dam_break_8m,batched_64",
+                    help="comma-separated further workloads measured the same way: the first is reported under "
+                         "'secondary', the others under 'additional' ('' for none)")
+    ap.add_argument("--closure-workload", default="snow_sand_2m",
+                    help="also measure this workload with the learned closure against the return maps, reported "
+                         "under 'closure_check' ('' for none; --closure learned measures the headline instead)")
     ap.add_argument("--min-seconds", type=float, default=0.5,
                     help="repeat the K-substep timed region until the repeats cover this long; the median is reported")
     ap.add_argument("--max-repeats", type=int, default=2000)
@@ -654,13 +658,35 @@ def run_ours(args, rank, world, local):
         dist.init_process_group("nccl", device_id=dev)
     main = measure_scene(args, args.scene, rank, world, local, dev, primary=True)
     scene = main.pop("scene")
-    secondary = None
-    if args.secondary and args.secondary != args.scene:
-        sec = measure_scene(args, args.secondary, rank, world, local, dev, primary=False)
-        sec.pop("scene")
-        secondary = {k: sec[k] for k in ("value", "ms_per_step", "config", "roofline", "e2e", "gpu_launches",
-                                         "clocks", "fp64_svd_particles", "error_vs_fp64")}
-        secondary["unit"] = METRIC
+    # further workloads: each in its own handle, after the headline; a
+    # failure is reported in its record and does not cost the headline line
+    others = {}
+    for name in [x for x in args.secondary.split(",") if x and x != args.scene]:
+        try:
+            sec = measure_scene(args, name, rank, world, local, dev, primary=False)
+            sec.pop("scene")
+            rec = {k: sec[k] for k in ("value", "ms_per_step", "config", "roofline", "e2e", "gpu_launches",
+                                       "clocks", "fp64_svd_particles", "error_vs_fp64")}
+            rec["unit"] = METRIC
+        except Exception as exc:  # noqa: BLE001 -- recorded in the line
+            rec = {"error": f"{type(exc).__name__}: {exc}"[:400]}
+        others[name] = rec
+        torch.cuda.synchronize()
+    names = [x for x in args.secondary.split(",") if x and x != args.scene]
+    secondary = others.get(names[0]) if names else None
+    additional = {k: v for k, v in others.items() if not names or k != names[0]} or None
+    closure_check = None
+    if args.closure_workload and args.closure == "plain" and world == 1:
+        import copy
+
+        cargs = copy.copy(args)
+        cargs.closure, cargs.no_autotune, cargs.no_e2e, cargs.error_substeps = "learned", True, True, 0
+        try:
+            rec = measure_scene(cargs, args.closure_workload, rank, world, local, dev, primary=True)
+            closure_check = {"workload": args.closure_workload, "value_learned": rec["value"], "unit": METRIC,
+                             **(rec["closure"] or {})}
+        except Exception as exc:  # noqa: BLE001 -- recorded in the line
+            closure_check = {"workload": args.closure_workload, "error": f"{type(exc).__name__}: {exc}"[:400]}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(scene, args.cpu_seconds)
@@ -689,6 +715,8 @@ def run_ours(args, rank, world, local):
         "closure": main["closure"],
         "bake": main["bake"],
         "secondary": secondary,
+        "additional": additional,
+        "closure_check": closure_check,
     }
     if rank == 0:
         print(json.dumps(line))
