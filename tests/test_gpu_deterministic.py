@@ -1,7 +1,7 @@
 """The deterministic P2G mode (sv_consts.deterministic_p2g = 1).
 
-The north-star correctness clause asks grid mass to "match exactly to FP32
-rounding of a deterministic segmented sum".  The reference sums each node's
+Grid mass must match exactly the fp32 rounding of a deterministic
+segmented sum.  The reference sums each node's
 contributions in whatever order its contributor lists were filled under a
 mutex (rust/crates/cpu/src/phase/update_grid_nodes.rs:101-122), so its
 result is not reproducible; the oracle's svo_deterministic_grid_mass fixes
