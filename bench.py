@@ -60,6 +60,8 @@ def parse():
                     help="skip sv_autotune (by default the binning interval x CTAs/SM candidates are timed first "
                          "and the fastest is kept; the handle's defaults win unless beaten by more than 2 %%)")
     ap.add_argument("--no-graphs", action="store_true", help="launch every kernel directly (no CUDA graphs)")
+    ap.add_argument("--deterministic", action="store_true",
+                    help="the deterministic P2G mode (fixed summation order, fp32 positions, no graphs)")
     ap.add_argument("--closure", default="plain", choices=["plain", "learned"],
                     help="snow/sand constitutive update: SVD + return map, or the learned closure (trained first)")
     ap.add_argument("--closure-source", default="batched_64,self",
@@ -341,6 +343,8 @@ def measure_scene(args, name, rank, world, local, dev, primary):
         scene = made
         n = scene.io_state.particles.n
         scene.extras.sort_interval = args.sort_interval
+        if args.deterministic and primary:
+            scene.extras.deterministic_p2g, scene.extras.position_form = 1, 0
         make_gpu = lambda: CudaState.from_io_state(scene.io_state, scene.consts, scene.extras)
         h2d_particles = [scene.io_state.particles]
     gpu = make_gpu()

@@ -465,21 +465,27 @@ __global__ void __launch_bounds__(ELEM_THREADS)
         if (i < sn * 64) grid_next[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     if (!want_sums) return;  // uniform over the grid
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        sm += __shfl_xor_sync(0xffffffffu, sm, o);
-        sx += __shfl_xor_sync(0xffffffffu, sx, o);
-        sy += __shfl_xor_sync(0xffffffffu, sy, o);
-        sz += __shfl_xor_sync(0xffffffffu, sz, o);
-    }
-    __shared__ double red[ELEM_THREADS / 32][4];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) red[warp][0] = sm, red[warp][1] = sx, red[warp][2] = sy, red[warp][3] = sz;
+    // The block's sum in fp64 with few fp64 instructions (about 16 clocks
+    // per warp instruction on this part): every thread's partial sums go
+    // to shared memory and warp 0 alone adds them up, rather than eight
+    // warps running a shuffle tree each.
+    __shared__ double red[4][ELEM_THREADS];
+    red[0][threadIdx.x] = sm, red[1][threadIdx.x] = sx, red[2][threadIdx.x] = sy, red[3][threadIdx.x] = sz;
     __syncthreads();
-    if (threadIdx.x < 4) {
-        double t = 0.0;
-        for (int w = 0; w < ELEM_THREADS / 32; ++w) t += red[w][threadIdx.x];
-        if (t != 0.0) atomicAdd(&sums_cur[threadIdx.x], t);
+    if (threadIdx.x < 32) {
+        double t[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+        for (int j = 0; j < ELEM_THREADS / 32; ++j)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) t[c] += red[c][threadIdx.x + 32 * j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) t[c] += __shfl_xor_sync(0xffffffffu, t[c], o);
+        if (threadIdx.x < 4) {
+            const double v = threadIdx.x == 0 ? t[0] : threadIdx.x == 1 ? t[1] : threadIdx.x == 2 ? t[2] : t[3];
+            if (v != 0.0) atomicAdd(&sums_cur[threadIdx.x], v);
+        }
     }
 }
 

@@ -40,7 +40,7 @@ def _grid_vs_oracle(oracle_mod, io_state, consts, extras, dt, gravity):
     np.testing.assert_array_equal(g.masses.view(np.uint32), m.view(np.uint32))
 
 
-@pytest.mark.parametrize("scene", ["small_mixed", "cube_64k"])
+@pytest.mark.parametrize("scene", ["small_mixed", "cube_64k", "three_boxes_1m"])
 def test_deterministic_grid_mass_is_bit_exact(cuda_lib, oracle_mod, scene):
     s = scenes.SCENES[scene]()
     _grid_vs_oracle(oracle_mod, s.io_state, s.consts, s.extras, s.dt, s.gravity)
