@@ -520,7 +520,7 @@ int ensure_net(sv_handle *h, uint32_t seed) {
 
 void free_closure(sv_handle *h) {
     cudaFree(h->cl_params), cudaFree(h->cl_grad), cudaFree(h->cl_m), cudaFree(h->cl_v), cudaFree(h->cl_img);
-    cudaFree(h->cl_hull), cudaFree(h->cl_samples), cudaFree(h->cl_X), cudaFree(h->cl_Y), cudaFree(h->cl_W);
+    cudaFree(h->cl_hull), cudaFree(h->cl_samples), cudaFree(h->cl_X), cudaFree(h->cl_Y);
     cudaFree(h->cl_loss), cudaFree(h->cl_err), cudaFree(h->cl_count), cudaFree(h->cl_sums);
 }
 

@@ -279,9 +279,9 @@ struct sv_handle {
     float *cl_params = nullptr, *cl_grad = nullptr, *cl_m = nullptr, *cl_v = nullptr;  // fp32 master + Adam
     uint8_t *cl_img = nullptr;      // packed bf16 weight image
     void *cl_hull = nullptr;        // closure::Hull of the training features
-    float *cl_samples = nullptr;    // [cl_cap][CL_SAMPLE]: trial F, plastic J, material index bits
+    float *cl_samples = nullptr;    // [cl_cap][CL_SAMPLE]: trial F, plastic J, material kind and parameters
     uint64_t cl_n = 0, cl_cap = 0;  // harvested samples
-    float *cl_X = nullptr, *cl_Y = nullptr, *cl_W = nullptr;  // features, targets, weights
+    float *cl_X = nullptr, *cl_Y = nullptr;  // normalised features and targets of the yielding samples
     uint64_t cl_xy_cap = 0;
     int cl_step = 0;                // Adam steps taken
     uint64_t cl_yielding = 0;       // yielding (weighted) samples of the last labelling
