@@ -479,11 +479,18 @@ def measure_scene(args, name, rank, world, local, dev, primary):
         fps = scene.consts.frames_per_second
         frame_substeps = int(math.ceil((1.0 / fps) / scene.dt))
         frame_substeps = min(frame_substeps, scene.substeps)
-        reps_e2e = 2
+        reps_e2e = 3
         h2d = sum(q.nbytes() for q in h2d_particles)
         d2h = 0
-        t0 = time.perf_counter()
-        for _ in range(reps_e2e):
+        # one untimed step first: the process's first create / graph capture
+        # / download pays one-off costs (module loading, the first mapping of
+        # the output arrays' pages, which later steps' fresh arrays reuse
+        # from the host allocator); every timed step still creates its
+        # handle, uploads, captures its graphs, steps and downloads into
+        # fresh arrays
+        for rep in range(reps_e2e + 1):
+            if rep == 1:
+                t0 = time.perf_counter()
             st_ = make_gpu()
             params = RunParameters(target_time=frame_substeps * scene.dt * (1 - 1e-9), max_time_step=scene.dt)
             io, err = st_.produce_next_state(Harness(), FrameInput(scene.consts, scene.gravity), params)
@@ -498,7 +505,7 @@ def measure_scene(args, name, rank, world, local, dev, primary):
             "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h),
             "substeps_per_step": frame_substeps,
-            "step": "sv_create (upload) + one frame of substeps + sv_download",
+            "step": "sv_create (upload) + one frame of substeps + sv_download, mean of 3 after 1 untimed",
         }
 
     bake = None
