@@ -142,7 +142,7 @@ typedef struct sv_handle sv_handle;
 /* CpuState::from_io_state (cpu/src/cpu_state.rs:25-66): uploads the particles
  * and sizes the sparse grid.  Fails on invalid flags (neither or both of
  * IS_SOLID/IS_FLUID, like core/src/initialization.rs:197-201), on a domain
- * whose dense block index exceeds 2^26 blocks, or on a CUDA error. */
+ * whose dense block index reaches 2^26 blocks, or on a CUDA error. */
 int sv_create(const sv_consts *consts, const sv_particles *particles, sv_handle **out);
 
 /* The substep loop of CpuState::produce_next_state (cpu_state.rs:167-194)

@@ -803,9 +803,9 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
         L.origin[a] = (int32_t)(cmin - 8);
         L.nb[a] = (int32_t)((cmax - L.origin[a]) >> 2) + 4;
         total *= (uint64_t)L.nb[a];
-        if (total > (1ull << 26)) {
+        if (total >= (1ull << 26)) {
             free_handle(h);
-            return fail("sv_create: the dense block index would exceed 2^26 blocks of 4^3 nodes "
+            return fail("sv_create: the dense block index would reach 2^26 blocks of 4^3 nodes "
                         "(domain / grid_node_size too large)");
         }
     }

@@ -19,8 +19,9 @@
 //             force of substep t+1 (external_force.rs:17-50) and its stress
 //             (scatter_momentum.rs:22-93) into a per-particle scatter record.
 //             Warps then replay the records with one lane per stencil node,
-//             accumulating runs of same-cell particles in registers, into the
-//             8^3-node shared tile of G_t+1, flushed with float4 atomics.
+//             summing the records of each cell in registers, and add each
+//             cell's sums to G_t+1 with one float4 reduction per node (the
+//             segment's 27 blocks of G_t+1 stay resident in L2).
 //   sort      every `sort_interval` substeps: binning keys, a stable radix sort
 //             (bit-exact against a CPU stable sort) and the 4^3-block
 //             segments; the grid blocks of the next substeps are claimed for
@@ -597,14 +598,16 @@ __global__ void __launch_bounds__(ELEM_THREADS) k_interp_vertex_normals(FinDev f
 // ------------------------------------------------------------------ particle kernel
 // Scatter tile layout: node (tx, ty, tz) at tx*PX + ty*PY + tz.  With PX = 3
 // and PY = 9 (mod 32) the 27 stencil offsets 9i + 3j + k of any cell fall in
-// 27 distinct shared-memory banks, so a warp's lane-per-node atomics never
-// conflict.
+// 27 distinct shared-memory banks, so a warp's lane-per-node lookups of the
+// nodes' grid indices never conflict.  A grid index is slot * 64 + node, below
+// 2^32 - 1 (NO_NODE) because the block index holds fewer than 2^26 blocks.
+constexpr uint32_t NO_NODE = 0xFFFFFFFFu;
 constexpr int PY = 9, PX = 99;
 constexpr int PLANE = 7 * PX + 7 * PY + 8;  // 764 floats
 
 struct Shared {
     float4 gv[TILE_NODES];      // velocity tile of grid_cur (G2P2G), tx*64 + ty*8 + tz
-    float pt[4][PLANE];         // mass, px, py, pz tile of grid_next
+    uint32_t gidx[PLANE];       // float4 index in grid_next of each tile node (NO_NODE: no claimed block)
     Rec rec[PT];
     float2 meta[PT];            // (record cell as bits: REC_NONE, tile index or REC_GLOBAL; mass)
     int4 gbase[PT];             // global base cell of REC_GLOBAL records
@@ -622,12 +625,24 @@ __device__ __forceinline__ int tile_local(int tx, int ty, int tz) {
     return ((tx + 3) & 3) * 16 + ((ty + 3) & 3) * 4 + ((tz + 3) & 3);
 }
 
+// Adds one cell's summed contributions (mass, px | py, pz) to tile node t:
+// one float4 reduction into grid_next, which the 27 blocks of a segment keep
+// resident in L2.
+__device__ __forceinline__ void flush_node(Shared &sh, const StepArgs &A, int t, float2 amx, float2 ayz) {
+    const uint32_t g = sh.gidx[t];
+    if (g != NO_NODE)
+        atomicAdd(&A.grid_next[g], make_float4(amx.y, ayz.x, ayz.y, amx.x));
+    else
+        atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR), sh.raised = 1;
+}
+
 // Replays the chunk's scatter records: warp w owns records [32w, 32w + 32);
-// lane l < 27 is stencil offset (l/9, (l/3)%3, l%3).  Run starts and ends
-// (consecutive records with the same base cell) come from two ballots, so the
-// 32-record loop is unrolled with warp-uniform predicates only; a run is
-// summed in registers and leaves with one conflict-free shared atomic per
-// lane and component.
+// lane l < 27 is stencil offset (l/9, (l/3)%3, l%3).  The records of one
+// tile cell (found with a match over the warp's keys, wherever they sit in
+// the chunk) are summed in registers and leave once per lane, so each
+// distinct cell of the warp's records costs one float4 reduction per node
+// however far the particles drifted since the binning sort.  Two records per
+// step keep two sets of shared loads in flight.
 __device__ __forceinline__ void scatter_records(Shared &sh, int count, const StepArgs &A) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int li = lane / 9, lj = (lane / 3) % 3, lk = lane % 3;
@@ -637,37 +652,38 @@ __device__ __forceinline__ void scatter_records(Shared &sh, int count, const Ste
     if (r0 >= count) return;
     const float2 me = lane < count - r0 ? sh.meta[r0 + lane] : make_float2(__uint_as_float(REC_NONE), 0.f);
     const uint32_t key = __float_as_uint(me.x);
-    const uint32_t prev = __shfl_up_sync(0xffffffffu, key, 1);
-    const uint32_t next = __shfl_down_sync(0xffffffffu, key, 1);
     const bool valid = key < REC_GLOBAL;  // a tile index
-    const uint32_t start = __ballot_sync(0xffffffffu, valid && (lane == 0 || prev != key));
-    const uint32_t end = __ballot_sync(0xffffffffu, valid && (lane == 31 || next != key));
-    const uint32_t vmask = __ballot_sync(0xffffffffu, valid);
     const uint32_t gmask = __ballot_sync(0xffffffffu, key == REC_GLOBAL);
     const uint32_t cmask = __ballot_sync(0xffffffffu, key == REC_VARIANT);
-    float2 amx = make_float2(0.f, 0.f), ayz = make_float2(0.f, 0.f);
-    // unrolled by 4 (measured against 1, 2 and 8: by 8 the kernel grows and
-    // misses the instruction cache, 2.7 % slower on the 1M three-box scene;
-    // by 2 and 1 the 8M dam break is 0.7 and 3 % slower)
-#pragma unroll 4
-    for (int r = 0; r < 32; ++r) {
-        if ((vmask >> r) & 1u) {
-            const float4 nd = rec_node(sh.rec[r0 + r], li, lj, lk);
-            const float w = nd.w;
-            const float m = __shfl_sync(0xffffffffu, me.y, r);
-            if ((start >> r) & 1u) amx = make_float2(0.f, 0.f), ayz = make_float2(0.f, 0.f);
-            amx = __ffma2_rn(make_float2(w, w), make_float2(m, nd.x), amx);
-            ayz = __ffma2_rn(make_float2(w, w), make_float2(nd.y, nd.z), ayz);
-            if ((end >> r) & 1u) {
-                const int t = (int)__shfl_sync(0xffffffffu, key, r) + off;
-                if (active) {
-                    atomicAdd(&sh.pt[0][t], amx.x);
-                    atomicAdd(&sh.pt[1][t], amx.y);
-                    atomicAdd(&sh.pt[2][t], ayz.x);
-                    atomicAdd(&sh.pt[3][t], ayz.y);
-                }
+    // lanes with the same key; the lowest valid lane of each group leads it
+    const uint32_t grp = __match_any_sync(0xffffffffu, key);
+    const uint32_t lead = __ballot_sync(0xffffffffu, valid && (grp & ((1u << lane) - 1u)) == 0u);
+    const Rec *rp = &sh.rec[r0];
+    for (uint32_t lb = lead; lb; lb &= lb - 1) {
+        const int s = __ffs(lb) - 1;
+        uint32_t mm = __shfl_sync(0xffffffffu, grp, s);
+        float2 amx = make_float2(0.f, 0.f), ayz = make_float2(0.f, 0.f);
+        while (mm) {
+            const int ra = __ffs(mm) - 1;
+            mm &= mm - 1;
+            const float4 na = rec_node(rp[ra], li, lj, lk);
+            const float ma = __shfl_sync(0xffffffffu, me.y, ra);
+            if (mm) {
+                const int rb = __ffs(mm) - 1;
+                mm &= mm - 1;
+                const float4 nb = rec_node(rp[rb], li, lj, lk);
+                const float mb = __shfl_sync(0xffffffffu, me.y, rb);
+                amx = __ffma2_rn(make_float2(na.w, na.w), make_float2(ma, na.x), amx);
+                ayz = __ffma2_rn(make_float2(na.w, na.w), make_float2(na.y, na.z), ayz);
+                amx = __ffma2_rn(make_float2(nb.w, nb.w), make_float2(mb, nb.x), amx);
+                ayz = __ffma2_rn(make_float2(nb.w, nb.w), make_float2(nb.y, nb.z), ayz);
+            } else {
+                amx = __ffma2_rn(make_float2(na.w, na.w), make_float2(ma, na.x), amx);
+                ayz = __ffma2_rn(make_float2(na.w, na.w), make_float2(na.y, na.z), ayz);
             }
         }
+        const int t = (int)__shfl_sync(0xffffffffu, key, s) + off;
+        if (active) flush_node(sh, A, t, amx, ayz);
     }
     // records outside the tile: straight to global memory
     for (uint32_t g = gmask; g; g &= g - 1) {
@@ -915,9 +931,13 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
             sh.slot_next[threadIdx.x] = A.map_next[nbk];
             if (GATHER) sh.slot_cur[threadIdx.x] = A.map_cur[nbk];
         }
-        if (SCATTER)
-            for (int t = threadIdx.x; t < 4 * PLANE; t += PT) (&sh.pt[0][0])[t] = 0.f;
         __syncthreads();
+        if (SCATTER)
+            for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
+                const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
+                const int32_t slot = sh.slot_next[tile_neighbour(tx, ty, tz)];
+                sh.gidx[tx * PX + ty * PY + tz] = slot >= 0 ? (uint32_t)slot * 64u + (uint32_t)tile_local(tx, ty, tz) : NO_NODE;
+            }
         if (GATHER) {
             for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
                 const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
@@ -933,7 +953,8 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
             float rmass = 0.f;
             // this thread's particle; live across the closure network pass
             bool work = false;
-            uint32_t p = 0, packed = 0;
+            uint32_t p = 0, packed = 0, orig_p = 0;
+            float vel_w = 1.f;
             float4 pos = make_float4(0.f, 0.f, 0.f, 0.f);
             int4 cell = make_int4(0, 0, 0, 0);
             m3f F, C;
@@ -948,6 +969,11 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
                 pos = A.in.pos[p];
                 packed = __float_as_uint(pos.w);
                 if (CELL) cell = A.in.cell[p];
+                // issued with the position: neither waits for the material
+                // table, and the copy of orig does not wait behind this
+                // particle's stores
+                if (!LOAD_VC) vel_w = A.in.vel[p].w;
+                if (G2P) orig_p = A.in.orig[p];
                 if (packed & SV_TOMBSTONED) {
                     if (G2P) {
                         copy_particle(A.in, A.out, A.n, p, i, CELL);
@@ -964,7 +990,7 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
                         v[0] = vel.x, v[1] = vel.y, v[2] = vel.z;
                         plastic_j = vel.w;
                     } else {
-                        plastic_j = (kind == KIND_SNOW || MODE == MODE_G2P_ONLY) ? A.in.vel[p].w : 1.f;
+                        plastic_j = (kind == KIND_SNOW || MODE == MODE_G2P_ONLY) ? vel_w : 1.f;
                         // ---- G2P (collect_velocity.rs:40-72)
                         int base[3];
                         float fx[3];
@@ -1200,7 +1226,7 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
                     store_mat9(A.out.C, A.n, i, C);
                     store_mat9(A.out.F, A.n, i, F);
                     A.out.energy[i] = energy;
-                    A.out.orig[i] = A.in.orig[p];
+                    A.out.orig[i] = orig_p;
                     if constexpr (FIN) {
                         // the bits of the completed substep; the next
                         // scatter's Collide (below) replaces the ones in effect
@@ -1263,27 +1289,13 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
             if (SCATTER) {
                 sh.meta[threadIdx.x] = make_float2(__uint_as_float(rcell), rmass);
                 // Warp w replays only its own threads' records, so warp
-                // barriers would do here; measured 2 % slower than keeping the
-                // CTA's warps in step, so the CTA barriers stay.
+                // barriers would do here; measured 1-2 % slower than keeping
+                // the CTA's warps in step, so the CTA barriers stay.
                 __syncthreads();
                 scatter_records(sh, count, A);
                 __syncthreads();
             }
         }
-        // flush the tile of grid_next
-        if (SCATTER)
-            for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
-                const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
-                const int s = tx * PX + ty * PY + tz;
-                const float m = sh.pt[0][s], px = sh.pt[1][s], py = sh.pt[2][s], pz = sh.pt[3][s];
-                if (m != 0.f || px != 0.f || py != 0.f || pz != 0.f) {
-                    const int32_t slot = sh.slot_next[tile_neighbour(tx, ty, tz)];
-                    if (slot >= 0)
-                        atomicAdd(&A.grid_next[(uint64_t)slot * 64 + tile_local(tx, ty, tz)], make_float4(px, py, pz, m));
-                    else
-                        atomicOr(&A.counters[C_STATUS], ST_MOVED_FAR), sh.raised = 1;
-                }
-            }
         __syncthreads();
     }
     if (G2P_LIMITS_MODE && g2p_limits) {
