@@ -833,6 +833,7 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     uint64_t tiles = (n + 2047) / 2048 + 1;
     arena.add(&h->materials, mats.size()), arena.add(&h->scenes, n_scenes);
     arena.add(&h->keys, n), arena.add(&h->sorted_keys, n), arena.add(&h->perm, n), arena.add(&h->inv, n);
+    arena.add(&h->defer_list, n);
     arena.add(&h->grid_sums, 8);
     arena.add(&h->seg_start, n + 1), arena.add(&h->seg_block, n), arena.add(&h->counters, C_COUNT);
     arena.add((char **)&h->sort_temp, h->sort_temp_bytes), arena.add(&h->tile_counts, tiles);

@@ -53,7 +53,8 @@ enum Counter : int {
     C_TRANSFER_BAD = 13, // a direct download met an original index out of range or repeated
     C_ADT_MISS = 14,     // adaptive substeps whose speculative steps failed (fused form)
     C_SUMS_AT = 15,      // the grid updates take the fp64 conservation sums from this substep on
-    C_COUNT = 16,
+    C_DEFER = 16,        // particles of this substep's fused pass left for its fp64 pass (defer_list)
+    C_COUNT = 17,
 };
 
 // One side of the particle state (ping-pong).  Structure of arrays: pos and
@@ -132,6 +133,7 @@ struct sv_handle {
     bool keys_valid = false;
     uint32_t *sorted_keys = nullptr;  // [n]
     uint32_t *perm = nullptr;         // [n] device slot of each sorted position
+    uint32_t *defer_list = nullptr;   // [n] sorted positions the fused pass left for its fp64 pass
     void *sort_temp = nullptr;
     size_t sort_temp_bytes = 0;
 

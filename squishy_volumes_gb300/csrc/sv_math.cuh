@@ -158,8 +158,10 @@ __device__ __forceinline__ void svd3(const Mat3<T> &F, Mat3<T> &U, T S[3], Mat3<
 // test of one-sided Jacobi): near-identity F then gives U = V = I up to
 // rounding instead of the arbitrary 45-degree rotations of a degenerate
 // pair, whose fp32 rounding would put ~1e-7 noise into U V^T -- the fluid
-// and sand returns rebuild F from U V^T every substep.
-__device__ __forceinline__ void svd3_fast(const m3f &F, m3f &U, float S[3], m3f &V) {
+// and sand returns rebuild F from U V^T every substep.  Returns true when a
+// column vanished (degenerate F): U is then incomplete and the caller takes
+// the fp64 path.
+__device__ __forceinline__ bool svd3_fast_f32(const m3f &F, m3f &U, float S[3], m3f &V) {
     constexpr float EPS2 = 1.4210855e-14f;  // FLT_EPSILON^2
     float A[9];
 #pragma unroll
@@ -210,42 +212,44 @@ __device__ __forceinline__ void svd3_fast(const m3f &F, m3f &U, float S[3], m3f 
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) V.a[i] = W[i];
-    if (!(good[0] && good[1] && good[2])) {
-        // Degenerate F: fall back to the general path in fp64 for U.
-        m3d Fd, Ud, Vd;
-        double Sd[3];
-#pragma unroll
-        for (int i = 0; i < 9; ++i) Fd.a[i] = (double)F.a[i];
-        svd3<double>(Fd, Ud, Sd, Vd, 12);
-#pragma unroll
-        for (int i = 0; i < 9; ++i) U.a[i] = (float)Ud.a[i], V.a[i] = (float)Vd.a[i];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) S[i] = (float)Sd[i];
-    }
+    // a vanished column: degenerate F, whose U the fp64 path completes
+    return !(good[0] && good[1] && good[2]);
 }
 
-// fp32 SVD of a particle's F with the fp64 redo for flagged particles:
-// policy 1 redoes it when det F < 0.05, policy 2 also when two singular
-// values are closer than 1e-4.
-__device__ __forceinline__ void particle_svd(const m3f &F, m3f &U, float S[3], m3f &V, uint32_t policy,
-                                             uint32_t &fp64_count) {
-    svd3_fast(F, U, S, V);
-    bool redo = false;
-    if (policy >= 1 && det3(F) < 0.05f) redo = true;
-    if (policy >= 2) {
-        float g = fminf(fabsf(S[0] - S[1]), fminf(fabsf(S[1] - S[2]), fabsf(S[0] - S[2])));
+// The fp64 SVD of an fp32 F, rounded back to fp32.
+__device__ __forceinline__ void svd3_fp64(const m3f &F, m3f &U, float S[3], m3f &V) {
+    m3d Fd, Ud, Vd;
+    double Sd[3];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Fd.a[k] = (double)F.a[k];
+    svd3<double>(Fd, Ud, Sd, Vd, 12);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) U.a[k] = (float)Ud.a[k], V.a[k] = (float)Vd.a[k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) S[k] = (float)Sd[k];
+}
+
+// Whether a particle's SVD is redone in fp64: a degenerate F always; policy
+// 1 when det F < 0.05, policy 2 also when two singular values are closer
+// than 1e-4.  SVD_ALWAYS_FP64 forces it (the deferred fp64 pass).
+constexpr uint32_t SVD_ALWAYS_FP64 = 0x100u;
+__device__ __forceinline__ bool svd_needs_fp64(const m3f &F, const float S[3], bool degenerate, uint32_t policy) {
+    bool redo = degenerate || (policy & SVD_ALWAYS_FP64);
+    if ((policy & 0xFFu) >= 1 && det3(F) < 0.05f) redo = true;
+    if ((policy & 0xFFu) >= 2) {
+        const float g = fminf(fabsf(S[0] - S[1]), fminf(fabsf(S[1] - S[2]), fabsf(S[0] - S[2])));
         if (g < 1e-4f) redo = true;
     }
-    if (redo) {
-        m3d Fd, Ud, Vd;
-        double Sd[3];
-#pragma unroll
-        for (int k = 0; k < 9; ++k) Fd.a[k] = (double)F.a[k];
-        svd3<double>(Fd, Ud, Sd, Vd, 12);
-#pragma unroll
-        for (int k = 0; k < 9; ++k) U.a[k] = (float)Ud.a[k], V.a[k] = (float)Vd.a[k];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) S[k] = (float)Sd[k];
+    return redo;
+}
+
+// fp32 SVD of a particle's F with the fp64 redo for flagged particles
+// (svd_needs_fp64).
+__device__ __forceinline__ void particle_svd(const m3f &F, m3f &U, float S[3], m3f &V, uint32_t policy,
+                                             uint32_t &fp64_count) {
+    const bool degenerate = svd3_fast_f32(F, U, S, V);
+    if (svd_needs_fp64(F, S, degenerate, policy)) {
+        svd3_fp64(F, U, S, V);
         ++fp64_count;
     }
 }

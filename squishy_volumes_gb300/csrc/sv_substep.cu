@@ -97,6 +97,7 @@ struct StepArgs {
     const float4 *grid_cur;
     float4 *grid_next;
     uint32_t *keys_out;  // nullptr: keys not needed after this substep
+    uint32_t *defer_list;  // sorted positions left by the fused pass for its fp64 pass ([C_DEFER] of them)
     const uint8_t *closure_img;          // packed network weights (learned mode)
     const closure::Hull *closure_hull;   // training hull of the features (learned mode)
     adaptive::State *adt;                // adaptive time steps: device dt and reductions (else nullptr)
@@ -843,6 +844,7 @@ __device__ __forceinline__ void cta_done(const StepArgs &A, uint32_t stop_at_sta
             A.counters[C_STOP] = status & STOP_MASK;
             if (!stop_at_start) A.counters[C_SUBSTEPS] += 1;
             A.counters[C_CTA_DONE] = 0;
+            A.counters[C_DEFER] = 0;  // the fused pass's fp64 list has been served
         }
     }
 }
@@ -853,13 +855,24 @@ __device__ __forceinline__ void cta_done(const StepArgs &A, uint32_t stop_at_sta
 // frame-input variant four.
 // FIN: a frame input is loaded -- interpolated gravity and goals, Collide
 // (collide.rs:21-206) before the scatter, collider bits and their variants.
+// REDO (with MODE_G2P2G): the fused pass's fp64 pass.  The plain fused pass
+// holds no fp64 SVD code: inlined, that rarely taken path gave the pass a
+// 256-byte stack frame and four times the register spills of the fp32 path
+// (0.66M against 0.20M local loads per 1M-particle launch).  A particle whose
+// fp32 SVD is degenerate or flagged by the fp64 policy is left out of the
+// fused pass and listed; the REDO pass then runs the whole substep for the
+// listed particles (from the same input state and grid, the gather and
+// scatter through global memory) with the fp64 SVD, and latches the stop
+// bits for both.
 #ifndef SV_PARTICLE_CTAS_PER_SM
 #define SV_PARTICLE_CTAS_PER_SM 5
 #endif
-template <bool CELL, int MODE, bool FIN = false>
+template <bool CELL, int MODE, bool FIN = false, bool REDO = false>
 __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 : SV_PARTICLE_CTAS_PER_SM)
     k_particles(StepArgs A) {
+    static_assert(!REDO || (MODE == MODE_G2P2G && !FIN), "the fp64 pass follows the plain fused pass");
     constexpr bool LEARNED = MODE == MODE_G2P2G_LEARNED;
+    constexpr bool DEFER64 = MODE == MODE_G2P2G && !FIN && !REDO;
     // what the pass does: gather from the grid, advance the particles (and
     // write them out in sorted order), scatter into the next grid
     constexpr bool ADT_FUSED = MODE == MODE_G2P2G_ADAPTIVE;
@@ -873,7 +886,7 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
     if (MODE == MODE_P2G && A.adt_pass == 4 && !*(volatile const uint32_t *)&A.adt->p2g_redo) return;
     const uint32_t stop_at_start = stopped(A.counters);
     if (stop_at_start) {
-        if (G2P) {
+        if (G2P && !REDO) {
             // Keep the state as it is (identity copy) so the buffer swap is a no-op.
             for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x)
                 copy_particle(A.in, A.out, A.n, i, i, CELL);
@@ -912,7 +925,7 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
     // limits of the advanced state
     constexpr bool FORCE_LIMITS_MODE = MODE == MODE_ADVANCE || MODE == MODE_G2P_ADVANCE || ADT_FUSED;
     float lim_sound = adaptive::NONE, lim_iso = adaptive::NONE;
-    if (G2P) {
+    if (G2P && !REDO) {
         // particles that were tombstoned at binning time are carried over
         for (uint64_t i = nlive + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.n; i += (uint64_t)gridDim.x * blockDim.x) {
             copy_particle(A.in, A.out, A.n, A.perm ? A.perm[i] : i, i, CELL);
@@ -920,383 +933,407 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
         }
     }
     uint32_t fp64_count = 0, fallback = 0;
-    for (uint32_t seg = blockIdx.x; seg < nseg; seg += gridDim.x) {
-        const uint32_t b = A.seg_block[seg];
-        const uint32_t start = A.seg_start[seg], end = A.seg_start[seg + 1];
-        int bx, by, bz;
-        block_coords(b, A.L, bx, by, bz);
-        const int org[3] = {A.L.origin[0] + 4 * bx - 1, A.L.origin[1] + 4 * by - 1, A.L.origin[2] + 4 * bz - 1};
-        if (threadIdx.x < 27) {
-            const uint32_t nbk = neighbour27(b, threadIdx.x, A.L);
-            sh.slot_next[threadIdx.x] = A.map_next[nbk];
-            if (GATHER) sh.slot_cur[threadIdx.x] = A.map_cur[nbk];
-        }
-        __syncthreads();
-        if (SCATTER)
-            for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
-                const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
-                const int32_t slot = sh.slot_next[tile_neighbour(tx, ty, tz)];
-                sh.gidx[tx * PX + ty * PY + tz] = slot >= 0 ? (uint32_t)slot * 64u + (uint32_t)tile_local(tx, ty, tz) : NO_NODE;
-            }
-        if (GATHER) {
-            for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
-                const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
-                const int32_t slot = sh.slot_cur[tile_neighbour(tx, ty, tz)];
-                sh.gv[t] = slot >= 0 ? A.grid_cur[(uint64_t)slot * 64 + tile_local(tx, ty, tz)] : make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-            __syncthreads();
-        }
-        for (uint32_t c0 = start; c0 < end; c0 += PT) {
-            const uint32_t i = c0 + threadIdx.x;
-            const int count = (int)min((uint32_t)PT, end - c0);
-            uint32_t rcell = REC_NONE;
-            float rmass = 0.f;
-            // this thread's particle; live across the closure network pass
-            bool work = false;
-            uint32_t p = 0, packed = 0, orig_p = 0;
-            float vel_w = 1.f;
-            float4 pos = make_float4(0.f, 0.f, 0.f, 0.f);
-            int4 cell = make_int4(0, 0, 0, 0);
-            m3f F, C;
-            float v[3] = {0.f, 0.f, 0.f};
-            float plastic_j = 1.f;
-            // collider bits in effect for this pass (FIN): for a gather the
-            // bits the particle scattered with, for a standalone scatter the
-            // bits after the last completed substep
-            uint32_t bits_in = 0;
-            if (i < end) {
-                p = A.perm ? A.perm[i] : i;
-                pos = A.in.pos[p];
-                packed = __float_as_uint(pos.w);
-                if (CELL) cell = A.in.cell[p];
-                // issued with the position: neither waits for the material
-                // table, and the copy of orig does not wait behind this
-                // particle's stores
-                if (!LOAD_VC) vel_w = A.in.vel[p].w;
-                if (G2P) orig_p = A.in.orig[p];
-                if (packed & SV_TOMBSTONED) {
-                    if (G2P) {
-                        copy_particle(A.in, A.out, A.n, p, i, CELL);
-                        if (A.keys_out) A.keys_out[i] = SENTINEL_KEY;
-                    }
+    // One chunk of up to PT particles: thread t takes the particle at sorted
+    // position i (has: there is one), org is the tile's node origin.
+    auto chunk = [&](const uint32_t i, const bool has, const int count, const int *org) {
+        uint32_t rcell = REC_NONE;
+        float rmass = 0.f;
+        // this thread's particle; live across the closure network pass
+        bool work = false;
+        uint32_t p = 0, packed = 0, orig_p = 0;
+        float vel_w = 1.f;
+        float4 pos = make_float4(0.f, 0.f, 0.f, 0.f);
+        int4 cell = make_int4(0, 0, 0, 0);
+        m3f F, C;
+        float v[3] = {0.f, 0.f, 0.f};
+        float plastic_j = 1.f;
+        // collider bits in effect for this pass (FIN): for a gather the
+        // bits the particle scattered with, for a standalone scatter the
+        // bits after the last completed substep
+        uint32_t bits_in = 0;
+        if (has) {
+            p = A.perm ? A.perm[i] : i;
+            pos = A.in.pos[p];
+            packed = __float_as_uint(pos.w);
+            if (CELL) cell = A.in.cell[p];
+            // issued with the position: neither waits for the material
+            // table, and the copy of orig does not wait behind this
+            // particle's stores
+            if (!LOAD_VC) vel_w = A.in.vel[p].w;
+            if (G2P) orig_p = A.in.orig[p];
+            if (packed & SV_TOMBSTONED) {
+                if (G2P) {
+                    copy_particle(A.in, A.out, A.n, p, i, CELL);
+                    if (A.keys_out) A.keys_out[i] = SENTINEL_KEY;
+                }
+            } else {
+                work = true;
+                const uint32_t kind = A.mats[packed >> MATERIAL_SHIFT].kind;
+                if constexpr (FIN) bits_in = MODE == MODE_P2G ? A.in.cbits_done[p] : A.in.cbits[p];
+                if (MODE != MODE_G2P_ONLY) load_mat9(A.in.F, A.n, p, F);
+                if (LOAD_VC) {
+                    load_mat9(A.in.C, A.n, p, C);
+                    const float4 vel = A.in.vel[p];
+                    v[0] = vel.x, v[1] = vel.y, v[2] = vel.z;
+                    plastic_j = vel.w;
                 } else {
-                    work = true;
-                    const uint32_t kind = A.mats[packed >> MATERIAL_SHIFT].kind;
-                    if constexpr (FIN) bits_in = MODE == MODE_P2G ? A.in.cbits_done[p] : A.in.cbits[p];
-                    if (MODE != MODE_G2P_ONLY) load_mat9(A.in.F, A.n, p, F);
-                    if (LOAD_VC) {
-                        load_mat9(A.in.C, A.n, p, C);
-                        const float4 vel = A.in.vel[p];
-                        v[0] = vel.x, v[1] = vel.y, v[2] = vel.z;
-                        plastic_j = vel.w;
+                    plastic_j = (kind == KIND_SNOW || MODE == MODE_G2P_ONLY) ? vel_w : 1.f;
+                    // ---- G2P (collect_velocity.rs:40-72)
+                    int base[3];
+                    float fx[3];
+                    grid_position<CELL>(pos, cell, dx, base, fx);
+                    float w[3][3];
+                    bspline_weights(fx[0], w[0]);
+                    bspline_weights(fx[1], w[1]);
+                    bspline_weights(fx[2], w[2]);
+                    float d[3][3];
+#pragma unroll
+                    for (int a = 0; a < 3; ++a)
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) d[a][k] = ((float)k - fx[a]) * dx;
+                    const int tx = base[0] - org[0], ty = base[1] - org[1], tz = base[2] - org[2];
+                    const bool in_tile = tx >= 0 && ty >= 0 && tz >= 0 && tx <= TN - 3 && ty <= TN - 3 && tz <= TN - 3;
+                    if (FIN && bits_in != 0u) {
+                        gather_variant(A, base, bits_in, w, d, v, C);  // collect_velocity.rs:61-62 keyed by bits
+                    } else if (in_tile) {
+                        gather_tile(sh.gv, tx * 64 + ty * 8 + tz, w, d, v, C);
                     } else {
-                        plastic_j = (kind == KIND_SNOW || MODE == MODE_G2P_ONLY) ? vel_w : 1.f;
-                        // ---- G2P (collect_velocity.rs:40-72)
-                        int base[3];
-                        float fx[3];
-                        grid_position<CELL>(pos, cell, dx, base, fx);
-                        float w[3][3];
-                        bspline_weights(fx[0], w[0]);
-                        bspline_weights(fx[1], w[1]);
-                        bspline_weights(fx[2], w[2]);
-                        float d[3][3];
+                        if (!REDO) ++fallback;
+                        gather_global(A, base, w, d, v, C);
+                    }
+                    const float cscale = 4.f / dx / dx;
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) C.a[k] *= cscale;
+                }
+                if constexpr (MODE == MODE_G2P_ONLY) {
+                    // v and C back into the state, in place
+                    A.in.vel[p] = make_float4(v[0], v[1], v[2], plastic_j);
+                    store_mat9(A.in.C, A.n, p, C);
+                }
+                if constexpr (G2P_LIMITS_MODE) {
+                    // the limits of limit_time_step.rs:189-222 reduce over v and C
+                    if (g2p_limits) {
+                        red_v = fmaxf(red_v, sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
+#pragma unroll
+                        for (int k = 0; k < 9; ++k) red_c = fmaxf(red_c, fabsf(C.a[k]));
+                        red_live = true;
+                    }
+                }
+                if (G2P) {
+                    // ---- advance (advance_particles.rs:39-41): x += v dt, F += C F dt
+                    {
+                        const m3f CF = mat_mul(C, F);
+#pragma unroll
+                        for (int k = 0; k < 9; ++k) F.a[k] += CF.a[k] * dt_adv;
+                    }
+                    if (!CELL) {
+                        pos.x += v[0] * dt_adv, pos.y += v[1] * dt_adv, pos.z += v[2] * dt_adv;
+                    } else {
+                        float o[3] = {pos.x + v[0] * dt_adv / dx, pos.y + v[1] * dt_adv / dx, pos.z + v[2] * dt_adv / dx};
+                        int ci[3] = {cell.x, cell.y, cell.z};
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) {
+                            const float fl = floorf(o[k]);
+                            ci[k] += (int)fl;
+                            o[k] -= fl;
+                            if (o[k] >= 1.f) o[k] = 0.f, ci[k] += 1;
+                        }
+                        pos.x = o[0], pos.y = o[1], pos.z = o[2];
+                        cell = make_int4(ci[0], ci[1], ci[2], 0);
+                    }
+                }
+            }
+        }
+        // ---- learned closure (snow, sand): closed-form principal
+        // stretches, then one network pass for the whole chunk on the
+        // tensor cores (all threads take part)
+        int l_class = closure::L_PLAIN;  // after the network: L_PLAIN, L_ELASTIC or L_NET
+        float l_sig[3], l_V[9], l_y[tc::NOUT];
+        if constexpr (LEARNED) {
+            float x[tc::NIN];
+            if (work) {
+                const Material &lm = A.mats[packed >> MATERIAL_SHIFT];
+                if (closure::applies(lm.kind)) l_class = closure::learned_features(lm, F, shl.hull, l_sig, l_V, x);
+            }
+            const bool want = l_class == closure::L_NET;
+            if (!want)
+#pragma unroll
+                for (int k = 0; k < tc::NIN; ++k) x[k] = 0.f;
+            if (__syncthreads_or(want)) {
+                bool ok = false;
+                if (!shl.ctl.abort) {
+                    uint8_t *a0 = reinterpret_cast<uint8_t *>(sh.rec);
+                    ok = mlp::infer_tile(shl.ctl, ph, learned_img, a0, a0 + tc::NIN * PT * 2, x, l_y);
+                }
+                if (want && !ok) l_class = closure::L_PLAIN;
+            }
+        }
+        // ---- SVD (advance_particles.rs:42-44); in the plain fused pass the
+        // fp32 SVD only, a particle it cannot serve going to the fp64 pass
+        m3f U, V;
+        float S[3] = {1.f, 1.f, 1.f};
+        if constexpr (DEFER64) {
+            if (work && A.mats[packed >> MATERIAL_SHIFT].kind != KIND_NEO_HOOKEAN) {
+                const bool degenerate = svd3_fast_f32(F, U, S, V);
+                if (svd_needs_fp64(F, S, degenerate, A.L.svd_policy)) {
+                    A.defer_list[atomicAdd(&A.counters[C_DEFER], 1u)] = i;
+                    work = false;
+                }
+            }
+        }
+        if (work && (G2P || SCATTER)) {
+            const Material mat = A.mats[packed >> MATERIAL_SHIFT];
+            const uint32_t kind = mat.kind;
+            // ---- plasticity (advance_particles.rs:45-86), energy
+            float energy = 0.f;
+            m3f tau_l{};  // learned path: Kirchhoff stress P F^T
+            bool use_l = false;
+            if constexpr (LEARNED) {
+                if (l_class != closure::L_PLAIN) {
+                    m3f Fn;
+                    float e_l, jp_l, J_l;
+                    if (closure::learned_apply(mat, F, l_sig, l_V, l_class == closure::L_NET ? l_y : nullptr, shl.hull,
+                                               plastic_j, Fn, tau_l, e_l, jp_l, J_l)) {
+                        use_l = true;
+                        F = Fn;
+                        plastic_j = jp_l;
+                        energy = e_l;
+                    }
+                }
+                if (closure::applies(kind)) {
+                    if (use_l) ++n_learned;
+                    else ++n_closure_fb;
+                }
+            }
+            if (!use_l) {
+                const bool need_svd = G2P ? kind != KIND_NEO_HOOKEAN : (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW);
+                if (need_svd && !DEFER64) particle_svd(F, U, S, V, A.L.svd_policy | (REDO ? SVD_ALWAYS_FP64 : 0u), fp64_count);
+                if (G2P) {
+                    if (kind == KIND_SAND) {
+                        // Drucker-Prager return map in Hencky strain (advance_particles.rs:48-71)
+                        const float e[3] = {logf(S[0]), logf(S[1]), logf(S[2])};
+                        const float e_tr = e[0] + e[1] + e[2];
+                        const float eh[3] = {e[0] - e_tr / 3.f, e[1] - e_tr / 3.f, e[2] - e_tr / 3.f};
+                        const float ehn = sqrtf(eh[0] * eh[0] + eh[1] * eh[1] + eh[2] * eh[2]);
+                        if (e_tr < 0.f && ehn > 0.f) {
+                            if (!(mat.mu > 0.f)) {
+                                // the reference asserts mu > 0 here (:57)
+                                atomicOr(&A.counters[C_STATUS], ST_SAND_MU), sh.raised = 1;
+                            } else {
+                                const float dg = ehn + (3.f * mat.lambda + 2.f * mat.mu) / 2.f / mat.mu * e_tr * mat.alpha;
+                                if (dg > 0.f) {
+#pragma unroll
+                                    for (int k = 0; k < 3; ++k) S[k] = expf(e[k] - dg / ehn * eh[k]);
+                                    F = recompose(U, S, V);
+                                }
+                            }
+                        } else {
+                            // expansion: U V^T whatever mu is
+                            S[0] = S[1] = S[2] = 1.f;
+                            F = mat_mul_bt(U, V);
+                        }
+                    } else if (kind == KIND_FLUID) {
+                        // advance_particles.rs:77-85: singular values -> geometric mean
+                        const float g = powf(S[0] * S[1] * S[2], 1.f / 3.f);
+                        S[0] = S[1] = S[2] = g;
+                        F = recompose(U, S, V);
+                    } else if (kind == KIND_SNOW) {
+                        // addition: Stomakhin et al. 2013 clamp + hardening state
+                        float s[3];
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) s[k] = fminf(fmaxf(S[k], 1.f - mat.theta_c), 1.f + mat.theta_s);
+                        plastic_j = plastic_j * (S[0] * S[1] * S[2]) / (s[0] * s[1] * s[2]);
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) S[k] = s[k];
+                        F = recompose(U, S, V);
+                    }
+                }
+            }
+            const float J = det3(F);
+            const float hard = kind == KIND_SNOW ? expf(mat.xi * (1.f - plastic_j)) : 1.f;
+            bool alive = true;
+            if (G2P) {
+                if (use_l) {
+                    // energy of the learned projected stretches (J > 0 by construction)
+                } else if (kind == KIND_FLUID) {
+                    // util/src/elastic.rs:546-553
+                    const float K = mat.bulk_modulus, gm = (float)mat.exponent;
+                    const float at_rest = K * (1.f - 1.f / (1.f - gm));
+                    energy = K * (J - powi_f(J, 1 - mat.exponent) / (1.f - gm)) - at_rest;
+                } else if (!(J > 0.f)) {
+                    // try_elastic_energy_neo_hookean: J <= 0 -> FAILED (advance_particles.rs:73-74)
+                    packed |= SV_FAILED;
+                    atomicOr(&A.counters[C_STATUS], ST_INVERTED), sh.raised = 1;
+                } else if (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW) {
+                    // mu |F - R|^2 + lambda/2 (J - 1)^2 = mu sum (s - 1)^2 + ...
+                    const float d2 = (S[0] - 1.f) * (S[0] - 1.f) + (S[1] - 1.f) * (S[1] - 1.f) + (S[2] - 1.f) * (S[2] - 1.f);
+                    energy = mat.mu * hard * d2 + mat.lambda * hard / 2.f * (J - 1.f) * (J - 1.f);
+                } else {
+                    // util/src/elastic.rs:233-241
+                    float I2 = 0.f;
+#pragma unroll
+                    for (int k = 0; k < 9; ++k) I2 += F.a[k] * F.a[k];
+                    const float lj = logf(J);
+                    energy = mat.mu / 2.f * (I2 - 3.f) - mat.mu * lj + mat.lambda / 2.f * lj * lj;
+                }
+                // cull (cull_particles.rs:17-41): strict domain bounds
+                bool inside;
+                if (!CELL) {
+                    inside = pos.x > A.L.domain_min[0] && pos.x < A.L.domain_max[0] && pos.y > A.L.domain_min[1] &&
+                             pos.y < A.L.domain_max[1] && pos.z > A.L.domain_min[2] && pos.z < A.L.domain_max[2];
+                } else {
+                    // scene-local cell coordinates against the scene's domain
+                    const SceneInfo &sc = A.scenes[mat.scene];
+                    const double q[3] = {(double)(cell.x - sc.off[0]) + pos.x, (double)(cell.y - sc.off[1]) + pos.y,
+                                         (double)(cell.z - sc.off[2]) + pos.z};
+                    inside = q[0] > sc.dmin[0] && q[0] < sc.dmax[0] && q[1] > sc.dmin[1] && q[1] < sc.dmax[1] &&
+                             q[2] > sc.dmin[2] && q[2] < sc.dmax[2];
+                }
+                if (!inside) packed |= SV_TOMBSTONED;
+                alive = !(packed & (SV_TOMBSTONED | SV_FAILED));
+                if constexpr (FORCE_LIMITS_MODE) {
+                    // LimitTimeStepBeforeForce of the next substep
+                    // (limit_time_step.rs:25-178) over the state just
+                    // written: the singular values come from this pass's
+                    // SVD (after the plastic projection, which sets them);
+                    // Neo-Hookean solids took none and take one here.
+                    if (A.adt && !(packed & SV_TOMBSTONED)) {
+                        float s[3] = {S[0], S[1], S[2]};
+                        if (kind == KIND_NEO_HOOKEAN) {
+                            uint32_t none = 0;
+                            particle_svd(F, U, s, V, 0, none);
+                        }
+                        if (s[0] < s[1]) { const float t = s[0]; s[0] = s[1], s[1] = t; }
+                        if (s[1] < s[2]) { const float t = s[1]; s[1] = s[2], s[2] = t; }
+                        if (s[0] < s[1]) { const float t = s[0]; s[0] = s[1], s[1] = t; }
+                        const bool fluid = kind == KIND_FLUID;
+                        const float a = adaptive::sound_limit<float>(fluid, mat.mu, mat.lambda, mat.bulk_modulus,
+                                                                     mat.exponent, mat.mass, mat.initial_volume, s, dx);
+                        const float b = fluid ? adaptive::isolated_limit<float>(true, mat.mu, mat.lambda, mat.bulk_modulus,
+                                                                                mat.exponent, mat.mass, mat.initial_volume, J, dx)
+                                              : mat.iso_limit;
+                        if (a > 0.f && a < adaptive::NONE) lim_sound = fminf(lim_sound, a);
+                        if (b > 0.f && b < adaptive::NONE) lim_iso = fminf(lim_iso, b);
+                    }
+                }
+                // write the advanced state in sorted order
+                pos.w = __uint_as_float(packed);
+                A.out.pos[i] = pos;
+                if (CELL) A.out.cell[i] = cell;
+                A.out.vel[i] = make_float4(v[0], v[1], v[2], plastic_j);
+                store_mat9(A.out.C, A.n, i, C);
+                store_mat9(A.out.F, A.n, i, F);
+                A.out.energy[i] = energy;
+                A.out.orig[i] = orig_p;
+                if constexpr (FIN) {
+                    // the bits of the completed substep; the next
+                    // scatter's Collide (below) replaces the ones in effect
+                    A.out.cbits_done[i] = bits_in;
+                    A.out.cbits[i] = bits_in;
+                }
+            }
+            int nbase[3];
+            float nfx[3];
+            grid_position<CELL>(pos, cell, dx, nbase, nfx);
+            if (G2P && A.keys_out) {
+                uint32_t key = SENTINEL_KEY;
+                if (!(packed & SV_TOMBSTONED)) {
+                    bool ok;
+                    key = cell_key(nbase[0], nbase[1], nbase[2], A.L, ok);
+                    if (!ok) atomicOr(&A.counters[C_STATUS], ST_OUT_OF_GRID), sh.raised = 1;
+                }
+                A.keys_out[i] = key;
+            }
+            if (SCATTER && alive) {
+                // ---- scatter record of the next substep: Collide
+                // (collide.rs:21-206), external force (external_force.rs:17-50),
+                // then the momentum of scatter_momentum.rs:38-90
+                uint32_t bits_new = 0u;
+                if constexpr (FIN) {
+                    const float P[3] = {CELL ? ((float)cell.x + pos.x) * dx : pos.x,
+                                        CELL ? ((float)cell.y + pos.y) * dx : pos.y,
+                                        CELL ? ((float)cell.z + pos.z) * dx : pos.z};
+                    bits_new = bits_in;
+                    if (A.fa.nt) col::collide_particle(A.fa, P, v, bits_new, dt_force);
+                    else bits_new = 0u;  // nothing to check (collide.rs:53-56)
+                    const uint32_t o = A.in.orig[p];
+                    if (A.fa.goal_both && A.fa.goal_both[o]) {
+                        // both frames give a goal: reach it in one step
+                        const float fb = A.fa.factor[0], fa_ = 1.f - fb;
 #pragma unroll
                         for (int a = 0; a < 3; ++a)
-#pragma unroll
-                            for (int k = 0; k < 3; ++k) d[a][k] = ((float)k - fx[a]) * dx;
-                        const int tx = base[0] - org[0], ty = base[1] - org[1], tz = base[2] - org[2];
-                        const bool in_tile = tx >= 0 && ty >= 0 && tz >= 0 && tx <= TN - 3 && ty <= TN - 3 && tz <= TN - 3;
-                        if (FIN && bits_in != 0u) {
-                            gather_variant(A, base, bits_in, w, d, v, C);  // collect_velocity.rs:61-62 keyed by bits
-                        } else if (in_tile) {
-                            gather_tile(sh.gv, tx * 64 + ty * 8 + tz, w, d, v, C);
-                        } else {
-                            ++fallback;
-                            gather_global(A, base, w, d, v, C);
-                        }
-                        const float cscale = 4.f / dx / dx;
-#pragma unroll
-                        for (int k = 0; k < 9; ++k) C.a[k] *= cscale;
-                    }
-                    if constexpr (MODE == MODE_G2P_ONLY) {
-                        // v and C back into the state, in place
-                        A.in.vel[p] = make_float4(v[0], v[1], v[2], plastic_j);
-                        store_mat9(A.in.C, A.n, p, C);
-                    }
-                    if constexpr (G2P_LIMITS_MODE) {
-                        // the limits of limit_time_step.rs:189-222 reduce over v and C
-                        if (g2p_limits) {
-                            red_v = fmaxf(red_v, sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]));
-#pragma unroll
-                            for (int k = 0; k < 9; ++k) red_c = fmaxf(red_c, fabsf(C.a[k]));
-                            red_live = true;
-                        }
-                    }
-                    if (G2P) {
-                        // ---- advance (advance_particles.rs:39-41): x += v dt, F += C F dt
-                        {
-                            const m3f CF = mat_mul(C, F);
-#pragma unroll
-                            for (int k = 0; k < 9; ++k) F.a[k] += CF.a[k] * dt_adv;
-                        }
-                        if (!CELL) {
-                            pos.x += v[0] * dt_adv, pos.y += v[1] * dt_adv, pos.z += v[2] * dt_adv;
-                        } else {
-                            float o[3] = {pos.x + v[0] * dt_adv / dx, pos.y + v[1] * dt_adv / dx, pos.z + v[2] * dt_adv / dx};
-                            int ci[3] = {cell.x, cell.y, cell.z};
-#pragma unroll
-                            for (int k = 0; k < 3; ++k) {
-                                const float fl = floorf(o[k]);
-                                ci[k] += (int)fl;
-                                o[k] -= fl;
-                                if (o[k] >= 1.f) o[k] = 0.f, ci[k] += 1;
-                            }
-                            pos.x = o[0], pos.y = o[1], pos.z = o[2];
-                            cell = make_int4(ci[0], ci[1], ci[2], 0);
-                        }
-                    }
-                }
-            }
-            // ---- learned closure (snow, sand): closed-form principal
-            // stretches, then one network pass for the whole chunk on the
-            // tensor cores (all threads take part)
-            int l_class = closure::L_PLAIN;  // after the network: L_PLAIN, L_ELASTIC or L_NET
-            float l_sig[3], l_V[9], l_y[tc::NOUT];
-            if constexpr (LEARNED) {
-                float x[tc::NIN];
-                if (work) {
-                    const Material &lm = A.mats[packed >> MATERIAL_SHIFT];
-                    if (closure::applies(lm.kind)) l_class = closure::learned_features(lm, F, shl.hull, l_sig, l_V, x);
-                }
-                const bool want = l_class == closure::L_NET;
-                if (!want)
-#pragma unroll
-                    for (int k = 0; k < tc::NIN; ++k) x[k] = 0.f;
-                if (__syncthreads_or(want)) {
-                    bool ok = false;
-                    if (!shl.ctl.abort) {
-                        uint8_t *a0 = reinterpret_cast<uint8_t *>(sh.rec);
-                        ok = mlp::infer_tile(shl.ctl, ph, learned_img, a0, a0 + tc::NIN * PT * 2, x, l_y);
-                    }
-                    if (want && !ok) l_class = closure::L_PLAIN;
-                }
-            }
-            if (work && (G2P || SCATTER)) {
-                const Material mat = A.mats[packed >> MATERIAL_SHIFT];
-                const uint32_t kind = mat.kind;
-                // ---- SVD, plasticity (advance_particles.rs:42-86), energy
-                m3f U, V;
-                float S[3] = {1.f, 1.f, 1.f};
-                float energy = 0.f;
-                m3f tau_l{};  // learned path: Kirchhoff stress P F^T
-                bool use_l = false;
-                if constexpr (LEARNED) {
-                    if (l_class != closure::L_PLAIN) {
-                        m3f Fn;
-                        float e_l, jp_l, J_l;
-                        if (closure::learned_apply(mat, F, l_sig, l_V, l_class == closure::L_NET ? l_y : nullptr, shl.hull,
-                                                   plastic_j, Fn, tau_l, e_l, jp_l, J_l)) {
-                            use_l = true;
-                            F = Fn;
-                            plastic_j = jp_l;
-                            energy = e_l;
-                        }
-                    }
-                    if (closure::applies(kind)) {
-                        if (use_l) ++n_learned;
-                        else ++n_closure_fb;
-                    }
-                }
-                if (!use_l) {
-                    const bool need_svd = G2P ? kind != KIND_NEO_HOOKEAN : (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW);
-                    if (need_svd) particle_svd(F, U, S, V, A.L.svd_policy, fp64_count);
-                    if (G2P) {
-                        if (kind == KIND_SAND) {
-                            // Drucker-Prager return map in Hencky strain (advance_particles.rs:48-71)
-                            const float e[3] = {logf(S[0]), logf(S[1]), logf(S[2])};
-                            const float e_tr = e[0] + e[1] + e[2];
-                            const float eh[3] = {e[0] - e_tr / 3.f, e[1] - e_tr / 3.f, e[2] - e_tr / 3.f};
-                            const float ehn = sqrtf(eh[0] * eh[0] + eh[1] * eh[1] + eh[2] * eh[2]);
-                            if (e_tr < 0.f && ehn > 0.f) {
-                                if (!(mat.mu > 0.f)) {
-                                    // the reference asserts mu > 0 here (:57)
-                                    atomicOr(&A.counters[C_STATUS], ST_SAND_MU), sh.raised = 1;
-                                } else {
-                                    const float dg = ehn + (3.f * mat.lambda + 2.f * mat.mu) / 2.f / mat.mu * e_tr * mat.alpha;
-                                    if (dg > 0.f) {
-#pragma unroll
-                                        for (int k = 0; k < 3; ++k) S[k] = expf(e[k] - dg / ehn * eh[k]);
-                                        F = recompose(U, S, V);
-                                    }
-                                }
-                            } else {
-                                // expansion: U V^T whatever mu is
-                                S[0] = S[1] = S[2] = 1.f;
-                                F = mat_mul_bt(U, V);
-                            }
-                        } else if (kind == KIND_FLUID) {
-                            // advance_particles.rs:77-85: singular values -> geometric mean
-                            const float g = powf(S[0] * S[1] * S[2], 1.f / 3.f);
-                            S[0] = S[1] = S[2] = g;
-                            F = recompose(U, S, V);
-                        } else if (kind == KIND_SNOW) {
-                            // addition: Stomakhin et al. 2013 clamp + hardening state
-                            float s[3];
-#pragma unroll
-                            for (int k = 0; k < 3; ++k) s[k] = fminf(fmaxf(S[k], 1.f - mat.theta_c), 1.f + mat.theta_s);
-                            plastic_j = plastic_j * (S[0] * S[1] * S[2]) / (s[0] * s[1] * s[2]);
-#pragma unroll
-                            for (int k = 0; k < 3; ++k) S[k] = s[k];
-                            F = recompose(U, S, V);
-                        }
-                    }
-                }
-                const float J = det3(F);
-                const float hard = kind == KIND_SNOW ? expf(mat.xi * (1.f - plastic_j)) : 1.f;
-                bool alive = true;
-                if (G2P) {
-                    if (use_l) {
-                        // energy of the learned projected stretches (J > 0 by construction)
-                    } else if (kind == KIND_FLUID) {
-                        // util/src/elastic.rs:546-553
-                        const float K = mat.bulk_modulus, gm = (float)mat.exponent;
-                        const float at_rest = K * (1.f - 1.f / (1.f - gm));
-                        energy = K * (J - powi_f(J, 1 - mat.exponent) / (1.f - gm)) - at_rest;
-                    } else if (!(J > 0.f)) {
-                        // try_elastic_energy_neo_hookean: J <= 0 -> FAILED (advance_particles.rs:73-74)
-                        packed |= SV_FAILED;
-                        atomicOr(&A.counters[C_STATUS], ST_INVERTED), sh.raised = 1;
-                    } else if (kind == KIND_FIXED_COROTATED || kind == KIND_SNOW) {
-                        // mu |F - R|^2 + lambda/2 (J - 1)^2 = mu sum (s - 1)^2 + ...
-                        const float d2 = (S[0] - 1.f) * (S[0] - 1.f) + (S[1] - 1.f) * (S[1] - 1.f) + (S[2] - 1.f) * (S[2] - 1.f);
-                        energy = mat.mu * hard * d2 + mat.lambda * hard / 2.f * (J - 1.f) * (J - 1.f);
+                            v[a] = (fa_ * A.fa.goal_a[3 * o + a] + fb * A.fa.goal_b[3 * o + a] - P[a]) / dt_force;
                     } else {
-                        // util/src/elastic.rs:233-241
-                        float I2 = 0.f;
 #pragma unroll
-                        for (int k = 0; k < 9; ++k) I2 += F.a[k] * F.a[k];
-                        const float lj = logf(J);
-                        energy = mat.mu / 2.f * (I2 - 3.f) - mat.mu * lj + mat.lambda / 2.f * lj * lj;
+                        for (int a = 0; a < 3; ++a) v[a] += dt_force * A.fa.gravity[a];
                     }
-                    // cull (cull_particles.rs:17-41): strict domain bounds
-                    bool inside;
-                    if (!CELL) {
-                        inside = pos.x > A.L.domain_min[0] && pos.x < A.L.domain_max[0] && pos.y > A.L.domain_min[1] &&
-                                 pos.y < A.L.domain_max[1] && pos.z > A.L.domain_min[2] && pos.z < A.L.domain_max[2];
-                    } else {
-                        // scene-local cell coordinates against the scene's domain
-                        const SceneInfo &sc = A.scenes[mat.scene];
-                        const double q[3] = {(double)(cell.x - sc.off[0]) + pos.x, (double)(cell.y - sc.off[1]) + pos.y,
-                                             (double)(cell.z - sc.off[2]) + pos.z};
-                        inside = q[0] > sc.dmin[0] && q[0] < sc.dmax[0] && q[1] > sc.dmin[1] && q[1] < sc.dmax[1] &&
-                                 q[2] > sc.dmin[2] && q[2] < sc.dmax[2];
-                    }
-                    if (!inside) packed |= SV_TOMBSTONED;
-                    alive = !(packed & (SV_TOMBSTONED | SV_FAILED));
-                    if constexpr (FORCE_LIMITS_MODE) {
-                        // LimitTimeStepBeforeForce of the next substep
-                        // (limit_time_step.rs:25-178) over the state just
-                        // written: the singular values come from this pass's
-                        // SVD (after the plastic projection, which sets them);
-                        // Neo-Hookean solids took none and take one here.
-                        if (A.adt && !(packed & SV_TOMBSTONED)) {
-                            float s[3] = {S[0], S[1], S[2]};
-                            if (kind == KIND_NEO_HOOKEAN) {
-                                uint32_t none = 0;
-                                particle_svd(F, U, s, V, 0, none);
-                            }
-                            if (s[0] < s[1]) { const float t = s[0]; s[0] = s[1], s[1] = t; }
-                            if (s[1] < s[2]) { const float t = s[1]; s[1] = s[2], s[2] = t; }
-                            if (s[0] < s[1]) { const float t = s[0]; s[0] = s[1], s[1] = t; }
-                            const bool fluid = kind == KIND_FLUID;
-                            const float a = adaptive::sound_limit<float>(fluid, mat.mu, mat.lambda, mat.bulk_modulus,
-                                                                         mat.exponent, mat.mass, mat.initial_volume, s, dx);
-                            const float b = fluid ? adaptive::isolated_limit<float>(true, mat.mu, mat.lambda, mat.bulk_modulus,
-                                                                                    mat.exponent, mat.mass, mat.initial_volume, J, dx)
-                                                  : mat.iso_limit;
-                            if (a > 0.f && a < adaptive::NONE) lim_sound = fminf(lim_sound, a);
-                            if (b > 0.f && b < adaptive::NONE) lim_iso = fminf(lim_iso, b);
-                        }
-                    }
-                    // write the advanced state in sorted order
-                    pos.w = __uint_as_float(packed);
-                    A.out.pos[i] = pos;
-                    if (CELL) A.out.cell[i] = cell;
-                    A.out.vel[i] = make_float4(v[0], v[1], v[2], plastic_j);
-                    store_mat9(A.out.C, A.n, i, C);
-                    store_mat9(A.out.F, A.n, i, F);
-                    A.out.energy[i] = energy;
-                    A.out.orig[i] = orig_p;
-                    if constexpr (FIN) {
-                        // the bits of the completed substep; the next
-                        // scatter's Collide (below) replaces the ones in effect
-                        A.out.cbits_done[i] = bits_in;
-                        A.out.cbits[i] = bits_in;
-                    }
+                    if (G2P) A.out.cbits[i] = bits_new;
+                    else A.in.cbits[p] = bits_new;
+                } else {
+                    v[0] += dt_force * A.gravity.x, v[1] += dt_force * A.gravity.y, v[2] += dt_force * A.gravity.z;
                 }
-                int nbase[3];
-                float nfx[3];
-                grid_position<CELL>(pos, cell, dx, nbase, nfx);
-                if (G2P && A.keys_out) {
-                    uint32_t key = SENTINEL_KEY;
-                    if (!(packed & SV_TOMBSTONED)) {
-                        bool ok;
-                        key = cell_key(nbase[0], nbase[1], nbase[2], A.L, ok);
-                        if (!ok) atomicOr(&A.counters[C_STATUS], ST_OUT_OF_GRID), sh.raised = 1;
-                    }
-                    A.keys_out[i] = key;
+                const m3f PFt = use_l ? tau_l : stress_times_ft(mat, F, J, U, S, hard);
+                make_record(mat, C, PFt, J, v, nfx, dx, dt_scatter, sh.rec[threadIdx.x]);
+                rmass = mat.mass;
+                int4 gb;
+                rcell = tile_cell(nbase, org, gb);
+                if (FIN && bits_new != 0u) {
+                    rcell = REC_VARIANT;
+                    gb = make_int4(nbase[0], nbase[1], nbase[2], (int)bits_new);
                 }
-                if (SCATTER && alive) {
-                    // ---- scatter record of the next substep: Collide
-                    // (collide.rs:21-206), external force (external_force.rs:17-50),
-                    // then the momentum of scatter_momentum.rs:38-90
-                    uint32_t bits_new = 0u;
-                    if constexpr (FIN) {
-                        const float P[3] = {CELL ? ((float)cell.x + pos.x) * dx : pos.x,
-                                            CELL ? ((float)cell.y + pos.y) * dx : pos.y,
-                                            CELL ? ((float)cell.z + pos.z) * dx : pos.z};
-                        bits_new = bits_in;
-                        if (A.fa.nt) col::collide_particle(A.fa, P, v, bits_new, dt_force);
-                        else bits_new = 0u;  // nothing to check (collide.rs:53-56)
-                        const uint32_t o = A.in.orig[p];
-                        if (A.fa.goal_both && A.fa.goal_both[o]) {
-                            // both frames give a goal: reach it in one step
-                            const float fb = A.fa.factor[0], fa_ = 1.f - fb;
-#pragma unroll
-                            for (int a = 0; a < 3; ++a)
-                                v[a] = (fa_ * A.fa.goal_a[3 * o + a] + fb * A.fa.goal_b[3 * o + a] - P[a]) / dt_force;
-                        } else {
-#pragma unroll
-                            for (int a = 0; a < 3; ++a) v[a] += dt_force * A.fa.gravity[a];
-                        }
-                        if (G2P) A.out.cbits[i] = bits_new;
-                        else A.in.cbits[p] = bits_new;
-                    } else {
-                        v[0] += dt_force * A.gravity.x, v[1] += dt_force * A.gravity.y, v[2] += dt_force * A.gravity.z;
-                    }
-                    const m3f PFt = use_l ? tau_l : stress_times_ft(mat, F, J, U, S, hard);
-                    make_record(mat, C, PFt, J, v, nfx, dx, dt_scatter, sh.rec[threadIdx.x]);
-                    rmass = mat.mass;
-                    int4 gb;
-                    rcell = tile_cell(nbase, org, gb);
-                    if (FIN && bits_new != 0u) {
-                        rcell = REC_VARIANT;
-                        gb = make_int4(nbase[0], nbase[1], nbase[2], (int)bits_new);
-                    }
-                    if (rcell == REC_GLOBAL || rcell == REC_VARIANT) sh.gbase[threadIdx.x] = gb;
-                }
-            }
-            if (SCATTER) {
-                sh.meta[threadIdx.x] = make_float2(__uint_as_float(rcell), rmass);
-                // Warp w replays only its own threads' records, so warp
-                // barriers would do here; measured 1-2 % slower than keeping
-                // the CTA's warps in step, so the CTA barriers stay.
-                __syncthreads();
-                scatter_records(sh, count, A);
-                __syncthreads();
+                if (rcell == REC_GLOBAL || rcell == REC_VARIANT) sh.gbase[threadIdx.x] = gb;
             }
         }
-        __syncthreads();
+        if (SCATTER) {
+            sh.meta[threadIdx.x] = make_float2(__uint_as_float(rcell), rmass);
+            // Warp w replays only its own threads' records, so warp
+            // barriers would do here; measured 1-2 % slower than keeping
+            // the CTA's warps in step, so the CTA barriers stay.
+            __syncthreads();
+            scatter_records(sh, count, A);
+            __syncthreads();
+        }
+    };
+    if constexpr (REDO) {
+        // one pass per CTA over its share of the list, with no tile: every
+        // listed particle takes the global gather and scatter
+        const uint32_t end = A.counters[C_DEFER];
+        const int org[3] = {-(1 << 30), -(1 << 30), -(1 << 30)};
+        for (uint32_t c0 = blockIdx.x * PT; c0 < end; c0 += gridDim.x * PT) {
+            const uint32_t slot = c0 + threadIdx.x;
+            chunk(slot < end ? A.defer_list[slot] : 0u, slot < end, (int)min((uint32_t)PT, end - c0), org);
+        }
+    } else {
+        for (uint32_t seg = blockIdx.x; seg < nseg; seg += gridDim.x) {
+            const uint32_t b = A.seg_block[seg];
+            const uint32_t start = A.seg_start[seg], end = A.seg_start[seg + 1];
+            int bx, by, bz;
+            block_coords(b, A.L, bx, by, bz);
+            const int org[3] = {A.L.origin[0] + 4 * bx - 1, A.L.origin[1] + 4 * by - 1, A.L.origin[2] + 4 * bz - 1};
+            if (threadIdx.x < 27) {
+                const uint32_t nbk = neighbour27(b, threadIdx.x, A.L);
+                sh.slot_next[threadIdx.x] = A.map_next[nbk];
+                if (GATHER) sh.slot_cur[threadIdx.x] = A.map_cur[nbk];
+            }
+            __syncthreads();
+            if (SCATTER)
+                for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
+                    const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
+                    const int32_t slot = sh.slot_next[tile_neighbour(tx, ty, tz)];
+                    sh.gidx[tx * PX + ty * PY + tz] = slot >= 0 ? (uint32_t)slot * 64u + (uint32_t)tile_local(tx, ty, tz) : NO_NODE;
+                }
+            if (GATHER) {
+                for (int t = threadIdx.x; t < TILE_NODES; t += PT) {
+                    const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
+                    const int32_t slot = sh.slot_cur[tile_neighbour(tx, ty, tz)];
+                    sh.gv[t] = slot >= 0 ? A.grid_cur[(uint64_t)slot * 64 + tile_local(tx, ty, tz)] : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+                __syncthreads();
+            }
+            for (uint32_t c0 = start; c0 < end; c0 += PT)
+                chunk(c0 + threadIdx.x, c0 + threadIdx.x < end, (int)min((uint32_t)PT, end - c0), org);
+            __syncthreads();
+        }
     }
     if (G2P_LIMITS_MODE && g2p_limits) {
 #pragma unroll
@@ -1631,6 +1668,7 @@ StepArgs make_args(sv_handle *h, float dt, float3 g) {
     A.self_latch = false;
     A.adt_pass = 0;
     A.keys_out = h->keys;
+    A.defer_list = h->defer_list;
     A.closure_img = nullptr;
     A.closure_hull = nullptr;
     A.adt = nullptr;
@@ -2034,6 +2072,16 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 g, bool write_keys, bool
         A.closure_img = h->cl_img;
         A.closure_hull = reinterpret_cast<const closure::Hull *>(h->cl_hull);
         launch_particles<MODE_G2P2G_LEARNED>(h, A);
+    } else if (!h->fin_active) {
+        // the fused pass without fp64 code, then its fp64 pass, which
+        // latches the stop bits for both (see k_particles)
+        StepArgs M = A;
+        M.self_latch = false;
+        launch_particles<MODE_G2P2G>(h, M);
+        if (h->layout.position_form) k_particles<true, MODE_G2P2G, false, true><<<sm_count(), PT, 0, h->stream>>>(A);
+        else k_particles<false, MODE_G2P2G, false, true><<<sm_count(), PT, 0, h->stream>>>(A);
+        h->stop_latched = A.self_latch;
+        h->launches += 1;
     } else {
         launch_particles<MODE_G2P2G>(h, A);
     }
