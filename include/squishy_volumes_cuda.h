@@ -271,6 +271,15 @@ typedef struct sv_stats {
      * calls take them on every substep. */
     double grid_mass;
     double grid_momentum[3];
+    /* Device time of the plain fused particle pass (gather, advance,
+     * scatter; its fp64 pass included), summed over its launches since
+     * sv_create, and the number of those launches: from the start of the
+     * pass's first CTA to the end of its last, read from the GPU's global
+     * nanosecond timer by the kernels themselves, so CUDA-graph replays are
+     * timed too.  Frame-input, learned-closure and adaptive passes are not
+     * counted. */
+    uint64_t pass_ns;
+    uint64_t pass_count;
 } sv_stats;
 
 /* Adaptive time steps: CpuState::produce_next_state with

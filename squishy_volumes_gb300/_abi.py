@@ -102,6 +102,8 @@ class SvStats(ct.Structure):
         ("adaptive_split", ct.c_uint64),
         ("grid_mass", ct.c_double),
         ("grid_momentum", ct.c_double * 3),
+        ("pass_ns", ct.c_uint64),
+        ("pass_count", ct.c_uint64),
     ]
 
 

@@ -835,6 +835,7 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     arena.add(&h->keys, n), arena.add(&h->sorted_keys, n), arena.add(&h->perm, n), arena.add(&h->inv, n);
     arena.add(&h->defer_list, n);
     arena.add(&h->grid_sums, 8);
+    arena.add(&h->pass_timer, 3);
     arena.add(&h->seg_start, n + 1), arena.add(&h->seg_block, n), arena.add(&h->counters, C_COUNT);
     arena.add((char **)&h->sort_temp, h->sort_temp_bytes), arena.add(&h->tile_counts, tiles);
     arena.add((char **)&h->scan_temp, scan_temp_bytes(tiles));
@@ -858,7 +859,8 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
     if ((e = cudaMemcpy(h->materials, mats.data(), mats.size() * sizeof(Material), cudaMemcpyHostToDevice)) ||
         (e = cudaMemcpy(h->scenes, scenes.data(), n_scenes * sizeof(SceneInfo), cudaMemcpyHostToDevice)) ||
         (e = cudaMemset(h->blockmap[0], 0xFF, total * 4)) || (e = cudaMemset(h->blockmap[1], 0xFF, total * 4)) ||
-        (e = cudaMemset(h->counters, 0, C_COUNT * 4)) || (e = cudaMemset(h->grid_sums, 0, 8 * sizeof(double))))
+        (e = cudaMemset(h->counters, 0, C_COUNT * 4)) || (e = cudaMemset(h->grid_sums, 0, 8 * sizeof(double))) ||
+        (e = cudaMemset(h->pass_timer, 0, 3 * sizeof(uint64_t))))
         return cuda_fail(e, "upload");
     h->direct_host = c.host_transfer == 0 && pageable_access();
     if (h->direct_host) {
@@ -1447,6 +1449,10 @@ int sv_get_stats(sv_handle *h, sv_stats *out) {
     const int gs = h->vel_side >= 0 ? h->vel_side : h->gcur;
     out->grid_mass = sums[4 * gs];
     for (int a = 0; a < 3; ++a) out->grid_momentum[a] = sums[4 * gs + 1 + a];
+    uint64_t timer[3] = {0, 0, 0};
+    SV_CUDA(cudaMemcpy(timer, h->pass_timer, sizeof(timer), cudaMemcpyDeviceToHost));
+    out->pass_ns = timer[1];
+    out->pass_count = timer[2];
     return 0;
 }
 

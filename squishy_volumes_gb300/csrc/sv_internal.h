@@ -176,6 +176,7 @@ struct sv_handle {
     // device [2][4] fp64 sums (mass, px, py, pz) of grid[0] and grid[1] in
     // momentum form, taken by the grid update; zeroed where a grid is cleared
     double *grid_sums = nullptr;
+    uint64_t *pass_timer = nullptr;     // device [3]: start of the current fused pass, ns summed, passes (globaltimer)
     uint32_t *counters = nullptr;       // device [C_COUNT]
     uint32_t *host_counters = nullptr;  // pinned mirror
 

@@ -98,6 +98,7 @@ struct StepArgs {
     float4 *grid_next;
     uint32_t *keys_out;  // nullptr: keys not needed after this substep
     uint32_t *defer_list;  // sorted positions left by the fused pass for its fp64 pass ([C_DEFER] of them)
+    uint64_t *pass_timer;  // plain fused pass only: [start ns, ns summed, passes] (else nullptr)
     const uint8_t *closure_img;          // packed network weights (learned mode)
     const closure::Hull *closure_hull;   // training hull of the features (learned mode)
     adaptive::State *adt;                // adaptive time steps: device dt and reductions (else nullptr)
@@ -117,6 +118,12 @@ struct StepArgs {
     float dt;
     float3 gravity;
 };
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ uint32_t stopped(const uint32_t *counters) {
     return *(volatile const uint32_t *)&counters[C_STOP];
@@ -420,13 +427,38 @@ __global__ void __launch_bounds__(ELEM_THREADS)
 }
 
 // ------------------------------------------------------------------ grid update
+// Momentum -> velocity of grid node i (block index `block`): the
+// compatible collider variants' momentum first (meld_grid.rs:29-58: bits 0 is
+// compatible with every variant), the fp64 sums on the way.
+__device__ __forceinline__ float4 grid_node(float4 g, uint64_t i, uint32_t block, const GridLayout &L,
+                                            const col::VariantTable &var, bool want_sums, double s[4]) {
+    int bx = 0, by = 0, bz = 0;
+    if (var.key || L.ground_mode != 0) block_coords(block, L, bx, by, bz);
+    const int l = (int)(i & 63);
+    const int x = L.origin[0] + 4 * bx + (l >> 4), y = L.origin[1] + 4 * by + ((l >> 2) & 3), z = L.origin[2] + 4 * bz + (l & 3);
+    if (var.key) {
+        const int64_t e = col::node_entry(var, x, y, z);
+        if (e >= 0)
+            for (int j = 0; j < col::VK; ++j)
+                if (var.bits[e * col::VK + j]) {
+                    const float4 a = var.acc[e * col::VK + j];
+                    g.x += a.x, g.y += a.y, g.z += a.z, g.w += a.w;
+                }
+    }
+    if (want_sums) s[0] += (double)g.w, s[1] += (double)g.x, s[2] += (double)g.y, s[3] += (double)g.z;
+    return node_velocity(g, x, y, z, L);
+}
+
 // Momentum -> velocity on grid_cur (slots of map `wc`), and zeroes grid_next
 // (slots of map `wn`) for the scatter that follows.  On the way it adds the
 // fp64 sums of mass and momentum over grid_cur's nodes (variants included)
 // into sums_cur -- from substep counters[C_SUMS_AT] on (sv_step sets it to
 // the last substep of the call: the fp64 work costs 7 % of a substep) --
-// and zeroes sums_next with grid_next.
-__global__ void __launch_bounds__(ELEM_THREADS)
+// and zeroes sums_next with grid_next.  Launched as one wave of resident
+// CTAs, each thread takes two nodes a stride apart with both loads in
+// flight: the 1M-particle scene's 0.3M nodes then take one pass of memory
+// latency instead of two waves of one node per thread.
+__global__ void __launch_bounds__(ELEM_THREADS, 4)
     k_grid_update(float4 *grid_cur, const uint32_t *active_cur, float4 *grid_next, uint64_t capacity, GridLayout L,
                   uint32_t *counters, int wc, int wn, col::VariantTable var, double *sums_cur, double *sums_next) {
     if (stopped(counters)) return;
@@ -435,37 +467,22 @@ __global__ void __launch_bounds__(ELEM_THREADS)
     if (sn > capacity) sn = capacity;
     if (grid_next && blockIdx.x == 0 && threadIdx.x < 4) sums_next[threadIdx.x] = 0.0;
     const bool want_sums = counters[C_SUBSTEPS] >= counters[C_SUMS_AT];
-    const uint64_t total = (sc > sn ? sc : sn) * 64;
-    double sm = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-        if (i < sc * 64) {
-            float4 g = grid_cur[i];
-            if (var.key) {
-                // meld_grid.rs:29-58: bits 0 is compatible with every variant
-                int bx, by, bz;
-                block_coords(active_cur[i >> 6], L, bx, by, bz);
-                const int l = (int)(i & 63);
-                const int64_t e = col::node_entry(var, L.origin[0] + 4 * bx + (l >> 4), L.origin[1] + 4 * by + ((l >> 2) & 3),
-                                                  L.origin[2] + 4 * bz + (l & 3));
-                if (e >= 0)
-                    for (int j = 0; j < col::VK; ++j)
-                        if (var.bits[e * col::VK + j]) {
-                            const float4 a = var.acc[e * col::VK + j];
-                            g.x += a.x, g.y += a.y, g.z += a.z, g.w += a.w;
-                        }
-            }
-            if (want_sums) sm += (double)g.w, sx += (double)g.x, sy += (double)g.y, sz += (double)g.z;
-            int x = 0, y = 0, z = 0;
-            if (L.ground_mode != 0) {
-                int bx, by, bz;
-                block_coords(active_cur[i >> 6], L, bx, by, bz);
-                const int l = (int)(i & 63);
-                x = L.origin[0] + 4 * bx + (l >> 4), y = L.origin[1] + 4 * by + ((l >> 2) & 3), z = L.origin[2] + 4 * bz + (l & 3);
-            }
-            grid_cur[i] = node_velocity(g, x, y, z, L);
-        }
-        if (i < sn * 64) grid_next[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool need_block = var.key || L.ground_mode != 0;
+    const uint64_t total = (sc > sn ? sc : sn) * 64, nc = sc * 64, nn = sn * 64;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += 2 * stride) {
+        const uint64_t j = i + stride;
+        const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 gi = i < nc ? grid_cur[i] : zero, gj = j < nc ? grid_cur[j] : zero;
+        const uint32_t bi = need_block && i < nc ? active_cur[i >> 6] : 0u;
+        const uint32_t bj = need_block && j < nc ? active_cur[j >> 6] : 0u;
+        if (i < nc) grid_cur[i] = grid_node(gi, i, bi, L, var, want_sums, s);
+        if (j < nc) grid_cur[j] = grid_node(gj, j, bj, L, var, want_sums, s);
+        if (i < nn) grid_next[i] = zero;
+        if (j < nn) grid_next[j] = zero;
     }
+    double sm = s[0], sx = s[1], sy = s[2], sz = s[3];
     if (!want_sums) return;  // uniform over the grid
     // The block's sum in fp64 with few fp64 instructions (about 16 clocks
     // per warp instruction on this part): every thread's partial sums go
@@ -845,6 +862,11 @@ __device__ __forceinline__ void cta_done(const StepArgs &A, uint32_t stop_at_sta
             if (!stop_at_start) A.counters[C_SUBSTEPS] += 1;
             A.counters[C_CTA_DONE] = 0;
             A.counters[C_DEFER] = 0;  // the fused pass's fp64 list has been served
+            if (A.pass_timer && !stop_at_start) {
+                // the plain fused pass and its fp64 pass, first CTA start to here
+                A.pass_timer[1] += global_ns() - A.pass_timer[0];
+                A.pass_timer[2] += 1;
+            }
         }
     }
 }
@@ -873,6 +895,8 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
     static_assert(!REDO || (MODE == MODE_G2P2G && !FIN), "the fp64 pass follows the plain fused pass");
     constexpr bool LEARNED = MODE == MODE_G2P2G_LEARNED;
     constexpr bool DEFER64 = MODE == MODE_G2P2G && !FIN && !REDO;
+    // the pass's start for its timer (CTA 0 is among the first to run)
+    if (DEFER64 && A.pass_timer && blockIdx.x == 0 && threadIdx.x == 0) A.pass_timer[0] = global_ns();
     // what the pass does: gather from the grid, advance the particles (and
     // write them out in sorted order), scatter into the next grid
     constexpr bool ADT_FUSED = MODE == MODE_G2P2G_ADAPTIVE;
@@ -1669,6 +1693,7 @@ StepArgs make_args(sv_handle *h, float dt, float3 g) {
     A.adt_pass = 0;
     A.keys_out = h->keys;
     A.defer_list = h->defer_list;
+    A.pass_timer = nullptr;
     A.closure_img = nullptr;
     A.closure_hull = nullptr;
     A.adt = nullptr;
@@ -2004,7 +2029,9 @@ cudaError_t launch_grid_update(sv_handle *h, bool clear_next, bool latch) {
                                                                                 h->counters);
         h->launches += 1;
     }
-    k_grid_update<<<elem_blocks(h->capacity * 64), ELEM_THREADS, 0, h->stream>>>(
+    const unsigned gu_blocks = (unsigned)std::min<uint64_t>((h->capacity * 64 + 2 * ELEM_THREADS - 1) / (2 * ELEM_THREADS),
+                                                           (uint64_t)sm_count() * 4);
+    k_grid_update<<<gu_blocks ? gu_blocks : 1, ELEM_THREADS, 0, h->stream>>>(
         h->grid[h->gcur], h->active[h->map_cur], clear_next ? h->grid[h->gcur ^ 1] : nullptr, h->capacity, h->layout,
         h->counters, h->map_cur, h->map_next, var, h->grid_sums + 4 * h->gcur, h->grid_sums + 4 * (h->gcur ^ 1));
     h->launches += 1;
@@ -2075,6 +2102,7 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 g, bool write_keys, bool
     } else if (!h->fin_active) {
         // the fused pass without fp64 code, then its fp64 pass, which
         // latches the stop bits for both (see k_particles)
+        A.pass_timer = h->pass_timer;
         StepArgs M = A;
         M.self_latch = false;
         launch_particles<MODE_G2P2G>(h, M);
