@@ -54,7 +54,8 @@ enum Counter : int {
     C_ADT_MISS = 14,     // adaptive substeps whose speculative steps failed (fused form)
     C_SUMS_AT = 15,      // the grid updates take the fp64 conservation sums from this substep on
     C_DEFER = 16,        // particles of this substep's fused pass left for its fp64 pass (defer_list)
-    C_COUNT = 17,
+    C_SEGQ = 17,         // next segment for the fused pass's CTAs to take
+    C_COUNT = 18,
 };
 
 // One side of the particle state (ping-pong).  Structure of arrays: pos and

@@ -862,6 +862,7 @@ __device__ __forceinline__ void cta_done(const StepArgs &A, uint32_t stop_at_sta
             if (!stop_at_start) A.counters[C_SUBSTEPS] += 1;
             A.counters[C_CTA_DONE] = 0;
             A.counters[C_DEFER] = 0;  // the fused pass's fp64 list has been served
+            A.counters[C_SEGQ] = 0;
             if (A.pass_timer && !stop_at_start) {
                 // the plain fused pass and its fp64 pass, first CTA start to here
                 A.pass_timer[1] += global_ns() - A.pass_timer[0];
@@ -1328,7 +1329,19 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
             chunk(slot < end ? A.defer_list[slot] : 0u, slot < end, (int)min((uint32_t)PT, end - c0), org);
         }
     } else {
-        for (uint32_t seg = blockIdx.x; seg < nseg; seg += gridDim.x) {
+        // The plain fused pass: one resident wave of CTAs takes segments
+        // from a queue, so segments of uneven size balance without the
+        // oversubscribed grid the other passes use (which pays each CTA's
+        // start and end per segment).
+        constexpr bool QUEUE = DEFER64;
+        __shared__ uint32_t next_seg;
+        uint32_t seg = blockIdx.x;
+        if (QUEUE) {
+            if (threadIdx.x == 0) next_seg = atomicAdd(&A.counters[C_SEGQ], 1u);
+            __syncthreads();
+            seg = next_seg;
+        }
+        while (seg < nseg) {
             const uint32_t b = A.seg_block[seg];
             const uint32_t start = A.seg_start[seg], end = A.seg_start[seg + 1];
             int bx, by, bz;
@@ -1356,6 +1369,14 @@ __global__ void __launch_bounds__(PT, MODE == MODE_G2P2G_LEARNED ? 3 : FIN ? 4 :
             }
             for (uint32_t c0 = start; c0 < end; c0 += PT)
                 chunk(c0 + threadIdx.x, c0 + threadIdx.x < end, (int)min((uint32_t)PT, end - c0), org);
+            if (QUEUE) {
+                // (every thread read next_seg before this segment's barriers)
+                if (threadIdx.x == 0) next_seg = atomicAdd(&A.counters[C_SEGQ], 1u);
+                __syncthreads();
+                seg = next_seg;
+            } else {
+                seg += gridDim.x;
+            }
             __syncthreads();
         }
     }
@@ -2105,7 +2126,7 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 g, bool write_keys, bool
         A.pass_timer = h->pass_timer;
         StepArgs M = A;
         M.self_latch = false;
-        launch_particles<MODE_G2P2G>(h, M);
+        launch_particles<MODE_G2P2G>(h, M, (unsigned)sm_count() * SV_PARTICLE_CTAS_PER_SM);
         if (h->layout.position_form) k_particles<true, MODE_G2P2G, false, true><<<sm_count(), PT, 0, h->stream>>>(A);
         else k_particles<false, MODE_G2P2G, false, true><<<sm_count(), PT, 0, h->stream>>>(A);
         h->stop_latched = A.self_latch;
