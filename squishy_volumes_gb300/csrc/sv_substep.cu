@@ -2121,8 +2121,9 @@ cudaError_t launch_g2p2g(sv_handle *h, float dt, float3 g, bool write_keys, bool
         A.closure_hull = reinterpret_cast<const closure::Hull *>(h->cl_hull);
         launch_particles<MODE_G2P2G_LEARNED>(h, A);
     } else if (!h->fin_active) {
-        // the fused pass without fp64 code, then its fp64 pass, which
-        // latches the stop bits for both (see k_particles)
+        // the fused pass without fp64 code, as one resident wave taking
+        // segments from the queue, then its fp64 pass, which latches the
+        // stop bits for both (see k_particles)
         A.pass_timer = h->pass_timer;
         StepArgs M = A;
         M.self_latch = false;
