@@ -254,7 +254,7 @@ typedef struct sv_stats {
     uint64_t sort_interval;     /* current substeps between binning sorts */
     uint64_t tile_misses;       /* gathers that missed their block's shared tile (low 32 bits) */
     uint64_t graph_replays;     /* binning periods run as CUDA graph replays */
-    uint64_t cta_per_sm;        /* CTAs per SM of the particle kernels */
+    uint64_t cta_per_sm;        /* CTAs per SM of the particle kernels other than the plain fused pass */
     uint64_t closure_learned;   /* snow/sand particle-substeps through the learned closure (low 32 bits) */
     uint64_t closure_fallbacks; /* of the learned mode's snow/sand particle-substeps: return-map fallbacks */
     uint64_t closure_mode;      /* 0 return maps, 1 learned closure */
@@ -367,7 +367,10 @@ int sv_get_stats(sv_handle *h, sv_stats *out);
  * another is more than 2 % faster.  The state is restored afterwards.  The
  * chosen values are written to the out pointers when not NULL.  One launch
  * covers all scenes of a batched handle, so these settings apply to all of
- * them alike. */
+ * them alike.  The plain fused pass of sv_step always runs as one resident
+ * wave taking segments from a queue; the CTAs-per-SM choice applies to the
+ * other particle passes (standalone scatter, adaptive, frame-input and
+ * learned forms). */
 int sv_autotune(sv_handle *h, float dt, const float gravity[3], uint32_t substeps_per_trial,
                 uint32_t *sort_interval_out, uint32_t *cta_per_sm_out);
 
