@@ -92,7 +92,7 @@ def parse():
     ap.add_argument("--closure-workload", default="snow_sand_2m",
                     help="also measure this workload with the learned closure against the return maps, reported "
                          "under 'closure_check' ('' for none; --closure learned measures the headline instead)")
-    ap.add_argument("--min-seconds", type=float, default=1.0,
+    ap.add_argument("--min-seconds", type=float, default=0.5,
                     help="repeat the K-substep timed region until the repeats cover this long; the median is reported")
     ap.add_argument("--max-repeats", type=int, default=2000)
     return ap.parse_args()
