@@ -151,7 +151,7 @@ int sv_create(const sv_consts *consts, const sv_particles *particles, sv_handle 
  * at a nonzero value the call stops (Harness::check, xpu/src/harness.rs:69-75)
  * and reports SV_STATUS_CANCELED.  Substeps are queued in chunks (16 when
  * `cancel` is given, 64 otherwise) and the host waits for each chunk by
- * polling it every 50 us, checking `cancel` meanwhile, like the reference's
+ * polling it (yielding between polls), checking `cancel` meanwhile, like the reference's
  * GPU backend waits (gpu_state.rs:509-522): a cancel set from another thread
  * during a call takes effect once the chunk in flight has completed, and the
  * state stays that of the last completed substep.  The number of substeps

@@ -563,9 +563,22 @@ void clear_graphs(sv_handle *h) {
 // the pointers and the host-side bookkeeping differ between configurations,
 // and those are in the key and the saved state.  `adaptive`: substeps of the
 // fused adaptive form, whose steps all come from the device (key dt -1).
-int run_period_graph(sv_handle *h, float dt, float3 g, bool adaptive = false) {
+// Runs `count` substeps (whole binning periods by default) as one CUDA graph,
+// captured on first use for the host state they start from.
+int run_period_graph(sv_handle *h, float dt, float3 g, bool adaptive = false, uint32_t count = 0) {
     auto substep = [&]() { return adaptive ? adaptive_substep_fused(h, g) : fused_substep(h, dt, g); };
-    sv_handle::GraphKey key{h->cur, h->gcur, h->map_cur, h->sort_interval, adaptive ? -1.f : dt, {g.x, g.y, g.z}};
+    sv_handle::GraphKey key{h->cur,
+                            h->gcur,
+                            h->map_cur,
+                            h->map_next,
+                            h->sort_interval,
+                            std::min(h->since_sort, h->sort_interval),
+                            count ? count : h->sort_interval,
+                            h->keys_valid,
+                            h->need_perm,
+                            h->stop_latched,
+                            adaptive ? -1.f : dt,
+                            {g.x, g.y, g.z}};
     auto it = h->graphs.find(key);
     if (it == h->graphs.end()) {
         // host bookkeeping before the period, put back if the capture fails
@@ -579,7 +592,7 @@ int run_period_graph(sv_handle *h, float dt, float3 g, bool adaptive = false) {
         cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
             int rc = 0;
-            for (uint32_t s = 0; s < key.period && rc == 0; ++s) rc = substep();
+            for (uint32_t s = 0; s < key.count && rc == 0; ++s) rc = substep();
             e = cudaStreamEndCapture(h->stream, &graph);
             if (rc && e == cudaSuccess) e = cudaErrorStreamCaptureInvalidated;
             if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
@@ -596,7 +609,7 @@ int run_period_graph(sv_handle *h, float dt, float3 g, bool adaptive = false) {
             h->stop_latched = stop_latched0;
             h->launches = l0, h->sorts = sorts0;
             h->use_graphs = false;
-            for (uint32_t s = 0; s < key.period; ++s)
+            for (uint32_t s = 0; s < key.count; ++s)
                 if (substep()) return -1;
             return 0;
         }
@@ -607,9 +620,10 @@ int run_period_graph(sv_handle *h, float dt, float3 g, bool adaptive = false) {
         st.keys_valid = h->keys_valid, st.need_perm = h->need_perm, st.since_sort = h->since_sort;
         st.stop_latched = h->stop_latched;
         st.launches = h->launches - l0;
+        st.sorts = h->sorts - sorts0;
         it = h->graphs.emplace(key, st).first;
         h->launches = l0;
-        h->sorts -= 1;  // counted again below, like a replay
+        h->sorts = sorts0;  // counted again below, like a replay
     }
     const sv_handle::GraphState &st = it->second;
     SV_CUDA(cudaGraphLaunch(st.exec, h->stream));
@@ -618,7 +632,7 @@ int run_period_graph(sv_handle *h, float dt, float3 g, bool adaptive = false) {
     h->keys_valid = st.keys_valid, h->need_perm = st.need_perm, h->since_sort = st.since_sort;
     h->stop_latched = st.stop_latched;
     h->launches += st.launches;
-    h->sorts += 1;
+    h->sorts += st.sorts;
     h->graph_launches += 1;
     return 0;
 }
@@ -639,12 +653,15 @@ int read_counters_polled(sv_handle *h, const volatile int32_t *cancel, bool *can
     SV_CUDA(cudaMemcpyAsync(h->host_counters, h->counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
     if (!h->wait_event) SV_CUDA(cudaEventCreateWithFlags(&h->wait_event, cudaEventDisableTiming));
     SV_CUDA(cudaEventRecord(h->wait_event, h->stream));
+    // The GPU idles from the end of the queued work until the caller queues
+    // more, so the wait polls without sleeping (a 50 us sleep cost up to
+    // 2 % of a 20-substep call); yielding leaves the core to other threads.
     while (true) {
         const cudaError_t q = cudaEventQuery(h->wait_event);
         if (q == cudaSuccess) break;
         if (q != cudaErrorNotReady) SV_CUDA(q);
         if (cancel && *cancel && canceled) *canceled = true;
-        std::this_thread::sleep_for(std::chrono::microseconds(50));
+        std::this_thread::yield();
     }
     if (cancel && *cancel && canceled) *canceled = true;
     return 0;
@@ -991,12 +1008,19 @@ int sv_step(sv_handle *h, uint32_t n_substeps, float dt, const float gravity[3],
         }
         double t_q = h->time;  // start time of the substep after the one launched
         for (uint32_t s = 0; s < todo;) {
-            // whole binning periods go through CUDA graphs once the binning
-            // keys come from the previous substep (steady state)
-            if (h->use_graphs && !h->fin_active && !h->deterministic && !h->profiling && h->since_sort >= h->sort_interval &&
-                h->keys_valid && todo - s >= h->sort_interval) {
-                if (run_period_graph(h, dt, g)) return -1;
-                s += h->sort_interval;
+            // CUDA graphs: whole binning periods once the binning keys come
+            // from the previous substep (steady state), and the start or the
+            // rest of a period where the call's substep count cuts one (a
+            // 20-substep call with binning every 8 replays 8 + 8 + 4, then
+            // 4 + 8 + 8 in the next call)
+            if (h->use_graphs && !h->fin_active && !h->deterministic && !h->profiling &&
+                (h->since_sort < h->sort_interval || h->keys_valid)) {
+                const uint32_t left = todo - s;
+                const uint32_t count = h->since_sort >= h->sort_interval
+                                           ? std::min(h->sort_interval, left)
+                                           : std::min(h->sort_interval - h->since_sort, left);
+                if (run_period_graph(h, dt, g, false, count)) return -1;
+                s += count;
             } else {
                 t_q += (double)dt;
                 if (fused_substep(h, dt, g, t_q)) return -1;

@@ -213,13 +213,20 @@ struct sv_handle {
 
     // CUDA graphs of one binning period (a binning substep and the substeps
     // up to the next binning), keyed by everything their launches bake in.
+    // A run of `count` substeps captured from host state (cur, gcur, map_cur,
+    // map_next, since_sort, keys_valid, need_perm, stop_latched) with the
+    // binning interval `period`: whole binning periods, or the part of one
+    // that a call's substep count leaves.
     struct GraphKey {
-        int cur, gcur, map_cur;
-        uint32_t period;
+        int cur, gcur, map_cur, map_next;
+        uint32_t period, since_sort, count;
+        bool keys_valid, need_perm, stop_latched;
         float dt, g[3];
         bool operator<(const GraphKey &o) const {
-            return std::tie(cur, gcur, map_cur, period, dt, g[0], g[1], g[2]) <
-                   std::tie(o.cur, o.gcur, o.map_cur, o.period, o.dt, o.g[0], o.g[1], o.g[2]);
+            return std::tie(cur, gcur, map_cur, map_next, period, since_sort, count, keys_valid, need_perm, stop_latched, dt,
+                            g[0], g[1], g[2]) < std::tie(o.cur, o.gcur, o.map_cur, o.map_next, o.period, o.since_sort,
+                                                         o.count, o.keys_valid, o.need_perm, o.stop_latched, o.dt, o.g[0],
+                                                         o.g[1], o.g[2]);
         }
     };
     struct GraphState {  // host-side state after the period
@@ -227,7 +234,7 @@ struct sv_handle {
         int cur, gcur, map_cur, map_next, vel_side, vel_map;
         bool keys_valid, need_perm, stop_latched;
         uint32_t since_sort;
-        uint64_t launches;
+        uint64_t launches, sorts;
     };
     std::map<GraphKey, GraphState> graphs;
     bool use_graphs = true;
