@@ -646,9 +646,9 @@ int read_counters(sv_handle *h) {
 // The same read for the substep loops, waiting like the reference's GPU
 // backend (gpu_state.rs:509-522 polls its device every 100 ms and checks the
 // harness in between): the queued work cannot be recalled, so the wait
-// polls the copy's event every 50 us and notes a cancel request seen
-// meanwhile in *canceled; the caller stops queueing once the chunk in
-// flight has completed.
+// polls the copy's event and notes a cancel request seen meanwhile in
+// *canceled; the caller stops queueing once the chunk in flight has
+// completed.
 int read_counters_polled(sv_handle *h, const volatile int32_t *cancel, bool *canceled) {
     SV_CUDA(cudaMemcpyAsync(h->host_counters, h->counters, C_COUNT * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
     if (!h->wait_event) SV_CUDA(cudaEventCreateWithFlags(&h->wait_event, cudaEventDisableTiming));
