@@ -580,6 +580,14 @@ int run_period_graph(sv_handle *h, float dt, float3 g, bool adaptive = false, ui
                             adaptive ? -1.f : dt,
                             {g.x, g.y, g.z}};
     auto it = h->graphs.find(key);
+    if (it == h->graphs.end() && key.count != key.period && h->partial_seen.insert(key).second) {
+        // A part of a period is captured only when it recurs (a caller's
+        // fixed substep count): a one-off part would pay its capture and
+        // instantiation for nothing.
+        for (uint32_t s = 0; s < key.count; ++s)
+            if (substep()) return -1;
+        return 0;
+    }
     if (it == h->graphs.end()) {
         // host bookkeeping before the period, put back if the capture fails
         const int cur0 = h->cur, gcur0 = h->gcur, map_cur0 = h->map_cur, map_next0 = h->map_next;

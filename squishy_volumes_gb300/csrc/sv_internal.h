@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <map>
+#include <set>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -237,6 +238,7 @@ struct sv_handle {
         uint64_t launches, sorts;
     };
     std::map<GraphKey, GraphState> graphs;
+    std::set<GraphKey> partial_seen;  // partial periods run once directly, captured when they recur
     bool use_graphs = true;
     uint64_t graph_launches = 0;  // graph replays issued
 
