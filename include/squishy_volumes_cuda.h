@@ -358,9 +358,10 @@ int sv_set_host_transfer(sv_handle *h, uint32_t mode, uint32_t *direct);
 int sv_prepare_host(void *const *arrays, const uint64_t *bytes, uint32_t count);
 int sv_get_stats(sv_handle *h, sv_stats *out);
 
-/* Addition: picks the substeps between binning sorts (2, 4, 8, 16) and the
- * CTAs per SM of the particle kernels (8, 16, 32, 64) by timing each
- * candidate from a snapshot of the current state: two binning periods of
+/* Addition: picks the substeps between binning sorts (2, 4, 6, 8, 12, 16, at
+ * the handle's CTAs per SM) and then the CTAs per SM of the particle kernels
+ * (8, 16, 32, 64, at the chosen interval) by timing each candidate from a
+ * snapshot of the current state: two binning periods of
  * warm-up (first scatter, graph capture, steady binning), then three repeats
  * of at least max(substeps_per_trial, 48) substeps, ranked by the median
  * repeat.  The handle's own configuration is a candidate and is kept unless

@@ -1544,17 +1544,24 @@ int sv_autotune(sv_handle *h, float dt, const float gravity[3], uint32_t substep
     struct Cand {
         uint32_t si, cta;
     };
+    // Two stages: the binning interval at the handle's CTAs per SM, then the
+    // CTAs per SM at the best interval (the plain fused pass runs as one
+    // resident wave whatever that setting is; the other passes use it).
     std::vector<Cand> cands = {{si0, cta0}};
-    for (uint32_t si : {2u, 4u, 8u, 16u})
-        for (uint32_t cta : {8u, 16u, 32u, 64u})
-            if (si != si0 || cta != cta0) cands.push_back({si, cta});
+    for (uint32_t si : {2u, 4u, 6u, 8u, 12u, 16u})
+        if (si != si0) cands.push_back({si, cta0});
+    const size_t stage1 = cands.size();
     const uint32_t trial = std::max<uint32_t>(substeps_per_trial, 48);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0), cudaEventCreate(&e1);
     h->adaptive_interval = false;
     double ms_default = 0.0, best_ms = 1e300;
     uint32_t best_si = si0, best_cta = cta0;
-    for (size_t ci = 0; ci < cands.size(); ++ci) {
+    for (size_t ci = 0;; ++ci) {
+        if (ci == stage1)
+            for (uint32_t cta : {8u, 16u, 32u, 64u})
+                if (cta != cta0) cands.push_back({best_si, cta});
+        if (ci >= cands.size()) break;
         const Cand c = cands[ci];
         restore();
         clear_graphs(h);
