@@ -875,6 +875,8 @@ int create_impl(const sv_consts *cs, const sv_particles *ps, uint32_t n_scenes, 
                                                                              m.initial_volume, 1.f, L.dx);
     h->host_materials = mats;
     h->host_scenes = scenes;
+    h->kind_set = 0;
+    for (const Material &m : mats) h->kind_set |= 1u << m.kind;
     // blocks claimed are about n / 200 for bodies of 8 particles per cell;
     // n / 16 leaves room for sparse ones, and sv_step doubles it on overflow
     uint64_t cap = c.block_capacity ? c.block_capacity : std::min<uint64_t>(total, std::max<uint64_t>(65536, n / 16));

@@ -136,6 +136,7 @@ struct sv_handle {
     uint32_t *sorted_keys = nullptr;  // [n]
     uint32_t *perm = nullptr;         // [n] device slot of each sorted position
     uint32_t *defer_list = nullptr;   // [n] sorted positions the fused pass left for its fp64 pass
+    uint32_t kind_set = 0x1F;         // 1 << kind of every material in use
     void *sort_temp = nullptr;
     size_t sort_temp_bytes = 0;
 
