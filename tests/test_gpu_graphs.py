@@ -47,6 +47,34 @@ def test_graph_replay_matches_direct_launches(cuda_lib, oracle_mod, form):
     graphs.close(), direct.close()
 
 
+@pytest.mark.parametrize("form", [0, 1])
+def test_partial_periods_replay_like_direct_launches(cuda_lib, form):
+    """Calls of 3 substeps with binning every 4 cut every binning period:
+    each call replays the rest of one period and the start of the next as
+    graphs keyed by where the period stands (captured when a part recurs).
+    The result must be what launching the same kernels one by one gives."""
+    s = scenes.small_mixed()
+    calls, k = 20, 3
+    graphs = CudaState.from_io_state(s.io_state, s.consts, Extras(sort_interval=4, position_form=form))
+    direct = CudaState.from_io_state(s.io_state, s.consts, Extras(sort_interval=4, position_form=form))
+    direct.set_graphs(False)
+    for _ in range(calls):
+        assert graphs.step(k, s.dt, s.gravity) == (0, k)
+        assert direct.step(k, s.dt, s.gravity) == (0, k)
+    sg, sd = graphs.stats(), direct.stats()
+    assert sg["substeps"] == sd["substeps"] == calls * k
+    # no call holds a whole period, so every replay is of a part of one;
+    # the host state repeats every 8 calls, so parts recur within 20
+    assert sg["graph_replays"] > 0
+    assert sg["sorts"] == sd["sorts"]
+    assert sg["kernel_launches"] == sd["kernel_launches"]
+    a, b = graphs.download(), direct.download()
+    np.testing.assert_array_equal(a.flags, b.flags)
+    live = (b.flags & SV_TOMBSTONED) == 0
+    compare_states(a, b, live, tol={"positions": 1e-6, "velocities": 1e-5, "position_gradients": 1e-6})
+    graphs.close(), direct.close()
+
+
 def test_graphs_follow_changing_inputs(cuda_lib):
     """A new dt or gravity is a new graph: the result still follows the
     inputs of each call."""
