@@ -198,7 +198,12 @@ def test_substeps_match_oracle(cuda_lib, oracle_mod, fp64, sort_interval):
     np.testing.assert_array_equal(out.flags, exp.flags)
     live = (exp.flags & SV_TOMBSTONED) == 0
     compare_states(out, exp, live, dx=s.consts.grid_node_size)
-    np.testing.assert_allclose(out.plastic_j, exp.plastic_j, rtol=1e-5)
+    # Snow's plastic J multiplies each substep's volume change, and its
+    # hardening exp(10 (1 - J_p)) feeds back into the stress, so the float
+    # atomics' summation order (which differs from run to run) moves single
+    # particles by up to about 1e-5 against the fp32 oracle after these 10
+    # substeps (1.04e-5 seen once in about 25 runs).
+    np.testing.assert_allclose(out.plastic_j, exp.plastic_j, rtol=3e-5 if not fp64 else 1e-5)
     gpu.close()
 
 
