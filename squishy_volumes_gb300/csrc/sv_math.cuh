@@ -152,8 +152,11 @@ __device__ __forceinline__ void svd3(const Mat3<T> &F, Mat3<T> &U, T S[3], Mat3<
 // in closed form after each rotation (|a_p|^2 -= t g, |a_q|^2 += t g), the
 // rotation uses fast reciprocal / square-root intrinsics (any angle close to
 // the optimal one still reduces the off-diagonal, and c^2 + s^2 = 1 keeps V
-// orthogonal), and sweeps stop once every pair is orthogonal to 1e-6
-// relative -- below fp32 resolution of the products formed from the result.
+// orthogonal), and sweeps stop after one that started with every pair's
+// cos^2 below 1e-9: in cyclic Jacobi's quadratic regime that sweep leaves
+// them near 1e-18, under the rotation threshold below, and a further sweep
+// would rotate nothing.  (Stopping only after a sweep that started
+// below 1e-12 ran that idle sweep: 0.9 % of the 1M three-box fused pass.)
 // A pair already orthogonal to fp32 epsilon is left alone (the reference
 // test of one-sided Jacobi): near-identity F then gives U = V = I up to
 // rounding instead of the arbitrary 45-degree rotations of a degenerate
@@ -198,7 +201,7 @@ __device__ __forceinline__ bool svd3_fast_f32(const m3f &F, m3f &U, float S[3], 
                 nrm[q] = nq + t * g;
             }
         }
-        if (off < 1e-12f) break;
+        if (off < 1e-9f) break;
     }
     bool good[3];
 #pragma unroll
