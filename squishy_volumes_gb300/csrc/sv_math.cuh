@@ -174,13 +174,13 @@ __device__ __forceinline__ bool svd3_fast_f32(const m3f &F, m3f &U, float S[3], 
 #pragma unroll
     for (int c = 0; c < 3; ++c) nrm[c] = A[c * 3] * A[c * 3] + A[c * 3 + 1] * A[c * 3 + 1] + A[c * 3 + 2] * A[c * 3 + 2];
     for (int sweep = 0; sweep < 6; ++sweep) {
-        float off = 0.f;
+        bool last = true;  // every pair's cos^2 below 1e-9 at the start of its rotation
 #pragma unroll
         for (int pq = 0; pq < 3; ++pq) {
             const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
             const float g = A[p * 3] * A[q * 3] + A[p * 3 + 1] * A[q * 3 + 1] + A[p * 3 + 2] * A[q * 3 + 2];
             const float np = nrm[p], nq = nrm[q];
-            off = fmaxf(off, __fdividef(g * g, fmaxf(np * nq, 1e-30f)));
+            last = last && g * g < 1e-9f * fmaxf(np * nq, 1e-30f);
             if (g * g > EPS2 * np * nq) {
                 const float d = nq - np, e = 2.f * g;
                 const float r2 = d * d + e * e;
@@ -201,7 +201,7 @@ __device__ __forceinline__ bool svd3_fast_f32(const m3f &F, m3f &U, float S[3], 
                 nrm[q] = nq + t * g;
             }
         }
-        if (off < 1e-9f) break;
+        if (last) break;
     }
     bool good[3];
 #pragma unroll
